@@ -1,0 +1,256 @@
+"""ctypes binding of the native library ``libplgpu_fem3d.so`` (include/plgpu_fem3d.h).
+
+The library is the only compute path: importing this module fails loudly when
+it is missing or cannot be loaded, and every call checks the returned status
+and raises with the handle's error text.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+_LIB_PATH = pathlib.Path(__file__).resolve().parent / "lib" / "libplgpu_fem3d.so"
+
+OK = 0
+ERR_ARG, ERR_CUDA, ERR_NOT_SPD, ERR_NOCONV, ERR_STATE, ERR_NONFINITE = -1, -2, -3, -4, -5, -6
+
+ORDERS = {"012": 0, "021": 1, "102": 2, "120": 3, "201": 4, "210": 5}
+BC_TEMPERATURE, BC_HEATFLUX, BC_CONVECTION, BC_RADIATION = 0, 1, 2, 3
+ALGORITHMS = {"cholesky": 0, "gauss": 1, "iterative": 2, "gpu-pcg": 3, "gpu-mixed": 4, "gpu-learned": 5}
+NOCONV = {"error": 0, "warning": 1, "continue": 2}
+EMPTY = {"default": 0, "exclude": 1, "excluded": 1, "include": 2, "included": 2}
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("loops", C.c_int),
+        ("total_loops", C.c_int),
+        ("inner_iterations", C.c_int),
+        ("refinements", C.c_int),
+        ("converged", C.c_int),
+        ("fallbacks", C.c_int),
+        ("err", C.c_double),
+        ("toterr", C.c_double),
+        ("max_t", C.c_double),
+        ("last_rel_residual", C.c_double),
+        ("solve_ms", C.c_double),
+        ("total_ms", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+LOG_CB = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_char_p)
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_lp = C.POINTER(C.c_int64)
+_up = C.POINTER(C.c_uint8)
+_h = C.c_void_p
+
+# name -> (restype, argtypes); every entry point declared in include/plgpu_fem3d.h
+SIGNATURES = {
+    "plgpu_fem3d_create": (C.c_int, [_dp, C.c_int, _dp, C.c_int, _dp, C.c_int, C.c_int, C.POINTER(_h)]),
+    "plgpu_fem3d_destroy": (C.c_int, [_h]),
+    "plgpu_fem3d_last_error": (C.c_char_p, [_h]),
+    "plgpu_fem3d_set_materials": (C.c_int, [_h, C.c_int, _dp, _dp, _dp, _dp, _up]),
+    "plgpu_fem3d_set_elements": (C.c_int, [_h, _ip, _dp, _dp]),
+    "plgpu_fem3d_set_heat": (C.c_int, [_h, _dp]),
+    "plgpu_fem3d_clear_bc": (C.c_int, [_h, C.c_int]),
+    "plgpu_fem3d_add_bc": (C.c_int, [_h, C.c_int, _lp, C.c_size_t, C.c_double, C.c_double]),
+    "plgpu_fem3d_set_solver": (C.c_int, [_h, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "plgpu_fem3d_set_loop": (C.c_int, [_h, C.c_double, C.c_double]),
+    "plgpu_fem3d_compute": (C.c_int, [_h, C.c_int, _dp, C.POINTER(Stats)]),
+    "plgpu_fem3d_invalidate": (C.c_int, [_h]),
+    "plgpu_fem3d_sizes": (C.c_int, [_h, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "plgpu_fem3d_get_temperature": (C.c_int, [_h, _dp]),
+    "plgpu_fem3d_set_temperature": (C.c_int, [_h, _dp]),
+    "plgpu_fem3d_get_heat_flux": (C.c_int, [_h, _dp]),
+    "plgpu_fem3d_get_conductivity": (C.c_int, [_h, _dp]),
+    "plgpu_fem3d_get_thickness": (C.c_int, [_h, _dp]),
+    "plgpu_fem3d_stream": (C.c_void_p, [_h]),
+    "plgpu_fem3d_set_log_callback": (C.c_int, [_h, LOG_CB, C.c_void_p]),
+}
+
+_lib = None
+
+
+def library_path():
+    return _LIB_PATH
+
+
+def load():
+    """Load the native library (building it first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not _LIB_PATH.exists():
+        from . import build as _build
+
+        _build.build()
+    if not _LIB_PATH.exists():
+        raise RuntimeError(f"native library {_LIB_PATH} is missing; run python -m plask_gb300.build")
+    lib = C.CDLL(str(_LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class NativeError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class ComputationError(NativeError):
+    """Linear-solve failure (non-SPD breakdown, no convergence with noconv=error, NaN)."""
+
+
+class BadInput(NativeError, ValueError):
+    """Invalid argument passed to the solver."""
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct)) if a is not None else None
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64) if a is not None else None
+
+
+class Fem3D:
+    """Owning wrapper of one ``plgpu_fem3d`` handle.
+
+    Arrays exchanged with it use the mesh iteration order given at creation.
+    """
+
+    def __init__(self, axes, ordering="012"):
+        lib = load()
+        self._lib = lib
+        ax = [_f64(a) for a in axes]
+        h = _h()
+        rc = lib.plgpu_fem3d_create(_ptr(ax[0], C.c_double), len(ax[0]), _ptr(ax[1], C.c_double), len(ax[1]),
+                                    _ptr(ax[2], C.c_double), len(ax[2]), ORDERS[ordering], C.byref(h))
+        if rc != OK:
+            msg = lib.plgpu_fem3d_last_error(None)
+            raise (BadInput if rc == ERR_ARG else NativeError)(rc, (msg or b"").decode())
+        self._h = h
+        self.shape = tuple(len(a) for a in ax[::-1])
+        self.ordering = ordering
+        self._log_cb = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.plgpu_fem3d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc == OK:
+            return
+        msg = (self._lib.plgpu_fem3d_last_error(self._h) or b"").decode()
+        if rc == ERR_ARG:
+            raise BadInput(rc, msg)
+        if rc in (ERR_NOT_SPD, ERR_NOCONV, ERR_NONFINITE):
+            raise ComputationError(rc, msg)
+        raise NativeError(rc, msg)
+
+    def set_log_callback(self, fn):
+        """fn(level, message) receives the solver's log lines."""
+        if fn is None:
+            self._log_cb = None
+            self._check(self._lib.plgpu_fem3d_set_log_callback(self._h, LOG_CB(), None))
+            return
+        cb = LOG_CB(lambda user, level, msg: fn(level, msg.decode()))
+        self._log_cb = cb
+        self._check(self._lib.plgpu_fem3d_set_log_callback(self._h, cb, None))
+
+    def set_materials(self, k300, p, kz_ratio=None, hexp=None, empty=None):
+        k300, p = _f64(k300), _f64(p)
+        kz, he = _f64(kz_ratio), _f64(hexp)
+        em = np.ascontiguousarray(empty, dtype=np.uint8) if empty is not None else None
+        self._check(self._lib.plgpu_fem3d_set_materials(self._h, len(k300), _ptr(k300, C.c_double), _ptr(p, C.c_double),
+                                                        _ptr(kz, C.c_double), _ptr(he, C.c_double),
+                                                        _ptr(em, C.c_uint8)))
+
+    def set_elements(self, material, heat=None, leaf_height=None):
+        m = np.ascontiguousarray(material, dtype=np.int32).ravel()
+        q, lh = _f64(heat), _f64(leaf_height)
+        self._check(self._lib.plgpu_fem3d_set_elements(self._h, _ptr(m, C.c_int32), _ptr(q, C.c_double),
+                                                       _ptr(lh, C.c_double)))
+
+    def set_heat(self, heat):
+        q = _f64(heat)
+        self._check(self._lib.plgpu_fem3d_set_heat(self._h, _ptr(q, C.c_double)))
+
+    def clear_bc(self, kind):
+        self._check(self._lib.plgpu_fem3d_clear_bc(self._h, kind))
+
+    def add_bc(self, kind, nodes, v0, v1=0.0):
+        nd = np.ascontiguousarray(nodes, dtype=np.int64).ravel()
+        self._check(self._lib.plgpu_fem3d_add_bc(self._h, kind, _ptr(nd, C.c_int64), nd.size, float(v0), float(v1)))
+
+    def set_solver(self, algorithm="iterative", rtol=1e-14, maxit=0, noconv="warning", empty_elements="default",
+                   bc_compat=True):
+        self._check(self._lib.plgpu_fem3d_set_solver(self._h, ALGORITHMS[algorithm], float(rtol), int(maxit),
+                                                     NOCONV[noconv], EMPTY[empty_elements], 1 if bc_compat else 0))
+
+    def set_loop(self, inittemp=300.0, maxerr=0.05):
+        self._check(self._lib.plgpu_fem3d_set_loop(self._h, float(inittemp), float(maxerr)))
+
+    def compute(self, loops=0):
+        """Run compute(loops); returns (toterr, stats dict)."""
+        tot = C.c_double(0.0)
+        st = Stats()
+        self._check(self._lib.plgpu_fem3d_compute(self._h, int(loops), C.byref(tot), C.byref(st)))
+        return tot.value, st.as_dict()
+
+    def invalidate(self):
+        self._check(self._lib.plgpu_fem3d_invalidate(self._h))
+
+    def sizes(self):
+        nn, ne = C.c_size_t(0), C.c_size_t(0)
+        self._check(self._lib.plgpu_fem3d_sizes(self._h, C.byref(nn), C.byref(ne)))
+        return nn.value, ne.value
+
+    def temperature(self, out=None):
+        nn, _ = self.sizes()
+        out = np.empty(nn) if out is None else out
+        self._check(self._lib.plgpu_fem3d_get_temperature(self._h, _ptr(out, C.c_double)))
+        return out
+
+    def set_temperature(self, values):
+        v = _f64(values).ravel()
+        self._check(self._lib.plgpu_fem3d_set_temperature(self._h, _ptr(v, C.c_double)))
+
+    def heat_flux(self):
+        _, ne = self.sizes()
+        out = np.empty((ne, 3))
+        self._check(self._lib.plgpu_fem3d_get_heat_flux(self._h, _ptr(out, C.c_double)))
+        return out
+
+    def conductivity(self):
+        _, ne = self.sizes()
+        out = np.empty((ne, 2))
+        self._check(self._lib.plgpu_fem3d_get_conductivity(self._h, _ptr(out, C.c_double)))
+        return out
+
+    def thickness(self):
+        _, ne = self.sizes()
+        out = np.empty(ne)
+        self._check(self._lib.plgpu_fem3d_get_thickness(self._h, _ptr(out, C.c_double)))
+        return out
+
+    def stream(self):
+        return self._lib.plgpu_fem3d_stream(self._h)

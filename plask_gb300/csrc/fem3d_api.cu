@@ -1,0 +1,1172 @@
+// Host driver of the Static3D GPU solver and its C ABI (include/plgpu_fem3d.h).
+//
+// The handle mirrors the state PLaSK's ThermalFem3DSolver keeps between calls
+// (solvers/thermal/static/therm3d.hpp:31-39): the temperature field persists on
+// the device across compute() calls and is reset by invalidate().  Boundary
+// conditions are materialised once per change into compact device lists; the
+// volume operator is applied matrix-free from per-element conductivities.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/plgpu_fem3d.h"
+#include "fem3d_device.cuh"
+#include "fem3d_kernels.h"
+
+using namespace plgpu;
+
+namespace {
+
+constexpr double kSB = 5.670373e-8;  // plask/phys/constants.hpp:41
+constexpr int kMaxOuterLoops = 100000;
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct ArgError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct StateError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct SolveError : std::runtime_error {
+    int code;
+    SolveError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+inline void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// RAII device allocation
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void alloc(size_t nbytes) {
+        if (nbytes == bytes && p) return;
+        release();
+        if (nbytes == 0) return;
+        ck(cudaMalloc(&p, nbytes), "cudaMalloc");
+        bytes = nbytes;
+    }
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+template <typename T>
+void upload(DevBuf& d, const std::vector<T>& v, cudaStream_t s) {
+    d.alloc(v.size() * sizeof(T));
+    if (!v.empty()) ck(cudaMemcpyAsync(d.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
+}
+
+}  // namespace
+
+struct plgpu_fem3d {
+    std::string err;
+    // mesh
+    int n[3] = {0, 0, 0};
+    long long N = 0, NE = 0;
+    int ordering = PLGPU_ORDER_012;
+    int major = 0, medium = 1, minor = 2;
+    long long ns[3] = {0, 0, 0};  // mesh-order node strides of axes 0/1/2
+    long long es[3] = {0, 0, 0};  // mesh-order element strides
+    std::vector<double> ax[3];
+    cudaStream_t stream = nullptr;
+    LaunchCfg cfg{};
+    int sm_count = 0;
+
+    DevBuf h64[3], r64[3], h32[3], r32[3], z64;
+    GridT<double> g64{};
+    GridT<float> g32{};
+
+    // materials
+    int n_mat = 0;
+    std::vector<double> k300, pexp, kzr, hexp;
+    std::vector<uint8_t> empty;
+    bool aniso = false;
+    DevBuf d_k300, d_p, d_kzr, d_hexp, d_excl;
+    MatTable tab{};
+
+    // elements (canonical padded layout)
+    std::vector<int32_t> host_mat;  // mesh element order
+    DevBuf d_mat, d_heat, d_th, d_hleaf;
+    bool have_elements = false, have_leaf = false, heat_dirty = true;
+
+    // fields
+    DevBuf T, T0, F, b, r64v, vD, diag, minv64, minv32, k64, k32, kz64, kz32;
+    DevBuf p64, q64, x32, r32v, p32, q32;
+    DevBuf partials, d_ctl;
+    SolveCtl* h_ctl = nullptr;
+
+    // boundary conditions as appended
+    struct Cond {
+        std::vector<int64_t> nodes;  // mesh-order node indices
+        double v0, v1;
+    };
+    std::vector<Cond> bcs[4];
+    bool bc_dirty = true;
+
+    // materialised boundary conditions
+    int nD = 0;
+    DevBuf d_didx, d_dval, dmask, inactive_mask;
+    bool any_inactive = false;
+    SurfaceT<double> s64{};
+    SurfaceT<float> s32{};
+    DevBuf s_row, s_ptr, s_col, s_val64, s_val32;
+    int rad_rows = 0;
+    DevBuf rad_row, rad_ptr, rad_src, rad_coef, rad_tamb;
+    int n_fbc = 0;
+    DevBuf fbc_idx, fbc_val;
+
+    // masked numbering
+    bool masked = false;
+    long long n_active = 0;
+    DevBuf d_active;                    // canonical index of every masked node, mesh order
+    std::vector<long long> h_active;    // same, host
+    std::vector<int64_t> h_canon2mask;  // canonical -> masked id (-1 inactive); only when masked
+
+    // parameters
+    int algorithm = PLGPU_ALGO_ITERATIVE;
+    double rtol = 1e-14;
+    int maxit = 0;  // 0: automatic cap
+    int noconv = PLGPU_NOCONV_WARNING;
+    int empty_mode = PLGPU_EMPTY_DEFAULT;
+    int bc_compat = 1;
+    double inittemp = 300.0, maxerr = 0.05;
+    double inner_rtol = 1e-4;
+    int chunk = 32;
+
+    bool initialized = false;
+    int loopno = 0;
+    bool converged = true;
+    void (*log_cb)(void*, int, const char*) = nullptr;
+    void* log_user = nullptr;
+
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+
+    ~plgpu_fem3d() {
+        if (h_ctl) cudaFreeHost(h_ctl);
+        for (cudaEvent_t e : {ev0, ev1, ev2, ev3})
+            if (e) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    void log(int level, const char* fmt, ...) {
+        if (!log_cb) return;
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        log_cb(log_user, level, buf);
+    }
+
+    // ---------------------------------------------------------------------------------
+    // mesh
+
+    void setup_mesh(const double* a0, int n0, const double* a1, int n1, const double* a2, int n2, int ord) {
+        const double* a[3] = {a0, a1, a2};
+        const int nn[3] = {n0, n1, n2};
+        for (int d = 0; d < 3; ++d) {
+            if (!a[d] || nn[d] < 2) throw ArgError("every axis needs at least 2 nodes");
+            ax[d].assign(a[d], a[d] + nn[d]);
+            for (int i = 1; i < nn[d]; ++i)
+                if (!(ax[d][i] > ax[d][i - 1])) throw ArgError("axis coordinates must be strictly increasing");
+            n[d] = nn[d];
+        }
+        if (ord < 0 || ord > 5) throw ArgError("unknown iteration order");
+        static const int orders[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+        ordering = ord;
+        major = orders[ord][0];
+        medium = orders[ord][1];
+        minor = orders[ord][2];
+        ns[minor] = 1;
+        ns[medium] = n[minor];
+        ns[major] = (long long)n[minor] * n[medium];
+        es[minor] = 1;
+        es[medium] = n[minor] - 1;
+        es[major] = (long long)(n[minor] - 1) * (n[medium] - 1);
+        N = (long long)n[0] * n[1] * n[2];
+        NE = (long long)(n[0] - 1) * (n[1] - 1) * (n[2] - 1);
+        if (N > (1LL << 31) - 1) throw ArgError("meshes above 2^31 nodes are not supported");
+
+        ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        int dev = 0;
+        ck(cudaGetDevice(&dev), "cudaGetDevice");
+        ck(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+        cfg.stream = stream;
+        cfg.vec_blocks = sm_count * 4;
+        if (cfg.vec_blocks > kMaxPartialBlocks) cfg.vec_blocks = kMaxPartialBlocks;
+        // choose z-planes per operator block so that the block count stays within the partial slots
+        cfg.apply_planes = 1;
+        while (apply_blocks(cfg, n[0], n[1], n[2]) > kMaxPartialBlocks - 256) cfg.apply_planes *= 2;
+        while (apply_blocks(cfg, n[0], n[1], n[2]) > sm_count * 16 && cfg.apply_planes < 16) cfg.apply_planes *= 2;
+
+        for (int d = 0; d < 3; ++d) {
+            std::vector<double> h(n[d] - 1), r(n[d] - 1);
+            std::vector<float> hf(n[d] - 1), rf(n[d] - 1);
+            for (int i = 0; i < n[d] - 1; ++i) {
+                h[i] = ax[d][i + 1] - ax[d][i];
+                r[i] = 1.0 / h[i];
+                hf[i] = (float)h[i];
+                rf[i] = (float)r[i];
+            }
+            upload(h64[d], h, stream);
+            upload(r64[d], r, stream);
+            upload(h32[d], hf, stream);
+            upload(r32[d], rf, stream);
+        }
+        upload(z64, ax[2], stream);
+        g64 = GridT<double>{n[0], n[1], n[2], N, h64[0].as<double>(), h64[1].as<double>(), h64[2].as<double>(),
+                            r64[0].as<double>(), r64[1].as<double>(), r64[2].as<double>()};
+        g32 = GridT<float>{n[0], n[1], n[2], N, h32[0].as<float>(), h32[1].as<float>(), h32[2].as<float>(),
+                           r32[0].as<float>(), r32[1].as<float>(), r32[2].as<float>()};
+
+        const size_t N8 = (size_t)N * 8, N4 = (size_t)N * 4;
+        T.alloc(N8);
+        T0.alloc(N8);
+        F.alloc(N8);
+        b.alloc(N8);
+        r64v.alloc(N8);
+        vD.alloc(N8);
+        diag.alloc(N8);
+        minv64.alloc(N8);
+        minv32.alloc(N4);
+        k64.alloc(N8);
+        k32.alloc(N4);
+        p64.alloc(N8);
+        q64.alloc(N8);
+        x32.alloc(N4);
+        r32v.alloc(N4);
+        p32.alloc(N4);
+        q32.alloc(N4);
+        d_mat.alloc((size_t)N * 4);
+        d_heat.alloc(N8);
+        d_th.alloc(N8);
+        const size_t words = (size_t)(N + 31) / 32 + 1;
+        dmask.alloc(words * 4);
+        inactive_mask.alloc(words * 4);
+        partials.alloc(sizeof(double) * kMaxPartialBlocks * 4);
+        d_ctl.alloc(sizeof(SolveCtl));
+        ck(cudaMemsetAsync(d_ctl.p, 0, sizeof(SolveCtl), stream), "memset");
+        ck(cudaMallocHost(&h_ctl, sizeof(SolveCtl)), "cudaMallocHost");
+        std::memset(h_ctl, 0, sizeof(SolveCtl));
+        for (cudaEvent_t* e : {&ev0, &ev1, &ev2, &ev3}) ck(cudaEventCreate(e), "cudaEventCreate");
+        ck(cudaStreamSynchronize(stream), "sync");
+    }
+
+    // canonical index of a mesh-order node index
+    long long canon_of_mesh(long long m) const {
+        const long long imin = m % n[minor];
+        const long long imed = (m / n[minor]) % n[medium];
+        const long long imaj = m / ((long long)n[minor] * n[medium]);
+        long long id[3];
+        id[minor] = imin;
+        id[medium] = imed;
+        id[major] = imaj;
+        return id[0] + (long long)n[0] * (id[1] + (long long)n[1] * id[2]);
+    }
+    long long mesh_of_canon(long long c) const {
+        const long long i0 = c % n[0], i1 = (c / n[0]) % n[1], i2 = c / ((long long)n[0] * n[1]);
+        return i0 * ns[0] + i1 * ns[1] + i2 * ns[2];
+    }
+
+    // ---------------------------------------------------------------------------------
+    // inputs
+
+    void set_materials(int nm, const double* k3, const double* pp, const double* kz, const double* he,
+                       const uint8_t* em) {
+        if (nm <= 0 || !k3 || !pp) throw ArgError("material table needs k300 and p");
+        n_mat = nm;
+        k300.assign(k3, k3 + nm);
+        pexp.assign(pp, pp + nm);
+        kzr.assign(nm, 1.0);
+        hexp.assign(nm, 0.0);
+        empty.assign(nm, 0);
+        if (kz) kzr.assign(kz, kz + nm);
+        if (he) hexp.assign(he, he + nm);
+        if (em) empty.assign(em, em + nm);
+        aniso = false;
+        for (int m = 0; m < nm; ++m) {
+            if (!(k300[m] >= 0.0) || !std::isfinite(k300[m])) throw ArgError("k300 must be finite and >= 0");
+            if (kzr[m] != 1.0) aniso = true;
+        }
+        upload(d_k300, k300, stream);
+        upload(d_p, pexp, stream);
+        upload(d_kzr, kzr, stream);
+        upload(d_hexp, hexp, stream);
+        if (aniso) {
+            kz64.alloc((size_t)N * 8);
+            kz32.alloc((size_t)N * 4);
+        }
+        invalidate_solution();
+    }
+
+    void set_elements(const int32_t* mat, const double* heat, const double* leaf) {
+        if (!mat) throw ArgError("material ids are required");
+        if (n_mat == 0) throw StateError("set the material table first");
+        for (long long e = 0; e < NE; ++e)
+            if (mat[e] < 0 || mat[e] >= n_mat) throw ArgError("material id out of range");
+        host_mat.assign(mat, mat + NE);
+        DevBuf tmp;
+        tmp.alloc((size_t)NE * 8);
+        ck(cudaMemcpyAsync(tmp.p, mat, (size_t)NE * 4, cudaMemcpyHostToDevice, stream), "H2D mat");
+        launch_from_mesh_order_i32(cfg, n[0], n[1], n[2], n[0] - 1, n[1] - 1, n[2] - 1, es[0], es[1], es[2],
+                                   tmp.as<int>(), d_mat.as<int>(), 0);
+        set_heat_impl(heat, tmp);
+        if (leaf) {
+            d_hleaf.alloc((size_t)N * 8);
+            ck(cudaMemcpyAsync(tmp.p, leaf, (size_t)NE * 8, cudaMemcpyHostToDevice, stream), "H2D leaf");
+            launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], n[0] - 1, n[1] - 1, n[2] - 1, es[0], es[1], es[2],
+                                       tmp.as<double>(), d_hleaf.as<double>(), 0.0);
+            have_leaf = true;
+        } else {
+            have_leaf = false;
+        }
+        ck(cudaStreamSynchronize(stream), "sync");
+        have_elements = true;
+        invalidate_solution();
+    }
+
+    void set_heat_impl(const double* heat, DevBuf& tmp) {
+        if (heat) {
+            ck(cudaMemcpyAsync(tmp.p, heat, (size_t)NE * 8, cudaMemcpyHostToDevice, stream), "H2D heat");
+            launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], n[0] - 1, n[1] - 1, n[2] - 1, es[0], es[1], es[2],
+                                       tmp.as<double>(), d_heat.as<double>(), 0.0);
+        } else {
+            ck(cudaMemsetAsync(d_heat.p, 0, (size_t)N * 8, stream), "memset");
+        }
+        heat_dirty = true;
+    }
+
+    void set_heat(const double* heat) {
+        if (!have_elements) throw StateError("set the elements first");
+        DevBuf tmp;
+        tmp.alloc((size_t)NE * 8);
+        set_heat_impl(heat, tmp);
+        ck(cudaStreamSynchronize(stream), "sync");
+    }
+
+    void invalidate_solution() {
+        initialized = false;
+        bc_dirty = true;
+        heat_dirty = true;
+    }
+
+    // ---------------------------------------------------------------------------------
+    // initialisation (onInitialize, therm3d.cpp:71-115; setupMaskedMesh, fem_solver.hpp:182-189)
+
+    bool exclude_empty() const {
+        if (empty_mode == PLGPU_EMPTY_INCLUDE) return false;
+        if (empty_mode == PLGPU_EMPTY_EXCLUDE) return true;
+        return algorithm != PLGPU_ALGO_ITERATIVE;  // reference default: exclude unless iterative
+    }
+
+    void initialize() {
+        if (n_mat == 0 || !have_elements) throw StateError("materials and elements must be set before computing");
+        const bool excl = exclude_empty();
+        std::vector<uint8_t> ex(n_mat, 0);
+        bool any_ex = false;
+        for (int m = 0; m < n_mat; ++m) {
+            ex[m] = (excl && empty[m]) ? 1 : 0;
+            any_ex |= ex[m] != 0;
+        }
+        upload(d_excl, ex, stream);
+        tab = MatTable{d_k300.as<double>(), d_p.as<double>(), d_kzr.as<double>(), d_hexp.as<double>(),
+                       d_excl.as<uint8_t>()};
+
+        // masked numbering: nodes touched by an active element, in mesh order
+        masked = false;
+        any_inactive = false;
+        h_active.clear();
+        h_canon2mask.clear();
+        std::vector<uint32_t> inact((size_t)(N + 31) / 32 + 1, 0u);
+        if (any_ex) {
+            std::vector<uint8_t> used((size_t)N, 0);
+            for (int k = 0; k < n[2] - 1; ++k)
+                for (int j = 0; j < n[1] - 1; ++j)
+                    for (int i = 0; i < n[0] - 1; ++i) {
+                        const long long em = i * es[0] + j * es[1] + (long long)k * es[2];
+                        if (ex[host_mat[em]]) continue;
+                        for (int c = 0; c < 8; ++c) {
+                            const long long cn = (i + (c & 1)) + (long long)n[0] * ((j + ((c >> 1) & 1)) +
+                                                                                   (long long)n[1] * (k + (c >> 2)));
+                            used[cn] = 1;
+                        }
+                    }
+            std::vector<std::pair<long long, long long>> order;  // (mesh index, canonical)
+            for (long long cn = 0; cn < N; ++cn) {
+                if (used[cn])
+                    order.emplace_back(mesh_of_canon(cn), cn);
+                else {
+                    inact[cn >> 5] |= 1u << (cn & 31);
+                    any_inactive = true;
+                }
+            }
+            std::sort(order.begin(), order.end());
+            masked = true;
+            h_canon2mask.assign((size_t)N, -1);
+            h_active.resize(order.size());
+            for (size_t t = 0; t < order.size(); ++t) {
+                h_active[t] = order[t].second;
+                h_canon2mask[order[t].second] = (int64_t)t;
+            }
+            n_active = (long long)order.size();
+            upload(d_active, h_active, stream);
+        } else {
+            n_active = N;
+        }
+        upload(inactive_mask, inact, stream);
+
+        // thickness of layer runs
+        launch_thickness(cfg, n[0], n[1], n[2], d_mat.as<int>(), z64.as<double>(), d_th.as<double>());
+        // temperatures = inittemp
+        std::vector<double> t0((size_t)N, inittemp);
+        ck(cudaMemcpyAsync(T.p, t0.data(), (size_t)N * 8, cudaMemcpyHostToDevice, stream), "H2D T");
+        ck(cudaStreamSynchronize(stream), "sync");
+        loopno = 0;
+        initialized = true;
+        bc_dirty = true;
+        heat_dirty = true;
+    }
+
+    // ---------------------------------------------------------------------------------
+    // boundary conditions (setBoundaries, therm3d.cpp:141-168; applyBC, matrix.hpp:111-118)
+
+    bool node_active(long long cn) const { return !masked || h_canon2mask[cn] >= 0; }
+
+    // first matching condition per node (boundary_conditions.hpp:182-186)
+    std::unordered_map<long long, int> first_match(int kind) const {
+        std::unordered_map<long long, int> m;
+        for (size_t c = 0; c < bcs[kind].size(); ++c)
+            for (int64_t node : bcs[kind][c].nodes) {
+                const long long cn = canon_of_mesh(node);
+                if (!node_active(cn)) continue;
+                m.emplace(cn, (int)c);
+            }
+        return m;
+    }
+
+    void materialize_bc() {
+        // Dirichlet set: v_first eliminates, v_last stays in the row (matrix.hpp:132-145)
+        std::unordered_map<long long, std::pair<double, double>> dval;
+        std::vector<long long> dorder;
+        for (const Cond& c : bcs[PLGPU_BC_TEMPERATURE])
+            for (int64_t node : c.nodes) {
+                const long long cn = canon_of_mesh(node);
+                if (!node_active(cn)) continue;
+                auto it = dval.find(cn);
+                if (it == dval.end()) {
+                    dval.emplace(cn, std::make_pair(c.v0, c.v0));
+                    dorder.push_back(cn);
+                } else {
+                    it->second.second = c.v0;
+                }
+            }
+        std::vector<uint32_t> dm((size_t)(N + 31) / 32 + 1, 0u);
+        std::vector<int> didx;
+        std::vector<double> dv;
+        std::vector<double> vfirst_sparse;
+        for (long long cn : dorder) {
+            dm[cn >> 5] |= 1u << (cn & 31);
+            didx.push_back((int)cn);
+            dv.push_back(dval[cn].second);
+            vfirst_sparse.push_back(dval[cn].first);
+        }
+        std::vector<int> inactive_nodes;
+        if (any_inactive) {
+            for (long long cn = 0; cn < N; ++cn)
+                if (h_canon2mask[cn] < 0) {
+                    dm[cn >> 5] |= 1u << (cn & 31);
+                    inactive_nodes.push_back((int)cn);
+                }
+        }
+        auto is_d = [&](long long cn) { return (dm[cn >> 5] >> (cn & 31)) & 1u; };
+        nD = (int)didx.size();
+        // inactive nodes keep their temperature: treat them as Dirichlet rows at inittemp
+        for (int cn : inactive_nodes) {
+            didx.push_back(cn);
+            dv.push_back(inittemp);
+        }
+        upload(dmask, dm, stream);
+        upload(d_didx, didx, stream);
+        upload(d_dval, dv, stream);
+        // dense v_first (elimination input)
+        ck(cudaMemsetAsync(vD.p, 0, (size_t)N * 8, stream), "memset");
+        {
+            DevBuf ti, tv;
+            std::vector<int> ii(didx.begin(), didx.begin() + nD);
+            upload(ti, ii, stream);
+            upload(tv, vfirst_sparse, stream);
+            launch_scatter_add(cfg, nD, ti.as<int>(), tv.as<double>(), vD.as<double>());
+            ck(cudaStreamSynchronize(stream), "sync");
+        }
+
+        // face terms
+        auto mhf = first_match(PLGPU_BC_HEATFLUX);
+        auto mcv = first_match(PLGPU_BC_CONVECTION);
+        auto mrd = first_match(PLGPU_BC_RADIATION);
+        std::map<long long, double> fadd;                   // static load additions
+        std::map<std::pair<long long, long long>, double> K;  // surface stiffness (both triangles)
+        struct RadTerm {
+            long long row, src;
+            double coef, tamb;
+        };
+        std::vector<RadTerm> rad;
+
+        // global nodes 0..7 in the solver's numbering (radiation quirk, therm3d.cpp:265)
+        long long glob[8];
+        for (int w = 0; w < 8; ++w) {
+            long long cn = -1;
+            if (masked) {
+                if (w < (long long)h_active.size()) cn = h_active[w];
+            } else if (w < N) {
+                cn = canon_of_mesh(w);
+            }
+            glob[w] = cn;
+        }
+
+        std::vector<long long> cand;
+        {
+            std::vector<long long> nodes;
+            for (auto* m : {&mhf, &mcv, &mrd})
+                for (auto& kv : *m) nodes.push_back(kv.first);
+            std::vector<long long> els;
+            for (long long cn : nodes) {
+                const int i = (int)(cn % n[0]), j = (int)((cn / n[0]) % n[1]), k = (int)(cn / ((long long)n[0] * n[1]));
+                for (int c = 0; c < 8; ++c) {
+                    const int e0 = i - (c & 1), e1 = j - ((c >> 1) & 1), e2 = k - (c >> 2);
+                    if (e0 < 0 || e1 < 0 || e2 < 0 || e0 >= n[0] - 1 || e1 >= n[1] - 1 || e2 >= n[2] - 1) continue;
+                    els.push_back(e0 + (long long)n[0] * (e1 + (long long)n[1] * e2));
+                }
+            }
+            std::sort(els.begin(), els.end());
+            els.erase(std::unique(els.begin(), els.end()), els.end());
+            cand.swap(els);
+        }
+        static const int walls[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}};
+        for (long long ec : cand) {
+            const int i = (int)(ec % n[0]), j = (int)((ec / n[0]) % n[1]), k = (int)(ec / ((long long)n[0] * n[1]));
+            const long long em = i * es[0] + j * es[1] + (long long)k * es[2];
+            const int m = host_mat[em];
+            if (exclude_empty() && empty[m]) continue;
+            long long idx[8];
+            for (int c = 0; c < 8; ++c)
+                idx[c] = (i + (c & 1)) + (long long)n[0] * ((j + ((c >> 1) & 1)) + (long long)n[1] * (k + (c >> 2)));
+            const double dx = ax[0][i + 1] - ax[0][i], dy = ax[1][j + 1] - ax[1][j], dz = ax[2][k + 1] - ax[2][k];
+            const double areas[3] = {dx * dy, dy * dz, dz * dx};
+            for (int kind = PLGPU_BC_HEATFLUX; kind <= PLGPU_BC_RADIATION; ++kind) {
+                auto& mm = kind == PLGPU_BC_HEATFLUX ? mhf : kind == PLGPU_BC_CONVECTION ? mcv : mrd;
+                if (mm.empty()) continue;
+                int cond[8];
+                bool has[8];
+                for (int c = 0; c < 8; ++c) {
+                    auto it = mm.find(idx[c]);
+                    has[c] = it != mm.end();
+                    cond[c] = has[c] ? it->second : -1;
+                }
+                for (int side = 0; side < 6; ++side) {
+                    const int* w = walls[side];
+                    if (!(has[w[0]] && has[w[1]] && has[w[2]] && has[w[3]])) continue;
+                    const double area = areas[side / 2];
+                    for (int a = 0; a < 4; ++a) {
+                        const Cond& ca = bcs[kind][cond[w[a]]];
+                        // where the term lands: element corner a (reference placement) or the face node
+                        const long long ta = bc_compat ? idx[a] : idx[w[a]];
+                        if (kind == PLGPU_BC_HEATFLUX) {
+                            fadd[ta] += -0.25e-12 * area * ca.v0;
+                        } else if (kind == PLGPU_BC_CONVECTION) {
+                            fadd[ta] += 0.25e-12 * area * ca.v0 * ca.v1;
+                            for (int bq = 0; bq <= a; ++bq) {
+                                const Cond& cb = bcs[kind][cond[w[bq]]];
+                                const int ij = a ^ bq;
+                                const bool edge = (ij == 1 || ij == 2 || ij == 4);
+                                const double v = 0.125e-12 * area * (ca.v0 + cb.v0) / (a == bq ? 9.0 : edge ? 18.0 : 36.0);
+                                const long long tb = bc_compat ? idx[bq] : idx[w[bq]];
+                                K[{ta, tb}] += v;
+                                if (ta != tb) K[{tb, ta}] += v;
+                            }
+                        } else {
+                            const long long src = bc_compat ? glob[w[a]] : idx[w[a]];
+                            if (src < 0) throw ArgError("radiation boundary on a mesh with fewer than 8 nodes");
+                            rad.push_back({ta, src, -0.25e-12 * area * ca.v0 * kSB, ca.v1});
+                        }
+                    }
+                }
+            }
+        }
+        // split the surface stiffness: free-free part on the device, free-Dirichlet part
+        // eliminated into the static load (b_c -= A(c, r) v_first(r), matrix.hpp:137-144)
+        std::vector<int> srow, sptr, scol;
+        std::vector<double> sval;
+        std::vector<float> sval32;
+        long long cur = -1;
+        for (auto& kv : K) {
+            const long long r = kv.first.first, c = kv.first.second;
+            if (is_d(r)) continue;
+            if (is_d(c)) {
+                auto it = dval.find(c);
+                const double v = it != dval.end() ? it->second.first : inittemp;
+                fadd[r] -= kv.second * v;
+                continue;
+            }
+            if (r != cur) {
+                srow.push_back((int)r);
+                sptr.push_back((int)scol.size());
+                cur = r;
+            }
+            scol.push_back((int)c);
+            sval.push_back(kv.second);
+            sval32.push_back((float)kv.second);
+        }
+        sptr.push_back((int)scol.size());
+        upload(s_row, srow, stream);
+        upload(s_ptr, sptr, stream);
+        upload(s_col, scol, stream);
+        upload(s_val64, sval, stream);
+        upload(s_val32, sval32, stream);
+        const int nr = (int)srow.size();
+        s64 = SurfaceT<double>{nr, s_row.as<int>(), s_ptr.as<int>(), s_col.as<int>(), s_val64.as<double>()};
+        s32 = SurfaceT<float>{nr, s_row.as<int>(), s_ptr.as<int>(), s_col.as<int>(), s_val32.as<float>()};
+
+        std::vector<int> fi;
+        std::vector<double> fv;
+        for (auto& kv : fadd) {
+            if (is_d(kv.first)) continue;
+            fi.push_back((int)kv.first);
+            fv.push_back(kv.second);
+        }
+        n_fbc = (int)fi.size();
+        upload(fbc_idx, fi, stream);
+        upload(fbc_val, fv, stream);
+
+        std::stable_sort(rad.begin(), rad.end(), [](const RadTerm& a, const RadTerm& b) { return a.row < b.row; });
+        std::vector<int> rrow, rptr, rsrc;
+        std::vector<double> rcoef, rtamb;
+        cur = -1;
+        for (const RadTerm& t : rad) {
+            if (is_d(t.row)) continue;
+            if (t.row != cur) {
+                rrow.push_back((int)t.row);
+                rptr.push_back((int)rsrc.size());
+                cur = t.row;
+            }
+            rsrc.push_back((int)t.src);
+            rcoef.push_back(t.coef);
+            rtamb.push_back(t.tamb);
+        }
+        rptr.push_back((int)rsrc.size());
+        rad_rows = (int)rrow.size();
+        upload(rad_row, rrow, stream);
+        upload(rad_ptr, rptr, stream);
+        upload(rad_src, rsrc, stream);
+        upload(rad_coef, rcoef, stream);
+        upload(rad_tamb, rtamb, stream);
+        ck(cudaStreamSynchronize(stream), "sync");
+        bc_dirty = false;
+        heat_dirty = true;
+    }
+
+    void build_static_load() {
+        launch_heat_load(cfg, g64, d_heat.as<double>(), d_mat.as<int>(), tab, F.as<double>());
+        launch_scatter_add(cfg, n_fbc, fbc_idx.as<int>(), fbc_val.as<double>(), F.as<double>());
+        heat_dirty = false;
+    }
+
+    // ---------------------------------------------------------------------------------
+    // the linear solves
+
+    SolveCtl read_ctl() {
+        ck(cudaMemcpyAsync(h_ctl, d_ctl.p, sizeof(SolveCtl), cudaMemcpyDeviceToHost, stream), "D2H ctl");
+        ck(cudaStreamSynchronize(stream), "sync");
+        return *h_ctl;
+    }
+
+    int iteration_cap() const {
+        if (maxit > 0) return maxit;
+        long long m = 4 * (long long)(n[0] + n[1] + n[2]) * 50;
+        return (int)std::min<long long>(std::max<long long>(m, 2000), 200000);
+    }
+
+    template <typename R>
+    void cg_iterations(const GridT<R>& g, const R* kx, const R* kz, const SurfaceT<R>& s, R* x, R* r, R* p, R* q,
+                       const R* minv, int& status, int& iters, int cap) {
+        SolveCtl* ctl = d_ctl.as<SolveCtl>();
+        double* part = partials.as<double>();
+        const int slot0 = apply_blocks(cfg, n[0], n[1], n[2]);
+        int ch = chunk;
+        for (;;) {
+            for (int it = 0; it < ch; ++it) {
+                launch_apply(cfg, g, p, q, kx, kz, aniso, dmask.as<uint32_t>(), (const R*)nullptr, part, MODE_CG, ctl);
+                launch_surface(cfg, s, p, q, part, slot0, MODE_CG, ctl);
+                launch_cg_update(cfg, N, x, r, p, q, minv, part, ctl);
+                launch_cg_direction(cfg, N, p, r, minv, ctl);
+            }
+            ck(cudaGetLastError(), "launch");
+            SolveCtl c = read_ctl();
+            status = c.status;
+            iters = c.iter;
+            if (status != SOLVE_RUNNING) return;
+            if (c.iter >= cap) return;
+            if (ch < 256) ch *= 2;
+        }
+    }
+
+    // FP64 Jacobi-PCG on A T = b starting from the current T.  When the recursive
+    // residual reaches the tolerance the true residual is recomputed; CG restarts
+    // from the current iterate (at most 3 times) while it is still above 2 rtol.
+    void solve_fp64(int& status, int& iters, double& relres) {
+        SolveCtl* ctl = d_ctl.as<SolveCtl>();
+        double* part = partials.as<double>();
+        launch_norm2(cfg, N, b.as<double>(), nullptr, part, ctl, 2);  // ||b||^2
+        const int cap = iteration_cap();
+        iters = 0;
+        residual64();
+        for (int restart = 0; restart < 4; ++restart) {
+            int it = 0;
+            launch_cg_start(cfg, N, T.as<double>(), false, r64v.as<double>(), p64.as<double>(), minv64.as<double>(),
+                            part, ctl, rtol, 2, cap - iters, cap);
+            cg_iterations<double>(g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, s64, T.as<double>(),
+                                  r64v.as<double>(), p64.as<double>(), q64.as<double>(), minv64.as<double>(), status,
+                                  it, cap - iters);
+            iters += it;
+            residual64();  // true FP64 residual of the iterate
+            launch_norm2(cfg, N, r64v.as<double>(), nullptr, part, ctl, 3);
+            SolveCtl c = read_ctl();
+            relres = c.red[2] > 0 ? std::sqrt(c.red[3] / c.red[2]) : 0.0;
+            if (relres <= 2.0 * rtol) {
+                status = SOLVE_CONVERGED;
+                return;
+            }
+            if (status != SOLVE_CONVERGED || iters >= cap) return;
+        }
+    }
+
+    // r64 = b - A T (Dirichlet columns eliminated)
+    void residual64() {
+        launch_apply(cfg, g64, T.as<double>(), r64v.as<double>(), k64.as<double>(), aniso ? kz64.as<double>() : nullptr,
+                     aniso, dmask.as<uint32_t>(), b.as<double>(), partials.as<double>(), MODE_RESID, nullptr);
+        launch_surface(cfg, s64, T.as<double>(), r64v.as<double>(), partials.as<double>(), 0, MODE_RESID,
+                       d_ctl.as<SolveCtl>());
+    }
+
+    // FP32 Jacobi-PCG corrections inside FP64 iterative refinement
+    void solve_mixed(int& status, int& iters, int& refinements, double& relres) {
+        SolveCtl* ctl = d_ctl.as<SolveCtl>();
+        double* part = partials.as<double>();
+        launch_norm2(cfg, N, b.as<double>(), nullptr, part, ctl, 2);
+        const int cap = iteration_cap();
+        iters = 0;
+        refinements = 0;
+        status = SOLVE_RUNNING;
+        double prev = HUGE_VAL;
+        for (int step = 0; step < 60; ++step) {
+            residual64();
+            launch_norm2(cfg, N, r64v.as<double>(), r32v.as<float>(), part, ctl, 3);
+            SolveCtl c = read_ctl();
+            ++refinements;
+            relres = c.red[2] > 0 ? std::sqrt(c.red[3] / c.red[2]) : 0.0;
+            if (!std::isfinite(relres)) {
+                status = SOLVE_NONFINITE;
+                return;
+            }
+            if (relres <= rtol) {
+                status = SOLVE_CONVERGED;
+                return;
+            }
+            if (iters >= cap) {
+                status = SOLVE_MAXIT;
+                return;
+            }
+            if (step > 2 && relres > 0.5 * prev) {  // refinement no longer contracts: FP64 floor reached
+                status = relres < 1e-12 ? SOLVE_CONVERGED : SOLVE_STAGNATED;
+                return;
+            }
+            prev = relres;
+            int st = 0, it = 0;
+            launch_cg_start(cfg, N, x32.as<float>(), true, r32v.as<float>(), p32.as<float>(), minv32.as<float>(), part,
+                            ctl, inner_rtol, -1, cap - iters, cap);
+            cg_iterations<float>(g32, k32.as<float>(), aniso ? kz32.as<float>() : nullptr, s32, x32.as<float>(),
+                                 r32v.as<float>(), p32.as<float>(), q32.as<float>(), minv32.as<float>(), st, it,
+                                 cap - iters);
+            iters += it;
+            if (st == SOLVE_NONFINITE || st == SOLVE_BREAKDOWN) {
+                status = st;
+                return;
+            }
+            launch_add_correction(cfg, N, T.as<double>(), x32.as<float>());
+        }
+        status = SOLVE_MAXIT;
+    }
+
+    // ---------------------------------------------------------------------------------
+    // compute (therm3d.cpp:281-340)
+
+    double compute(int loops, plgpu_stats* st) {
+        if (!initialized) initialize();
+        if (bc_dirty) materialize_bc();
+        ck(cudaEventRecord(ev0, stream), "event");
+        if (heat_dirty) build_static_load();
+        log(3, "Running thermal calculations");
+        double toterr = 0.0, err = 0.0, maxT = 0.0, relres = 0.0;
+        int loop = 0, total_iters = 0, total_ref = 0;
+        float solve_ms = 0.f;
+        const bool mixed = algorithm == PLGPU_ALGO_ITERATIVE || algorithm == PLGPU_ALGO_GPU_MIXED ||
+                           algorithm == PLGPU_ALGO_GPU_LEARNED;
+        do {
+            ck(cudaMemcpyAsync(T0.p, T.p, (size_t)N * 8, cudaMemcpyDeviceToDevice, stream), "copy T0");
+            // setMatrix: coefficients, Jacobi diagonal, right-hand side with Dirichlet elimination
+            launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab,
+                        k64.as<double>(), k32.as<float>(), aniso ? kz64.as<double>() : nullptr,
+                        aniso ? kz32.as<float>() : nullptr, aniso);
+            launch_diag(cfg, g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, s64,
+                        dmask.as<uint32_t>(), diag.as<double>(), minv64.as<double>(), minv32.as<float>());
+            launch_apply(cfg, g64, vD.as<double>(), b.as<double>(), k64.as<double>(),
+                         aniso ? kz64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(), F.as<double>(),
+                         partials.as<double>(), MODE_RHS, nullptr);
+            launch_radiation(cfg, rad_rows, rad_row.as<int>(), rad_ptr.as<int>(), rad_src.as<int>(),
+                             rad_coef.as<double>(), rad_tamb.as<double>(), T.as<double>(), b.as<double>());
+            launch_set_dirichlet(cfg, (int)(d_didx.bytes / sizeof(int)), d_didx.as<int>(), d_dval.as<double>(),
+                                 b.as<double>(), T.as<double>());
+            ck(cudaGetLastError(), "launch");
+            ck(cudaEventRecord(ev2, stream), "event");
+            int status = 0, iters = 0, refs = 0;
+            if (mixed)
+                solve_mixed(status, iters, refs, relres);
+            else
+                solve_fp64(status, iters, relres);
+            ck(cudaEventRecord(ev3, stream), "event");
+            total_iters += iters;
+            total_ref += refs;
+            if (status == SOLVE_NONFINITE)
+                throw SolveError(PLGPU_ERR_NONFINITE, "non-finite value in the linear solve");
+            if (status == SOLVE_BREAKDOWN)
+                throw SolveError(PLGPU_ERR_NOT_SPD, "stiffness matrix is not positive definite (CG breakdown)");
+            converged = status == SOLVE_CONVERGED;
+            if (!converged) {
+                if (noconv == PLGPU_NOCONV_ERROR)
+                    throw SolveError(PLGPU_ERR_NOCONV, "failed to converge in " + std::to_string(iters) +
+                                                           " iterations (relative residual " +
+                                                           std::to_string(relres) + ")");
+                log(noconv == PLGPU_NOCONV_WARNING ? 2 : 5, "Failed to converge in %d iterations (error %g)", iters,
+                    relres);
+            }
+            launch_err(cfg, N, T.as<double>(), T0.as<double>(), any_inactive ? inactive_mask.as<uint32_t>() : nullptr,
+                       partials.as<double>(), d_ctl.as<SolveCtl>());
+            SolveCtl c = read_ctl();
+            float ms = 0.f;
+            ck(cudaEventElapsedTime(&ms, ev2, ev3), "elapsed");
+            solve_ms += ms;
+            err = c.red[0];
+            maxT = c.red[1] > 0 ? c.red[1] : 0.0;
+            if (err > toterr) toterr = err;
+            ++loopno;
+            ++loop;
+            log(4, "Loop %d(%d): max(T) = %.3f K, error = %g K", loop, loopno, maxT, err);
+            if (loop >= kMaxOuterLoops) break;
+        } while ((!converged || err > maxerr) && (loops == 0 || loop < loops));
+        ck(cudaEventRecord(ev1, stream), "event");
+        ck(cudaEventSynchronize(ev1), "sync");
+        float tot = 0.f;
+        ck(cudaEventElapsedTime(&tot, ev0, ev1), "elapsed");
+        if (st) {
+            st->loops = loop;
+            st->total_loops = loopno;
+            st->inner_iterations = total_iters;
+            st->refinements = total_ref;
+            st->converged = converged ? 1 : 0;
+            st->fallbacks = 0;
+            st->err = err;
+            st->toterr = toterr;
+            st->max_t = maxT;
+            st->last_rel_residual = relres;
+            st->solve_ms = solve_ms;
+            st->total_ms = tot;
+        }
+        return toterr;
+    }
+
+    // ---------------------------------------------------------------------------------
+    // outputs
+
+    void get_temperature(double* out) {
+        if (!initialized) {
+            for (long long t = 0; t < n_active; ++t) out[t] = inittemp;
+            return;
+        }
+        DevBuf tmp;
+        if (masked) {
+            tmp.alloc((size_t)n_active * 8);
+            launch_gather(cfg, n_active, d_active.as<long long>(), T.as<double>(), tmp.as<double>());
+        } else {
+            tmp.alloc((size_t)N * 8);
+            launch_to_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], (long long)n[0] * n[1], ns[0], ns[1], ns[2], 1,
+                                     T.as<double>(), tmp.as<double>());
+        }
+        ck(cudaMemcpyAsync(out, tmp.p, (size_t)n_active * 8, cudaMemcpyDeviceToHost, stream), "D2H T");
+        ck(cudaStreamSynchronize(stream), "sync");
+    }
+
+    void set_temperature(const double* in) {
+        if (!initialized) initialize();
+        DevBuf tmp;
+        tmp.alloc((size_t)n_active * 8);
+        ck(cudaMemcpyAsync(tmp.p, in, (size_t)n_active * 8, cudaMemcpyHostToDevice, stream), "H2D T");
+        if (masked)
+            launch_scatter(cfg, n_active, d_active.as<long long>(), tmp.as<double>(), T.as<double>());
+        else
+            launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], n[1], n[2], ns[0], ns[1], ns[2], tmp.as<double>(),
+                                       T.as<double>(), 0.0);
+        ck(cudaStreamSynchronize(stream), "sync");
+    }
+
+    void element_output(int comps, void (*fill)(plgpu_fem3d*, double*), double* out) {
+        DevBuf canon, tmp;
+        canon.alloc((size_t)NE * comps * 8);
+        tmp.alloc((size_t)NE * comps * 8);
+        fill(this, canon.as<double>());
+        launch_to_mesh_order_f64(cfg, n[0] - 1, n[1] - 1, n[2] - 1, n[0] - 1, (long long)(n[0] - 1) * (n[1] - 1), es[0],
+                                 es[1], es[2], comps, canon.as<double>(), tmp.as<double>());
+        ck(cudaMemcpyAsync(out, tmp.p, (size_t)NE * comps * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+        ck(cudaStreamSynchronize(stream), "sync");
+    }
+
+    void get_flux(double* out3) {
+        if (!initialized) initialize();
+        element_output(3,
+                       [](plgpu_fem3d* h, double* dst) {
+                           launch_flux(h->cfg, h->g64, h->T.as<double>(), h->d_mat.as<int>(),
+                                       h->have_leaf ? h->d_hleaf.as<double>() : h->d_th.as<double>(), h->tab, dst);
+                       },
+                       out3);
+    }
+    void get_conductivity(double* out2) {
+        if (!initialized) initialize();
+        element_output(2,
+                       [](plgpu_fem3d* h, double* dst) {
+                           launch_conductivity(h->cfg, h->n[0], h->n[1], h->n[2], h->T.as<double>(),
+                                               h->d_mat.as<int>(), h->d_th.as<double>(), h->tab, dst);
+                       },
+                       out2);
+    }
+    void get_thickness(double* out) {
+        if (!initialized) initialize();
+        DevBuf tmp;
+        tmp.alloc((size_t)NE * 8);
+        launch_to_mesh_order_f64(cfg, n[0] - 1, n[1] - 1, n[2] - 1, n[0], (long long)n[0] * n[1], es[0], es[1], es[2], 1,
+                                 d_th.as<double>(), tmp.as<double>());
+        ck(cudaMemcpyAsync(out, tmp.p, (size_t)NE * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+        ck(cudaStreamSynchronize(stream), "sync");
+    }
+};
+
+// ---------------------------------------------------------------------------------------
+// C ABI
+
+namespace {
+thread_local std::string g_create_error;
+
+template <typename F>
+int guarded(plgpu_fem3d* h, F&& f) {
+    if (!h) return PLGPU_ERR_ARG;
+    try {
+        f();
+        h->err.clear();
+        return PLGPU_OK;
+    } catch (const ArgError& e) {
+        h->err = e.what();
+        return PLGPU_ERR_ARG;
+    } catch (const StateError& e) {
+        h->err = e.what();
+        return PLGPU_ERR_STATE;
+    } catch (const SolveError& e) {
+        h->err = e.what();
+        return e.code;
+    } catch (const CudaError& e) {
+        h->err = e.what();
+        return PLGPU_ERR_CUDA;
+    } catch (const std::exception& e) {
+        h->err = e.what();
+        return PLGPU_ERR_ARG;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int plgpu_fem3d_create(const double* ax0, int n0, const double* ax1, int n1, const double* ax2, int n2, int ordering,
+                       plgpu_fem3d** out) {
+    if (!out) return PLGPU_ERR_ARG;
+    *out = nullptr;
+    std::unique_ptr<plgpu_fem3d> h(new plgpu_fem3d());
+    try {
+        h->setup_mesh(ax0, n0, ax1, n1, ax2, n2, ordering);
+    } catch (const ArgError& e) {
+        g_create_error = e.what();
+        return PLGPU_ERR_ARG;
+    } catch (const std::exception& e) {
+        g_create_error = e.what();
+        return PLGPU_ERR_CUDA;
+    }
+    *out = h.release();
+    return PLGPU_OK;
+}
+
+int plgpu_fem3d_destroy(plgpu_fem3d* h) {
+    if (!h) return PLGPU_ERR_ARG;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    delete h;
+    return PLGPU_OK;
+}
+
+const char* plgpu_fem3d_last_error(const plgpu_fem3d* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int plgpu_fem3d_set_materials(plgpu_fem3d* h, int n_mat, const double* k300, const double* p, const double* kz_ratio,
+                              const double* hexp, const uint8_t* empty) {
+    return guarded(h, [&] { h->set_materials(n_mat, k300, p, kz_ratio, hexp, empty); });
+}
+
+int plgpu_fem3d_set_elements(plgpu_fem3d* h, const int32_t* material, const double* heat, const double* leaf_height) {
+    return guarded(h, [&] { h->set_elements(material, heat, leaf_height); });
+}
+
+int plgpu_fem3d_set_heat(plgpu_fem3d* h, const double* heat) {
+    return guarded(h, [&] { h->set_heat(heat); });
+}
+
+int plgpu_fem3d_clear_bc(plgpu_fem3d* h, int kind) {
+    return guarded(h, [&] {
+        if (kind < 0 || kind > 3) throw ArgError("unknown boundary-condition kind");
+        h->bcs[kind].clear();
+        h->bc_dirty = true;
+    });
+}
+
+int plgpu_fem3d_add_bc(plgpu_fem3d* h, int kind, const int64_t* nodes, size_t count, double v0, double v1) {
+    return guarded(h, [&] {
+        if (kind < 0 || kind > 3) throw ArgError("unknown boundary-condition kind");
+        if (count && !nodes) throw ArgError("null node list");
+        plgpu_fem3d::Cond c;
+        c.nodes.assign(nodes, nodes + count);
+        for (int64_t m : c.nodes)
+            if (m < 0 || m >= h->N) throw ArgError("boundary node index out of range");
+        c.v0 = v0;
+        c.v1 = v1;
+        h->bcs[kind].push_back(std::move(c));
+        h->bc_dirty = true;
+    });
+}
+
+int plgpu_fem3d_set_solver(plgpu_fem3d* h, int algorithm, double rtol, int maxit, int noconv, int empty_elements,
+                           int bc_compat) {
+    return guarded(h, [&] {
+        if (algorithm < 0 || algorithm > PLGPU_ALGO_GPU_LEARNED) throw ArgError("unknown algorithm");
+        if (!(rtol > 0.0) || rtol >= 1.0) throw ArgError("rtol must be in (0, 1)");
+        if (noconv < 0 || noconv > 2) throw ArgError("unknown noconv behaviour");
+        if (empty_elements < 0 || empty_elements > 2) throw ArgError("unknown empty-elements mode");
+        const bool remask = h->exclude_empty();
+        h->algorithm = algorithm;
+        h->rtol = rtol;
+        h->maxit = maxit;
+        h->noconv = noconv;
+        h->empty_mode = empty_elements;
+        if (h->bc_compat != (bc_compat ? 1 : 0)) h->bc_dirty = true;
+        h->bc_compat = bc_compat ? 1 : 0;
+        if (remask != h->exclude_empty()) h->invalidate_solution();
+    });
+}
+
+int plgpu_fem3d_set_loop(plgpu_fem3d* h, double inittemp, double maxerr) {
+    return guarded(h, [&] {
+        if (!std::isfinite(inittemp) || !(maxerr >= 0.0)) throw ArgError("bad inittemp or maxerr");
+        h->inittemp = inittemp;
+        h->maxerr = maxerr;
+    });
+}
+
+int plgpu_fem3d_compute(plgpu_fem3d* h, int loops, double* toterr, plgpu_stats* stats) {
+    return guarded(h, [&] {
+        if (loops < 0) throw ArgError("loops must be >= 0");
+        const double t = h->compute(loops, stats);
+        if (toterr) *toterr = t;
+    });
+}
+
+int plgpu_fem3d_invalidate(plgpu_fem3d* h) {
+    return guarded(h, [&] { h->invalidate_solution(); });
+}
+
+int plgpu_fem3d_sizes(const plgpu_fem3d* h, size_t* n_nodes, size_t* n_elements) {
+    if (!h) return PLGPU_ERR_ARG;
+    plgpu_fem3d* m = const_cast<plgpu_fem3d*>(h);
+    return guarded(m, [&] {
+        if (!m->initialized && m->have_elements && m->n_mat) m->initialize();
+        if (n_nodes) *n_nodes = (size_t)(m->initialized ? m->n_active : m->N);
+        if (n_elements) *n_elements = (size_t)m->NE;
+    });
+}
+
+int plgpu_fem3d_get_temperature(plgpu_fem3d* h, double* out) {
+    return guarded(h, [&] {
+        if (!out) throw ArgError("null output");
+        h->get_temperature(out);
+    });
+}
+
+int plgpu_fem3d_set_temperature(plgpu_fem3d* h, const double* in) {
+    return guarded(h, [&] {
+        if (!in) throw ArgError("null input");
+        h->set_temperature(in);
+    });
+}
+
+int plgpu_fem3d_get_heat_flux(plgpu_fem3d* h, double* out3) {
+    return guarded(h, [&] {
+        if (!out3) throw ArgError("null output");
+        h->get_flux(out3);
+    });
+}
+
+int plgpu_fem3d_get_conductivity(plgpu_fem3d* h, double* out2) {
+    return guarded(h, [&] {
+        if (!out2) throw ArgError("null output");
+        h->get_conductivity(out2);
+    });
+}
+
+int plgpu_fem3d_get_thickness(plgpu_fem3d* h, double* out) {
+    return guarded(h, [&] {
+        if (!out) throw ArgError("null output");
+        h->get_thickness(out);
+    });
+}
+
+void* plgpu_fem3d_stream(plgpu_fem3d* h) { return h ? (void*)h->stream : nullptr; }
+
+int plgpu_fem3d_set_log_callback(plgpu_fem3d* h, void (*cb)(void*, int, const char*), void* user) {
+    return guarded(h, [&] {
+        h->log_cb = cb;
+        h->log_user = user;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,867 @@
+// Static3D thermal FEM kernels for sm_103a.
+//
+// What each kernel replaces in PLaSK (paths relative to the PLaSK tree):
+//   k_thickness      ThermalFem3DSolver::onInitialize layer-run thickness  solvers/thermal/static/therm3d.cpp:81-113
+//   k_coef           per-element k(T) of setMatrix                          therm3d.cpp:208-220
+//   k_heat_load      element load vector f = 0.125e-18 V q                  therm3d.cpp:222-223, 239-240, 274
+//   k_apply_*        the assembled stiffness matrix times a vector, matrix-free
+//                    (K_e of therm3d.cpp:226-237 summed over elements, Dirichlet rows
+//                    as after BandMatrix::setBC, plask/common/fem/matrix.hpp:132-145)
+//   k_surface        convective face terms of setBoundaries                  therm3d.cpp:141-168, 250-259
+//   k_cg_*           the linear solve that replaces dpbtrf/dpbtrs or NSPCG  cholesky_matrix.hpp:90-111,
+//                                                                            iterative_matrix.hpp:141-339
+//   k_err            outer-loop correction and max temperature             therm3d.cpp:317-326
+//   k_flux           saveHeatFluxes                                          therm3d.cpp:342-384
+//
+// All reductions are deterministic: every block writes one partial per value
+// and the last block to arrive sums the partials in a fixed order.
+#include <cfloat>
+#include <cstdint>
+
+#include "fem3d_device.cuh"
+#include "fem3d_kernels.h"
+
+namespace plgpu {
+
+// ----------------------------------------------------------------------------------------
+// reductions
+
+struct OpSum {
+    __device__ static double init() { return 0.0; }
+    __device__ static double op(double a, double b) { return a + b; }
+};
+struct OpMax {
+    __device__ static double init() { return -DBL_MAX; }
+    __device__ static double op(double a, double b) { return a > b ? a : b; }
+};
+
+__device__ __forceinline__ int linear_tid() {
+    return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+}
+__device__ __forceinline__ int block_threads() { return blockDim.x * blockDim.y * blockDim.z; }
+__device__ __forceinline__ int linear_bid() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
+
+// Block-wide reduction of NV values; the result is valid in every thread.
+template <int NV, typename Op>
+__device__ void block_reduce(double (&v)[NV]) {
+    __shared__ double sh[NV][32];
+    const int t = linear_tid(), lane = t & 31, warp = t >> 5, nw = (block_threads() + 31) >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+        for (int o = 16; o; o >>= 1) v[i] = Op::op(v[i], __shfl_xor_sync(0xffffffffu, v[i], o));
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) sh[i][warp] = v[i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        double w = lane < nw ? sh[i][lane] : Op::init();
+        for (int o = 16; o; o >>= 1) w = Op::op(w, __shfl_xor_sync(0xffffffffu, w, o));
+        v[i] = w;
+    }
+    __syncthreads();
+}
+
+// Write this block's reduced values to partials[i * kMaxPartialBlocks + slot].
+template <int NV, typename Op>
+__device__ void write_partial(double (&v)[NV], double* partials, int slot) {
+    block_reduce<NV, Op>(v);
+    if (linear_tid() == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) partials[(size_t)i * kMaxPartialBlocks + slot] = v[i];
+    }
+}
+
+// Count this block's arrival; true in the last of `expected` arriving blocks.
+__device__ bool arrive_last(unsigned int* counter, unsigned int expected) {
+    __shared__ int last;
+    __threadfence();
+    __syncthreads();
+    if (linear_tid() == 0) {
+        unsigned int prev = atomicAdd(counter, 1u);
+        last = (prev == expected - 1u);
+        if (last) *counter = 0u;  // ready for the next launch
+    }
+    __syncthreads();
+    if (last) __threadfence();
+    return last != 0;
+}
+
+// Sum partial slots [0, nslots) in a fixed order (valid in every thread).
+template <int NV, typename Op>
+__device__ void reduce_partials(double (&v)[NV], const double* partials, int nslots) {
+    const int t = linear_tid(), nt = block_threads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        double a = Op::init();
+        for (int s = t; s < nslots; s += nt) a = Op::op(a, __ldcg(partials + (size_t)i * kMaxPartialBlocks + s));
+        v[i] = a;
+    }
+    block_reduce<NV, Op>(v);
+}
+
+__device__ __forceinline__ bool is_dir(const uint32_t* __restrict__ dmask, long long n) {
+    return (__ldg(dmask + (n >> 5)) >> (n & 31)) & 1u;
+}
+
+// ----------------------------------------------------------------------------------------
+// element geometry
+
+// Scaled conductances of one element (therm3d.cpp:215-220):
+//   X = kx dy dz / dx,  Y = ky dx dz / dy,  Z = kz dx dy / dz,  kx = ky = k_xy.
+template <typename R>
+__device__ __forceinline__ void element_xyz(const GridT<R>& g, int e0, int e1, int e2, R kxy, R kz, R& X, R& Y, R& Z) {
+    const R dx = g.h0[e0], dy = g.h1[e1], dz = g.h2[e2];
+    X = kxy * g.r0[e0] * dy * dz;
+    Y = kxy * dx * g.r1[e1] * dz;
+    Z = kz * dx * dy * g.r2[e2];
+}
+
+// Entries of the trilinear-hex stiffness K_e: K[a][b] depends only on a ^ b (therm3d.cpp:227-237).
+template <typename R>
+__device__ __forceinline__ void element_g(R X, R Y, R Z, R (&gg)[8]) {
+    const R s = X + Y + Z;
+    const R c9 = R(1.0 / 9.0), c18 = R(1.0 / 18.0), c36 = R(1.0 / 36.0);
+    gg[0] = s * c9;
+    gg[1] = (Y + Z - R(2) * X) * c18;
+    gg[2] = (X + Z - R(2) * Y) * c18;
+    gg[4] = (X + Y - R(2) * Z) * c18;
+    gg[3] = (Z - R(2) * X - R(2) * Y) * c36;
+    gg[5] = (Y - R(2) * X - R(2) * Z) * c36;
+    gg[6] = (X - R(2) * Y - R(2) * Z) * c36;
+    gg[7] = -s * c36;
+}
+
+// ----------------------------------------------------------------------------------------
+// operator application (node-gather form)
+//
+// MODE_CG:    y = A x, Dirichlet rows y = x; per-block partial of (x, y)
+// MODE_RESID: y = rhs - A x with Dirichlet neighbours of x masked to zero,
+//             Dirichlet rows y = rhs - x
+// MODE_RHS:   y = rhs - A x with the full (unmasked) operator; Dirichlet rows
+//             are overwritten afterwards by k_set_dirichlet
+
+template <typename R, bool ANISO, int MODE>
+__global__ void __launch_bounds__(256) k_apply_gather(const GridT<R> g, const R* __restrict__ x, R* __restrict__ y,
+                                                      const R* __restrict__ kxy, const R* __restrict__ kzp,
+                                                      const uint32_t* __restrict__ dmask,
+                                                      const R* __restrict__ rhs, double* __restrict__ partials,
+                                                      int planes, const SolveCtl* __restrict__ ctl) {
+    if (MODE == MODE_CG && ctl != nullptr && ctl->status != SOLVE_RUNNING) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k0 = blockIdx.z * planes;
+    const int n0 = g.n0, n1 = g.n1, n2 = g.n2;
+    const int k1 = min(k0 + planes, n2);
+    const long long s1 = n0, s2 = (long long)n0 * n1;
+    double dot = 0.0;
+    if (i < n0 && j < n1) {
+        for (int k = k0; k < k1; ++k) {
+            const long long n = i + s1 * j + s2 * k;
+            const bool isd = is_dir(dmask, n);
+            R out;
+            if (MODE == MODE_CG && isd) {
+                out = x[n];
+            } else if (MODE == MODE_RESID && isd) {
+                out = rhs[n] - x[n];
+            } else {
+                R xv[27];
+#pragma unroll
+                for (int dk = 0; dk < 3; ++dk)
+#pragma unroll
+                    for (int dj = 0; dj < 3; ++dj)
+#pragma unroll
+                        for (int di = 0; di < 3; ++di) {
+                            const int ii = i + di - 1, jj = j + dj - 1, kk = k + dk - 1;
+                            R v = R(0);
+                            if (ii >= 0 && ii < n0 && jj >= 0 && jj < n1 && kk >= 0 && kk < n2) {
+                                const long long m = ii + s1 * jj + s2 * kk;
+                                v = x[m];
+                                if (MODE == MODE_RESID && is_dir(dmask, m)) v = R(0);
+                            }
+                            xv[di + 3 * (dj + 3 * dk)] = v;
+                        }
+                R acc = R(0);
+#pragma unroll
+                for (int ek = 0; ek < 2; ++ek)
+#pragma unroll
+                    for (int ej = 0; ej < 2; ++ej)
+#pragma unroll
+                        for (int ei = 0; ei < 2; ++ei) {
+                            const int e0 = i - 1 + ei, e1 = j - 1 + ej, e2 = k - 1 + ek;
+                            if (e0 < 0 || e0 >= n0 - 1 || e1 < 0 || e1 >= n1 - 1 || e2 < 0 || e2 >= n2 - 1) continue;
+                            const long long e = e0 + s1 * e1 + s2 * e2;
+                            const R kk = kxy[e];
+                            const R kv = ANISO ? kzp[e] : kk;
+                            R X, Y, Z, gg[8];
+                            element_xyz(g, e0, e1, e2, kk, kv, X, Y, Z);
+                            element_g(X, Y, Z, gg);
+                            const int a = (1 - ei) | ((1 - ej) << 1) | ((1 - ek) << 2);
+#pragma unroll
+                            for (int b = 0; b < 8; ++b) {
+                                const int bi = b & 1, bj = (b >> 1) & 1, bk = b >> 2;
+                                acc += gg[a ^ b] * xv[(ei + bi) + 3 * ((ej + bj) + 3 * (ek + bk))];
+                            }
+                        }
+                out = (MODE == MODE_CG) ? acc : R(rhs[n] - acc);
+            }
+            y[n] = out;
+            if (MODE == MODE_CG) dot += (double)x[n] * (double)out;
+        }
+    }
+    if (MODE == MODE_CG) {
+        double v[1] = {dot};
+        write_partial<1, OpSum>(v, partials, linear_bid());
+    }
+}
+
+// Convective face terms: a sparse symmetric operator on free nodes.
+// MODE_CG:    y[row] += S x; partial (x, S x); the last block finishes (p, A p) over
+//             all partial slots and sets alpha = rz / pq.
+// MODE_RESID: y[row] -= S x
+template <typename R, int MODE>
+__global__ void __launch_bounds__(256) k_surface(const SurfaceT<R> s, const R* __restrict__ x, R* __restrict__ y,
+                                                 double* __restrict__ partials, int slot0, int nslots,
+                                                 SolveCtl* __restrict__ ctl) {
+    if (MODE == MODE_CG && ctl->status != SOLVE_RUNNING) return;
+    double dot = 0.0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < s.nrows; r += gridDim.x * blockDim.x) {
+        const int n = s.row[r];
+        R acc = R(0);
+        for (int q = s.ptr[r]; q < s.ptr[r + 1]; ++q) acc += s.val[q] * x[s.col[q]];
+        if (MODE == MODE_CG) {
+            y[n] += acc;
+            dot += (double)x[n] * (double)acc;
+        } else {
+            y[n] -= acc;
+        }
+    }
+    if (MODE == MODE_CG) {
+        double v[1] = {dot};
+        write_partial<1, OpSum>(v, partials, slot0 + blockIdx.x);
+        if (arrive_last(&ctl->arrive[0], gridDim.x)) {
+            reduce_partials<1, OpSum>(v, partials, nslots);
+            if (linear_tid() == 0) {
+                const double pq = v[0];
+                ctl->pq = pq;
+                if (!isfinite(pq)) {
+                    ctl->status = SOLVE_NONFINITE;
+                } else if (!(pq > 0.0)) {
+                    ctl->status = SOLVE_BREAKDOWN;
+                } else {
+                    ctl->alpha = ctl->rz / pq;
+                }
+            }
+        }
+    }
+}
+
+// x += alpha p; r -= alpha q; then (r, M^-1 r) and (r, r); the last block sets beta
+// and the convergence status.
+template <typename R>
+__global__ void __launch_bounds__(256) k_cg_update(long long N, R* __restrict__ x, R* __restrict__ r,
+                                                   const R* __restrict__ p, const R* __restrict__ q,
+                                                   const R* __restrict__ minv, double* __restrict__ partials,
+                                                   SolveCtl* __restrict__ ctl) {
+    if (ctl->status != SOLVE_RUNNING) return;
+    const R alpha = R(ctl->alpha);
+    double rz = 0.0, rr = 0.0;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+        const R pn = p[n];
+        x[n] += alpha * pn;
+        const R rn = r[n] - alpha * q[n];
+        r[n] = rn;
+        rz += (double)rn * (double)(minv[n] * rn);
+        rr += (double)rn * (double)rn;
+    }
+    double v[2] = {rz, rr};
+    write_partial<2, OpSum>(v, partials, blockIdx.x);
+    if (arrive_last(&ctl->arrive[1], gridDim.x)) {
+        reduce_partials<2, OpSum>(v, partials, gridDim.x);
+        if (linear_tid() == 0) {
+            const double rzn = v[0], rrn = v[1];
+            ctl->iter += 1;
+            ctl->rz_old = ctl->rz;
+            ctl->beta = rzn / ctl->rz;
+            ctl->rz = rzn;
+            ctl->rr = rrn;
+            if (!isfinite(rrn) || !isfinite(rzn)) {
+                ctl->status = SOLVE_NONFINITE;
+            } else if (rrn <= ctl->tol2) {
+                ctl->status = SOLVE_CONVERGED;
+            } else if (ctl->iter >= ctl->maxit) {
+                ctl->status = SOLVE_MAXIT;
+            } else {
+                if (rrn < 0.81 * ctl->best_rr) {  // residual norm fell by 10 %
+                    ctl->best_rr = rrn;
+                    ctl->stall = 0;
+                } else if (++ctl->stall > ctl->stall_limit) {
+                    ctl->status = SOLVE_STAGNATED;
+                }
+            }
+        }
+    }
+}
+
+// p = M^-1 r + beta p
+template <typename R>
+__global__ void __launch_bounds__(256) k_cg_direction(long long N, R* __restrict__ p, const R* __restrict__ r,
+                                                      const R* __restrict__ minv, const SolveCtl* __restrict__ ctl) {
+    if (ctl->status != SOLVE_RUNNING) return;
+    const R beta = R(ctl->beta);
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x)
+        p[n] = minv[n] * r[n] + beta * p[n];
+}
+
+// Start a solve: r is the initial residual.  ZERO_X: x = 0 (correction solves).
+// p = M^-1 r; rz = (r, M^-1 r); rr = (r, r).  Stop threshold tol2 = rtol^2 * ref
+// where ref = ctl->red[ref_slot] if ref_slot >= 0, else the initial rr.
+template <typename R, bool ZERO_X>
+__global__ void __launch_bounds__(256) k_cg_start(long long N, R* __restrict__ x, const R* __restrict__ r,
+                                                  R* __restrict__ p, const R* __restrict__ minv,
+                                                  double* __restrict__ partials, SolveCtl* __restrict__ ctl,
+                                                  double rtol, int ref_slot, int maxit, int stall_limit) {
+    double rz = 0.0, rr = 0.0;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+        const R rn = r[n];
+        const R zn = minv[n] * rn;
+        p[n] = zn;
+        if (ZERO_X) x[n] = R(0);
+        rz += (double)rn * (double)zn;
+        rr += (double)rn * (double)rn;
+    }
+    double v[2] = {rz, rr};
+    write_partial<2, OpSum>(v, partials, blockIdx.x);
+    if (arrive_last(&ctl->arrive[1], gridDim.x)) {
+        reduce_partials<2, OpSum>(v, partials, gridDim.x);
+        if (linear_tid() == 0) {
+            const double ref = ref_slot >= 0 ? ctl->red[ref_slot] : v[1];
+            ctl->rz = v[0];
+            ctl->rz_old = v[0];
+            ctl->rr = v[1];
+            ctl->tol2 = rtol * rtol * ref;
+            ctl->best_rr = v[1];
+            ctl->iter = 0;
+            ctl->maxit = maxit;
+            ctl->stall = 0;
+            ctl->stall_limit = stall_limit;
+            ctl->alpha = 0.0;
+            ctl->beta = 0.0;
+            ctl->pq = 0.0;
+            if (!isfinite(v[0]) || !isfinite(v[1]))
+                ctl->status = SOLVE_NONFINITE;
+            else if (v[1] <= ctl->tol2 || v[1] == 0.0)
+                ctl->status = SOLVE_CONVERGED;
+            else if (!(v[0] > 0.0))
+                ctl->status = SOLVE_BREAKDOWN;
+            else
+                ctl->status = SOLVE_RUNNING;
+        }
+    }
+}
+
+// ||v||^2 into ctl->red[slot]; optionally also writes a float copy of v.
+__global__ void __launch_bounds__(256) k_norm2(long long N, const double* __restrict__ v, float* __restrict__ v32,
+                                               double* __restrict__ partials, SolveCtl* __restrict__ ctl, int slot) {
+    double s = 0.0;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+        const double a = v[n];
+        if (v32) v32[n] = (float)a;
+        s += a * a;
+    }
+    double w[1] = {s};
+    write_partial<1, OpSum>(w, partials, blockIdx.x);
+    if (arrive_last(&ctl->arrive[2], gridDim.x)) {
+        reduce_partials<1, OpSum>(w, partials, gridDim.x);
+        if (linear_tid() == 0) ctl->red[slot] = w[0];
+    }
+}
+
+// T += d (FP64 accumulation of an FP32 correction)
+__global__ void __launch_bounds__(256) k_add_correction(long long N, double* __restrict__ T, const float* __restrict__ d) {
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x)
+        T[n] += (double)d[n];
+}
+
+// ----------------------------------------------------------------------------------------
+// assembly-side kernels
+
+// Layer-run thickness (therm3d.cpp:81-113): for every element, the height of the
+// maximal vertical run of elements with the same material in its column.
+__global__ void k_thickness(int n0, int n1, int n2, const int* __restrict__ mat, const double* __restrict__ z,
+                            double* __restrict__ th) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= n0 - 1 || j >= n1 - 1) return;
+    const long long s2 = (long long)n0 * n1;
+    const long long base = i + (long long)n0 * j;
+    int start = 0;
+    for (int k = 1; k <= n2 - 1; ++k) {
+        const bool brk = (k == n2 - 1) || (mat[base + s2 * k] != mat[base + s2 * (k - 1)]);
+        if (brk) {
+            const double h = z[k] - z[start];
+            for (int q = start; q < k; ++q) th[base + s2 * q] = h;
+            start = k;
+        }
+    }
+}
+
+// Per-element conductivity at the 8-node mean temperature (therm3d.cpp:208-216),
+// stored in W/(um K).  Excluded and padding elements get 0.
+template <bool ANISO>
+__global__ void __launch_bounds__(256) k_coef(int n0, int n1, int n2, const double* __restrict__ T,
+                                              const int* __restrict__ mat, const double* __restrict__ th,
+                                              const MatTable tab, double* __restrict__ k64, float* __restrict__ k32,
+                                              double* __restrict__ kz64, float* __restrict__ kz32) {
+    const long long N = (long long)n0 * n1 * n2;
+    const long long s1 = n0, s2 = (long long)n0 * n1;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < N; e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n0);
+        const int j = (int)((e / n0) % n1);
+        const int k = (int)(e / s2);
+        double kxy = 0.0, kz = 0.0;
+        if (i < n0 - 1 && j < n1 - 1 && k < n2 - 1) {
+            const int m = mat[e];
+            if (!tab.excluded[m]) {
+                double t = 0.0;
+                t += T[e];
+                t += T[e + 1];
+                t += T[e + s1];
+                t += T[e + 1 + s1];
+                t += T[e + s2];
+                t += T[e + 1 + s2];
+                t += T[e + s1 + s2];
+                t += T[e + 1 + s1 + s2];
+                t *= 0.125;
+                double kk = tab.k300[m] * pow(300.0 / t, tab.p[m]);
+                if (tab.hexp[m] != 0.0) kk *= pow(th[e], tab.hexp[m]);
+                kxy = kk * 1e-6;
+                kz = (kk * tab.kz_ratio[m]) * 1e-6;
+            }
+        }
+        k64[e] = kxy;
+        k32[e] = (float)kxy;
+        if (ANISO) {
+            kz64[e] = kz;
+            kz32[e] = (float)kz;
+        }
+    }
+}
+
+// Jacobi diagonal: sum of K_e[a][a] = (X + Y + Z) / 9 over the node's elements.
+template <bool ANISO>
+__global__ void __launch_bounds__(256) k_diag(const GridT<double> g, const double* __restrict__ kxy,
+                                              const double* __restrict__ kzp, double* __restrict__ diag) {
+    const long long N = g.N;
+    const int n0 = g.n0, n1 = g.n1, n2 = g.n2;
+    const long long s1 = n0, s2 = (long long)n0 * n1;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(n % n0), j = (int)((n / n0) % n1), k = (int)(n / s2);
+        double d = 0.0;
+        for (int c = 0; c < 8; ++c) {
+            const int e0 = i - (c & 1), e1 = j - ((c >> 1) & 1), e2 = k - (c >> 2);
+            if (e0 < 0 || e0 >= n0 - 1 || e1 < 0 || e1 >= n1 - 1 || e2 < 0 || e2 >= n2 - 1) continue;
+            const long long e = e0 + s1 * e1 + s2 * e2;
+            double X, Y, Z;
+            element_xyz(g, e0, e1, e2, kxy[e], ANISO ? kzp[e] : kxy[e], X, Y, Z);
+            d += (X + Y + Z) * (1.0 / 9.0);
+        }
+        diag[n] = d;
+    }
+}
+
+// Add the diagonal of the surface operator, then invert (Dirichlet rows: 1).
+__global__ void k_surface_diag(const SurfaceT<double> s, double* __restrict__ diag) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < s.nrows; r += gridDim.x * blockDim.x) {
+        const int n = s.row[r];
+        double add = 0.0;
+        for (int q = s.ptr[r]; q < s.ptr[r + 1]; ++q)
+            if (s.col[q] == n) add += s.val[q];
+        diag[n] += add;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_invert_diag(long long N, const double* __restrict__ diag,
+                                                     const uint32_t* __restrict__ dmask, double* __restrict__ minv64,
+                                                     float* __restrict__ minv32) {
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+        double d = diag[n];
+        double v = (is_dir(dmask, n) || !(d > 0.0)) ? 1.0 : 1.0 / d;
+        minv64[n] = v;
+        minv32[n] = (float)v;
+    }
+}
+
+// Element heat load summed onto nodes: F_n = sum_e 0.125e-18 dx dy dz q_e (therm3d.cpp:223).
+__global__ void __launch_bounds__(256) k_heat_load(const GridT<double> g, const double* __restrict__ q,
+                                                   const int* __restrict__ mat, const MatTable tab,
+                                                   double* __restrict__ F) {
+    const long long N = g.N;
+    const int n0 = g.n0, n1 = g.n1, n2 = g.n2;
+    const long long s1 = n0, s2 = (long long)n0 * n1;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(n % n0), j = (int)((n / n0) % n1), k = (int)(n / s2);
+        double f = 0.0;
+        for (int c = 0; c < 8; ++c) {
+            const int e0 = i - (c & 1), e1 = j - ((c >> 1) & 1), e2 = k - (c >> 2);
+            if (e0 < 0 || e0 >= n0 - 1 || e1 < 0 || e1 >= n1 - 1 || e2 < 0 || e2 >= n2 - 1) continue;
+            const long long e = e0 + s1 * e1 + s2 * e2;
+            if (tab.excluded[mat[e]]) continue;
+            f += 0.125e-18 * g.h0[e0] * g.h1[e1] * g.h2[e2] * q[e];
+        }
+        F[n] = f;
+    }
+}
+
+// Scatter of sparse per-node additions (rows unique): F[idx] += val
+__global__ void k_scatter_add(int n, const int* __restrict__ idx, const double* __restrict__ val, double* __restrict__ F) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) F[idx[t]] += val[t];
+}
+
+// Dirichlet values: b[n] = T[n] = v_last (matrix.hpp:133-134).
+__global__ void k_set_dirichlet(int n, const int* __restrict__ idx, const double* __restrict__ v, double* __restrict__ b,
+                                double* __restrict__ T) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        b[idx[t]] = v[t];
+        T[idx[t]] = v[t];
+    }
+}
+
+// Radiation load, lagged in T (therm3d.cpp:262-268):
+//   b[row] += sum_terms -0.25e-12 area eps SB (T[src]^4 - Tamb^4)
+// coef already holds -0.25e-12 area eps SB; src is the node whose temperature is read.
+__global__ void k_radiation(int nrows, const int* __restrict__ row, const int* __restrict__ ptr,
+                            const int* __restrict__ src, const double* __restrict__ coef,
+                            const double* __restrict__ tamb, const double* __restrict__ T, double* __restrict__ b) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
+            double a = tamb[q];
+            a = a * a;
+            double t = T[src[q]];
+            t = t * t;
+            acc += coef[q] * (t * t - a * a);
+        }
+        b[row[r]] += acc;
+    }
+}
+
+// Outer-loop correction (therm3d.cpp:317-326): red[0] = max |T - T0| and red[1] = max T
+// (floored at 0) over active nodes.
+__global__ void __launch_bounds__(256) k_err(long long N, const double* __restrict__ T, const double* __restrict__ T0,
+                                             const uint32_t* __restrict__ inactive, double* __restrict__ partials,
+                                             SolveCtl* __restrict__ ctl) {
+    double err = 0.0, mx = 0.0;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+        if (inactive && is_dir(inactive, n)) continue;
+        const double t = T[n];
+        const double c = fabs(T0[n] - t);
+        if (!(c <= err)) err = (c != c) ? DBL_MAX : c;  // a NaN correction reads as the largest error
+        if (t > mx) mx = t;
+    }
+    double v[2] = {err, mx};
+    write_partial<2, OpMax>(v, partials, blockIdx.x);
+    if (arrive_last(&ctl->arrive[3], gridDim.x)) {
+        reduce_partials<2, OpMax>(v, partials, gridDim.x);
+        if (linear_tid() == 0) {
+            ctl->red[0] = v[0];
+            ctl->red[1] = v[1];
+        }
+    }
+}
+
+// Heat flux per element (therm3d.cpp:342-384) into out[3 * e] in canonical element order.
+__global__ void __launch_bounds__(256) k_flux(const GridT<double> g, const double* __restrict__ T,
+                                              const int* __restrict__ mat, const double* __restrict__ hleaf,
+                                              const MatTable tab, double* __restrict__ out) {
+    const int n0 = g.n0, n1 = g.n1, n2 = g.n2;
+    const long long NE = (long long)(n0 - 1) * (n1 - 1) * (n2 - 1);
+    const long long s1 = n0, s2 = (long long)n0 * n1;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < NE; t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % (n0 - 1));
+        const int j = (int)((t / (n0 - 1)) % (n1 - 1));
+        const int k = (int)(t / ((long long)(n0 - 1) * (n1 - 1)));
+        const long long e = i + s1 * j + s2 * k;
+        const int m = mat[e];
+        if (tab.excluded[m]) {
+            out[3 * t] = out[3 * t + 1] = out[3 * t + 2] = __longlong_as_double(0x7ff8000000000000LL);
+            continue;
+        }
+        const double lll = T[e], ull = T[e + 1], lul = T[e + s1], uul = T[e + 1 + s1];
+        const double llu = T[e + s2], ulu = T[e + 1 + s2], luu = T[e + s1 + s2], uuu = T[e + 1 + s1 + s2];
+        const double temp = 0.125 * (lll + llu + lul + luu + ull + ulu + uul + uuu);
+        double kk = tab.k300[m] * pow(300.0 / temp, tab.p[m]);
+        if (tab.hexp[m] != 0.0) kk *= pow(hleaf[e], tab.hexp[m]);
+        const double kxy = kk, kz = kk * tab.kz_ratio[m];
+        out[3 * t] = -0.25e6 * kxy * (-lll - llu - lul - luu + ull + ulu + uul + uuu) / g.h0[i];
+        out[3 * t + 1] = -0.25e6 * kxy * (-lll - llu + lul + luu - ull - ulu + uul + uuu) / g.h1[j];
+        out[3 * t + 2] = -0.25e6 * kz * (-lll + llu - lul + luu - ull + ulu - uul + uuu) / g.h2[k];
+    }
+}
+
+// Conductivity per element at the element-mean temperature and run thickness
+// (ThermalConductivityData::at, therm3d.cpp:421-435): out[2 t] = k_xy, out[2 t + 1] = k_z.
+__global__ void __launch_bounds__(256) k_conductivity(int n0, int n1, int n2, const double* __restrict__ T,
+                                                      const int* __restrict__ mat, const double* __restrict__ th,
+                                                      const MatTable tab, double* __restrict__ out) {
+    const long long NE = (long long)(n0 - 1) * (n1 - 1) * (n2 - 1);
+    const long long s1 = n0, s2 = (long long)n0 * n1;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < NE; t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % (n0 - 1));
+        const int j = (int)((t / (n0 - 1)) % (n1 - 1));
+        const int k = (int)(t / ((long long)(n0 - 1) * (n1 - 1)));
+        const long long e = i + s1 * j + s2 * k;
+        const int m = mat[e];
+        if (tab.excluded[m]) {
+            out[2 * t] = out[2 * t + 1] = __longlong_as_double(0x7ff8000000000000LL);
+            continue;
+        }
+        const double temp = 0.125 * (T[e] + T[e + 1] + T[e + s1] + T[e + 1 + s1] + T[e + s2] + T[e + 1 + s2] +
+                                     T[e + s1 + s2] + T[e + 1 + s1 + s2]);
+        double kk = tab.k300[m] * pow(300.0 / temp, tab.p[m]);
+        if (tab.hexp[m] != 0.0) kk *= pow(th[e], tab.hexp[m]);
+        out[2 * t] = kk;
+        out[2 * t + 1] = kk * tab.kz_ratio[m];
+    }
+}
+
+// ----------------------------------------------------------------------------------------
+// layout conversion between the mesh iteration order and the canonical layout
+
+// canonical element/node slot (padded to the node grid) <- mesh-order array.
+// (m0, m1, m2) are the extents of the mesh-order array along axes 0/1/2 (n or n-1),
+// (s0, s1, s2) its strides.  Slots outside the extents get `fill`.
+template <typename T>
+__global__ void __launch_bounds__(256) k_from_mesh_order(int n0, int n1, int n2, int m0, int m1, int m2, long long s0,
+                                                         long long s1, long long s2, const T* __restrict__ src,
+                                                         T* __restrict__ dst, T fill) {
+    const long long N = (long long)n0 * n1 * n2;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(n % n0), j = (int)((n / n0) % n1), k = (int)(n / ((long long)n0 * n1));
+        dst[n] = (i < m0 && j < m1 && k < m2) ? src[i * s0 + j * s1 + k * s2] : fill;
+    }
+}
+
+// mesh-order array (extents m0 x m1 x m2, strides s*, `comps` values per entry)
+// <- canonical array whose entry (i, j, k) sits at (i + c1 j + c2 k) * comps.
+template <typename T>
+__global__ void __launch_bounds__(256) k_to_mesh_order(int m0, int m1, int m2, long long c1, long long c2, long long s0,
+                                                       long long s1, long long s2, int comps, const T* __restrict__ src,
+                                                       T* __restrict__ dst) {
+    const long long M = (long long)m0 * m1 * m2;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < M; t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % m0), j = (int)((t / m0) % m1), k = (int)(t / ((long long)m0 * m1));
+        const long long from = (i + c1 * j + c2 * k) * comps;
+        const long long to = (i * s0 + j * s1 + k * s2) * comps;
+        for (int c = 0; c < comps; ++c) dst[to + c] = src[from + c];
+    }
+}
+
+// out[t] = in[idx[t]] and the inverse scatter.
+__global__ void k_gather(long long n, const long long* __restrict__ idx, const double* __restrict__ in,
+                         double* __restrict__ out) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        out[t] = in[idx[t]];
+}
+__global__ void k_scatter(long long n, const long long* __restrict__ idx, const double* __restrict__ in,
+                          double* __restrict__ out) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        out[idx[t]] = in[t];
+}
+
+// ----------------------------------------------------------------------------------------
+// launchers
+
+static inline int grid_for(long long n, int threads, int cap) {
+    long long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    return (int)(b < cap ? b : cap);
+}
+
+template <typename R>
+static void launch_apply_any(const LaunchCfg& c, const GridT<R>& g, const R* x, R* y, const R* kxy, const R* kz,
+                             bool aniso, const uint32_t* dmask, const R* rhs, double* partials, int mode,
+                             const SolveCtl* ctl, int* nblocks_out) {
+    dim3 block(32, 8, 1);
+    const int planes = c.apply_planes;
+    dim3 grid((g.n0 + 31) / 32, (g.n1 + 7) / 8, (g.n2 + planes - 1) / planes);
+    if (nblocks_out) *nblocks_out = (int)(grid.x * grid.y * grid.z);
+#define PLGPU_APPLY_CASE(MODEV)                                                                                          \
+    if (mode == MODEV) {                                                                                                 \
+        if (aniso)                                                                                                       \
+            k_apply_gather<R, true, MODEV><<<grid, block, 0, c.stream>>>(g, x, y, kxy, kz, dmask, rhs, partials, planes,  \
+                                                                         ctl);                                           \
+        else                                                                                                             \
+            k_apply_gather<R, false, MODEV><<<grid, block, 0, c.stream>>>(g, x, y, kxy, kz, dmask, rhs, partials, planes, \
+                                                                          ctl);                                          \
+        return;                                                                                                          \
+    }
+    PLGPU_APPLY_CASE(MODE_CG)
+    PLGPU_APPLY_CASE(MODE_RESID)
+    PLGPU_APPLY_CASE(MODE_RHS)
+#undef PLGPU_APPLY_CASE
+}
+
+int apply_blocks(const LaunchCfg& c, int n0, int n1, int n2) {
+    const int planes = c.apply_planes;
+    return ((n0 + 31) / 32) * ((n1 + 7) / 8) * ((n2 + planes - 1) / planes);
+}
+
+void launch_apply(const LaunchCfg& c, const GridT<double>& g, const double* x, double* y, const double* kxy,
+                  const double* kz, bool aniso, const uint32_t* dmask, const double* rhs, double* partials, int mode,
+                  const SolveCtl* ctl) {
+    launch_apply_any<double>(c, g, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, nullptr);
+}
+void launch_apply(const LaunchCfg& c, const GridT<float>& g, const float* x, float* y, const float* kxy,
+                  const float* kz, bool aniso, const uint32_t* dmask, const float* rhs, double* partials, int mode,
+                  const SolveCtl* ctl) {
+    launch_apply_any<float>(c, g, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, nullptr);
+}
+
+template <typename R>
+static void launch_surface_any(const LaunchCfg& c, const SurfaceT<R>& s, const R* x, R* y, double* partials, int slot0,
+                               int mode, SolveCtl* ctl) {
+    const int blocks = mode == MODE_CG ? surface_blocks(s.nrows) : grid_for(s.nrows, 256, 1024);
+    if (mode == MODE_CG) {
+        k_surface<R, MODE_CG><<<blocks, 256, 0, c.stream>>>(s, x, y, partials, slot0, slot0 + blocks, ctl);
+    } else {
+        if (s.nrows == 0) return;
+        k_surface<R, MODE_RESID><<<blocks, 256, 0, c.stream>>>(s, x, y, partials, slot0, slot0 + blocks, ctl);
+    }
+}
+int surface_blocks(int nrows) { return grid_for(nrows, 256, 64); }
+void launch_surface(const LaunchCfg& c, const SurfaceT<double>& s, const double* x, double* y, double* partials,
+                    int slot0, int mode, SolveCtl* ctl) {
+    launch_surface_any<double>(c, s, x, y, partials, slot0, mode, ctl);
+}
+void launch_surface(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, double* partials, int slot0,
+                    int mode, SolveCtl* ctl) {
+    launch_surface_any<float>(c, s, x, y, partials, slot0, mode, ctl);
+}
+
+int vec_blocks(const LaunchCfg& c, long long N) { return grid_for(N, 256, c.vec_blocks); }
+
+template <typename R>
+static void cg_update_any(const LaunchCfg& c, long long N, R* x, R* r, const R* p, const R* q, const R* minv,
+                          double* partials, SolveCtl* ctl) {
+    k_cg_update<R><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, x, r, p, q, minv, partials, ctl);
+}
+void launch_cg_update(const LaunchCfg& c, long long N, double* x, double* r, const double* p, const double* q,
+                      const double* minv, double* partials, SolveCtl* ctl) {
+    cg_update_any(c, N, x, r, p, q, minv, partials, ctl);
+}
+void launch_cg_update(const LaunchCfg& c, long long N, float* x, float* r, const float* p, const float* q,
+                      const float* minv, double* partials, SolveCtl* ctl) {
+    cg_update_any(c, N, x, r, p, q, minv, partials, ctl);
+}
+void launch_cg_direction(const LaunchCfg& c, long long N, double* p, const double* r, const double* minv,
+                         const SolveCtl* ctl) {
+    k_cg_direction<double><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, p, r, minv, ctl);
+}
+void launch_cg_direction(const LaunchCfg& c, long long N, float* p, const float* r, const float* minv,
+                         const SolveCtl* ctl) {
+    k_cg_direction<float><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, p, r, minv, ctl);
+}
+void launch_cg_start(const LaunchCfg& c, long long N, double* x, bool zero_x, const double* r, double* p,
+                     const double* minv, double* partials, SolveCtl* ctl, double rtol, int ref_slot, int maxit,
+                     int stall_limit) {
+    if (zero_x)
+        k_cg_start<double, true><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, x, r, p, minv, partials, ctl, rtol, ref_slot,
+                                                                         maxit, stall_limit);
+    else
+        k_cg_start<double, false><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, x, r, p, minv, partials, ctl, rtol,
+                                                                          ref_slot, maxit, stall_limit);
+}
+void launch_cg_start(const LaunchCfg& c, long long N, float* x, bool zero_x, const float* r, float* p,
+                     const float* minv, double* partials, SolveCtl* ctl, double rtol, int ref_slot, int maxit,
+                     int stall_limit) {
+    if (zero_x)
+        k_cg_start<float, true><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, x, r, p, minv, partials, ctl, rtol, ref_slot,
+                                                                        maxit, stall_limit);
+    else
+        k_cg_start<float, false><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, x, r, p, minv, partials, ctl, rtol, ref_slot,
+                                                                         maxit, stall_limit);
+}
+void launch_norm2(const LaunchCfg& c, long long N, const double* v, float* v32, double* partials, SolveCtl* ctl,
+                  int slot) {
+    k_norm2<<<vec_blocks(c, N), 256, 0, c.stream>>>(N, v, v32, partials, ctl, slot);
+}
+void launch_add_correction(const LaunchCfg& c, long long N, double* T, const float* d) {
+    k_add_correction<<<vec_blocks(c, N), 256, 0, c.stream>>>(N, T, d);
+}
+void launch_thickness(const LaunchCfg& c, int n0, int n1, int n2, const int* mat, const double* z, double* th) {
+    dim3 block(32, 8);
+    dim3 grid((n0 + 30) / 32, (n1 + 6) / 8);
+    k_thickness<<<grid, block, 0, c.stream>>>(n0, n1, n2, mat, z, th);
+}
+void launch_coef(const LaunchCfg& c, int n0, int n1, int n2, const double* T, const int* mat, const double* th,
+                 const MatTable& tab, double* k64, float* k32, double* kz64, float* kz32, bool aniso) {
+    const long long N = (long long)n0 * n1 * n2;
+    if (aniso)
+        k_coef<true><<<vec_blocks(c, N), 256, 0, c.stream>>>(n0, n1, n2, T, mat, th, tab, k64, k32, kz64, kz32);
+    else
+        k_coef<false><<<vec_blocks(c, N), 256, 0, c.stream>>>(n0, n1, n2, T, mat, th, tab, k64, k32, kz64, kz32);
+}
+void launch_diag(const LaunchCfg& c, const GridT<double>& g, const double* kxy, const double* kz, bool aniso,
+                 const SurfaceT<double>& s, const uint32_t* dmask, double* diag, double* minv64, float* minv32) {
+    if (aniso)
+        k_diag<true><<<vec_blocks(c, g.N), 256, 0, c.stream>>>(g, kxy, kz, diag);
+    else
+        k_diag<false><<<vec_blocks(c, g.N), 256, 0, c.stream>>>(g, kxy, kz, diag);
+    if (s.nrows > 0) k_surface_diag<<<grid_for(s.nrows, 256, 1024), 256, 0, c.stream>>>(s, diag);
+    k_invert_diag<<<vec_blocks(c, g.N), 256, 0, c.stream>>>(g.N, diag, dmask, minv64, minv32);
+}
+void launch_heat_load(const LaunchCfg& c, const GridT<double>& g, const double* q, const int* mat, const MatTable& tab,
+                      double* F) {
+    k_heat_load<<<vec_blocks(c, g.N), 256, 0, c.stream>>>(g, q, mat, tab, F);
+}
+void launch_scatter_add(const LaunchCfg& c, int n, const int* idx, const double* val, double* F) {
+    if (n > 0) k_scatter_add<<<grid_for(n, 256, 1024), 256, 0, c.stream>>>(n, idx, val, F);
+}
+void launch_set_dirichlet(const LaunchCfg& c, int n, const int* idx, const double* v, double* b, double* T) {
+    if (n > 0) k_set_dirichlet<<<grid_for(n, 256, 1024), 256, 0, c.stream>>>(n, idx, v, b, T);
+}
+void launch_radiation(const LaunchCfg& c, int nrows, const int* row, const int* ptr, const int* src, const double* coef,
+                      const double* tamb, const double* T, double* b) {
+    if (nrows > 0) k_radiation<<<grid_for(nrows, 256, 1024), 256, 0, c.stream>>>(nrows, row, ptr, src, coef, tamb, T, b);
+}
+void launch_err(const LaunchCfg& c, long long N, const double* T, const double* T0, const uint32_t* inactive,
+                double* partials, SolveCtl* ctl) {
+    k_err<<<vec_blocks(c, N), 256, 0, c.stream>>>(N, T, T0, inactive, partials, ctl);
+}
+void launch_flux(const LaunchCfg& c, const GridT<double>& g, const double* T, const int* mat, const double* hleaf,
+                 const MatTable& tab, double* out) {
+    const long long NE = (long long)(g.n0 - 1) * (g.n1 - 1) * (g.n2 - 1);
+    k_flux<<<vec_blocks(c, NE), 256, 0, c.stream>>>(g, T, mat, hleaf, tab, out);
+}
+void launch_conductivity(const LaunchCfg& c, int n0, int n1, int n2, const double* T, const int* mat, const double* th,
+                         const MatTable& tab, double* out) {
+    const long long NE = (long long)(n0 - 1) * (n1 - 1) * (n2 - 1);
+    k_conductivity<<<vec_blocks(c, NE), 256, 0, c.stream>>>(n0, n1, n2, T, mat, th, tab, out);
+}
+
+void launch_from_mesh_order_i32(const LaunchCfg& c, int n0, int n1, int n2, int m0, int m1, int m2, long long s0,
+                                long long s1, long long s2, const int* src, int* dst, int fill) {
+    const long long N = (long long)n0 * n1 * n2;
+    k_from_mesh_order<int><<<vec_blocks(c, N), 256, 0, c.stream>>>(n0, n1, n2, m0, m1, m2, s0, s1, s2, src, dst, fill);
+}
+void launch_from_mesh_order_f64(const LaunchCfg& c, int n0, int n1, int n2, int m0, int m1, int m2, long long s0,
+                                long long s1, long long s2, const double* src, double* dst, double fill) {
+    const long long N = (long long)n0 * n1 * n2;
+    k_from_mesh_order<double><<<vec_blocks(c, N), 256, 0, c.stream>>>(n0, n1, n2, m0, m1, m2, s0, s1, s2, src, dst,
+                                                                      fill);
+}
+void launch_to_mesh_order_f64(const LaunchCfg& c, int m0, int m1, int m2, long long c1, long long c2, long long s0,
+                              long long s1, long long s2, int comps, const double* src, double* dst) {
+    const long long M = (long long)m0 * m1 * m2;
+    k_to_mesh_order<double><<<vec_blocks(c, M), 256, 0, c.stream>>>(m0, m1, m2, c1, c2, s0, s1, s2, comps, src, dst);
+}
+void launch_gather(const LaunchCfg& c, long long n, const long long* idx, const double* in, double* out) {
+    if (n > 0) k_gather<<<vec_blocks(c, n), 256, 0, c.stream>>>(n, idx, in, out);
+}
+void launch_scatter(const LaunchCfg& c, long long n, const long long* idx, const double* in, double* out) {
+    if (n > 0) k_scatter<<<vec_blocks(c, n), 256, 0, c.stream>>>(n, idx, in, out);
+}
+
+}  // namespace plgpu

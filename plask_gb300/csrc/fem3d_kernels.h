@@ -1,0 +1,85 @@
+// Host-callable launchers of the Static3D kernels (fem3d_kernels.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fem3d_device.cuh"
+
+namespace plgpu {
+
+enum { MODE_CG = 0, MODE_RESID = 1, MODE_RHS = 2 };
+
+// Material table in device memory (one entry per material id).
+struct MatTable {
+    const double* k300;
+    const double* p;
+    const double* kz_ratio;
+    const double* hexp;
+    const uint8_t* excluded;  // element of this material is dropped from the system
+};
+
+struct LaunchCfg {
+    cudaStream_t stream;
+    int vec_blocks;    // grid size cap of streaming kernels (a multiple of the SM count)
+    int apply_planes;  // z-planes per block of the operator kernels
+};
+
+int apply_blocks(const LaunchCfg& c, int n0, int n1, int n2);
+int surface_blocks(int nrows);
+int vec_blocks(const LaunchCfg& c, long long N);
+
+void launch_apply(const LaunchCfg& c, const GridT<double>& g, const double* x, double* y, const double* kxy,
+                  const double* kz, bool aniso, const uint32_t* dmask, const double* rhs, double* partials, int mode,
+                  const SolveCtl* ctl);
+void launch_apply(const LaunchCfg& c, const GridT<float>& g, const float* x, float* y, const float* kxy,
+                  const float* kz, bool aniso, const uint32_t* dmask, const float* rhs, double* partials, int mode,
+                  const SolveCtl* ctl);
+void launch_surface(const LaunchCfg& c, const SurfaceT<double>& s, const double* x, double* y, double* partials,
+                    int slot0, int mode, SolveCtl* ctl);
+void launch_surface(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, double* partials,
+                    int slot0, int mode, SolveCtl* ctl);
+void launch_cg_update(const LaunchCfg& c, long long N, double* x, double* r, const double* p, const double* q,
+                      const double* minv, double* partials, SolveCtl* ctl);
+void launch_cg_update(const LaunchCfg& c, long long N, float* x, float* r, const float* p, const float* q,
+                      const float* minv, double* partials, SolveCtl* ctl);
+void launch_cg_direction(const LaunchCfg& c, long long N, double* p, const double* r, const double* minv,
+                         const SolveCtl* ctl);
+void launch_cg_direction(const LaunchCfg& c, long long N, float* p, const float* r, const float* minv,
+                         const SolveCtl* ctl);
+void launch_cg_start(const LaunchCfg& c, long long N, double* x, bool zero_x, const double* r, double* p,
+                     const double* minv, double* partials, SolveCtl* ctl, double rtol, int ref_slot, int maxit,
+                     int stall_limit);
+void launch_cg_start(const LaunchCfg& c, long long N, float* x, bool zero_x, const float* r, float* p,
+                     const float* minv, double* partials, SolveCtl* ctl, double rtol, int ref_slot, int maxit,
+                     int stall_limit);
+void launch_norm2(const LaunchCfg& c, long long N, const double* v, float* v32, double* partials, SolveCtl* ctl,
+                  int slot);
+void launch_add_correction(const LaunchCfg& c, long long N, double* T, const float* d);
+void launch_thickness(const LaunchCfg& c, int n0, int n1, int n2, const int* mat, const double* z, double* th);
+void launch_coef(const LaunchCfg& c, int n0, int n1, int n2, const double* T, const int* mat, const double* th,
+                 const MatTable& tab, double* k64, float* k32, double* kz64, float* kz32, bool aniso);
+void launch_diag(const LaunchCfg& c, const GridT<double>& g, const double* kxy, const double* kz, bool aniso,
+                 const SurfaceT<double>& s, const uint32_t* dmask, double* diag, double* minv64, float* minv32);
+void launch_heat_load(const LaunchCfg& c, const GridT<double>& g, const double* q, const int* mat, const MatTable& tab,
+                      double* F);
+void launch_scatter_add(const LaunchCfg& c, int n, const int* idx, const double* val, double* F);
+void launch_set_dirichlet(const LaunchCfg& c, int n, const int* idx, const double* v, double* b, double* T);
+void launch_radiation(const LaunchCfg& c, int nrows, const int* row, const int* ptr, const int* src, const double* coef,
+                      const double* tamb, const double* T, double* b);
+void launch_err(const LaunchCfg& c, long long N, const double* T, const double* T0, const uint32_t* inactive,
+                double* partials, SolveCtl* ctl);
+void launch_flux(const LaunchCfg& c, const GridT<double>& g, const double* T, const int* mat, const double* hleaf,
+                 const MatTable& tab, double* out);
+void launch_conductivity(const LaunchCfg& c, int n0, int n1, int n2, const double* T, const int* mat, const double* th,
+                         const MatTable& tab, double* out);
+void launch_from_mesh_order_i32(const LaunchCfg& c, int n0, int n1, int n2, int m0, int m1, int m2, long long s0,
+                                long long s1, long long s2, const int* src, int* dst, int fill);
+void launch_from_mesh_order_f64(const LaunchCfg& c, int n0, int n1, int n2, int m0, int m1, int m2, long long s0,
+                                long long s1, long long s2, const double* src, double* dst, double fill);
+void launch_to_mesh_order_f64(const LaunchCfg& c, int m0, int m1, int m2, long long c1, long long c2, long long s0,
+                              long long s1, long long s2, int comps, const double* src, double* dst);
+void launch_gather(const LaunchCfg& c, long long n, const long long* idx, const double* in, double* out);
+void launch_scatter(const LaunchCfg& c, long long n, const long long* idx, const double* in, double* out);
+
+}  // namespace plgpu

@@ -1,0 +1,219 @@
+"""Seeded synthetic layered structures for the Static3D thermal solver.
+
+PLaSK builds these inputs from a geometry tree and a mesh generator; here they
+are generated directly as what the FEM path consumes: three rectilinear axes
+(micrometres), one material id per element, a small material table with
+k(T) = k300 * (300/T)**p, one heat density per element (W/m^3) and boundary
+conditions on named mesh sides.
+
+Every generator takes a ``seed`` and draws from ``numpy.random.default_rng``
+(PCG64), so a seed names a structure exactly.
+
+Lateral refinement: the lateral axes span 0..50 um and are refined
+geometrically toward x = y = 0.  With 40 nodes the cell ratio is 1.15; for
+other node counts the ratio is ``1.15 ** (39 / (n - 1))`` so that the largest
+to smallest cell ratio (1.15**39 ~ 233) -- the grading of the 40-node mesh --
+is kept when the mesh is scaled.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+LATERAL_SPAN = 50.0
+SUBSTRATE = 150.0
+
+
+@dataclasses.dataclass
+class Structure:
+    """Everything one Static3D solve needs, in plain arrays.
+
+    * ``axes``: (axis0, axis1, axis2) node coordinates in um, axis 2 vertical
+    * ``mat``: int32 element material ids, shape (n2-1, n1-1, n0-1), axis 0 fastest
+    * ``k300``, ``p``, ``kz_ratio``, ``hexp``, ``empty``: per-material model
+      k_xy(T, h) = k300 * (300/T)**p * h**hexp,  k_z = kz_ratio * k_xy
+    * ``heat``: element heat density in W/m^3, same shape as ``mat``
+    * ``temperature``/``heatflux``/``convection``/``radiation``: boundary
+      conditions as (side, values...) with side one of
+      "bottom", "top", "back", "front", "left", "right"
+    """
+
+    axes: tuple
+    mat: np.ndarray
+    k300: np.ndarray
+    p: np.ndarray
+    kz_ratio: np.ndarray
+    hexp: np.ndarray
+    empty: np.ndarray
+    heat: np.ndarray
+    temperature: list = dataclasses.field(default_factory=list)
+    heatflux: list = dataclasses.field(default_factory=list)
+    convection: list = dataclasses.field(default_factory=list)
+    radiation: list = dataclasses.field(default_factory=list)
+    maxerr: float = 0.05
+    inittemp: float = 300.0
+    name: str = ""
+
+    @property
+    def shape(self):
+        """Node-grid shape (n2, n1, n0)."""
+        return tuple(len(a) for a in self.axes[::-1])
+
+    @property
+    def nodes(self):
+        return int(np.prod(self.shape))
+
+
+def side_mask(shape, side):
+    """Boolean node mask (n2, n1, n0) of a mesh side.
+
+    Names follow PLaSK's 3D rectangular mesh boundaries
+    (plask/mesh/rectilinear3d.cpp:158-190): back/front = axis 0 lo/hi,
+    left/right = axis 1 lo/hi, bottom/top = axis 2 lo/hi.
+    """
+    m = np.zeros(shape, bool)
+    if side == "bottom":
+        m[0] = True
+    elif side == "top":
+        m[-1] = True
+    elif side == "left":
+        m[:, 0] = True
+    elif side == "right":
+        m[:, -1] = True
+    elif side == "back":
+        m[:, :, 0] = True
+    elif side == "front":
+        m[:, :, -1] = True
+    else:
+        raise ValueError(f"unknown side {side!r}")
+    return m
+
+
+def graded_axis(n, span=LATERAL_SPAN, ratio40=1.15):
+    """n nodes on [0, span] with cells growing geometrically away from 0."""
+    if n < 2:
+        raise ValueError("an axis needs at least 2 nodes")
+    r = ratio40 ** (39.0 / (n - 1))
+    h = r ** np.arange(n - 1)
+    h *= span / h.sum()
+    x = np.concatenate([[0.0], np.cumsum(h)])
+    x[-1] = span
+    return x
+
+
+def _geometric_fill(length, cells, first):
+    """Cells on a segment of given length, growing from ``first`` by a common ratio."""
+    if cells * first >= length:
+        return np.full(cells, length / cells)
+    lo, hi = 1.0, 2.0
+    while first * (hi ** cells - 1) / (hi - 1) < length:
+        hi *= 2
+    for _ in range(200):
+        q = 0.5 * (lo + hi)
+        if first * (q ** cells - 1) / (q - 1) < length:
+            lo = q
+        else:
+            hi = q
+    h = first * q ** np.arange(cells)
+    return h * (length / h.sum())
+
+
+def _allocate(weights, total, minimum=1):
+    """Largest-remainder allocation of ``total`` cells with a per-entry minimum."""
+    n = len(weights)
+    base = np.full(n, minimum, np.int64)
+    rest = total - base.sum()
+    if rest < 0:
+        raise ValueError("not enough cells for the layers")
+    w = np.asarray(weights, np.float64)
+    share = rest * w / w.sum()
+    extra = np.floor(share).astype(np.int64)
+    left = rest - extra.sum()
+    order = np.argsort(-(share - extra), kind="stable")
+    extra[order[:left]] += 1
+    return base + extra
+
+
+def vertical_axis(thicknesses, n_nodes, substrate=SUBSTRATE, substrate_share=0.25):
+    """Node coordinates: a graded substrate under uniformly meshed layers.
+
+    Returns (z, layer_of_element) where layer 0 is the substrate and layer i >= 1
+    the i-th epitaxial layer from the bottom.
+    """
+    cells = n_nodes - 1
+    nl = len(thicknesses)
+    n_sub = max(1, int(round(substrate_share * cells)))
+    per_layer = _allocate(np.sqrt(np.asarray(thicknesses)), cells - n_sub)
+    hs = []
+    layer = []
+    first = 2.0 * thicknesses[0] / per_layer[0]
+    sub = _geometric_fill(substrate, n_sub, first)[::-1]
+    hs.append(sub)
+    layer.append(np.zeros(n_sub, np.int64))
+    for i, (t, c) in enumerate(zip(thicknesses, per_layer)):
+        hs.append(np.full(c, t / c))
+        layer.append(np.full(c, i + 1, np.int64))
+    h = np.concatenate(hs)
+    z = np.concatenate([[0.0], np.cumsum(h)])
+    return z, np.concatenate(layer)
+
+
+def _layered(rng, n, n_layers, active_thickness, anisotropic, source_radius, power):
+    thick = np.exp(rng.uniform(math.log(0.05), math.log(3.0), n_layers))
+    active = int(rng.integers(n_layers // 3, max(n_layers // 3 + 1, 2 * n_layers // 3)))
+    thick[active] = active_thickness
+    x0 = graded_axis(n[0])
+    x1 = graded_axis(n[1])
+    z, layer_of = vertical_axis(thick, n[2])
+    n_mat = n_layers + 1
+    k300 = np.exp(rng.uniform(math.log(1.0), math.log(150.0), n_mat))
+    p = rng.uniform(0.5, 1.5, n_mat)
+    kz = rng.uniform(0.5, 1.0, n_mat) if anisotropic else np.ones(n_mat)
+    mat = np.broadcast_to(layer_of[:, None, None], (n[2] - 1, n[1] - 1, n[0] - 1)).astype(np.int32)
+    xm = 0.5 * (x0[1:] + x0[:-1])
+    ym = 0.5 * (x1[1:] + x1[:-1])
+    r2 = xm[None, :] ** 2 + ym[:, None] ** 2
+    disc = r2 <= source_radius ** 2
+    heat = np.zeros(mat.shape)
+    heat[layer_of == active + 1] = np.where(disc, power, 0.0)[None]
+    return dict(axes=(x0, x1, z), mat=np.ascontiguousarray(mat), k300=k300, p=p, kz_ratio=kz,
+                hexp=np.zeros(n_mat), empty=np.zeros(n_mat, bool), heat=heat)
+
+
+def _fit_layers(n, n_layers):
+    """Number of layers that fits n[2] - 1 vertical cells next to the substrate."""
+    cells = n[2] - 1
+    return max(1, min(n_layers, cells - max(1, int(round(0.25 * cells)))))
+
+
+def layered_c0(seed=0, n=(40, 40, 60), power=1e16, n_layers=12):
+    """Plain Static3D case: 12 layers on a 150 um substrate, isotropic k(T),
+    a 4 um-radius disc source at 1e16 W/m^3 in a 0.1 um layer, bottom at 300 K.
+
+    Meshes with fewer than ``n_layers + 2`` vertical cells get fewer layers."""
+    rng = np.random.default_rng(seed)
+    d = _layered(rng, n, _fit_layers(n, n_layers), 0.1, False, 4.0, power)
+    return Structure(**d, temperature=[("bottom", 300.0)], name=f"layered-{n[0]}x{n[1]}x{n[2]}-s{seed}")
+
+
+def layered_c1(seed=1000, n=(128, 128, 200), power=1e16, n_layers=12):
+    """The scaled case: same generator at 128x128x200 nodes with lateral
+    anisotropy k_z/k_xy ~ U[0.5, 1] and a convective top (h = 10 W/m^2K, 300 K)."""
+    rng = np.random.default_rng(seed)
+    d = _layered(rng, n, _fit_layers(n, n_layers), 0.1, True, 4.0, power)
+    return Structure(**d, temperature=[("bottom", 300.0)], convection=[("top", 10.0, 300.0)],
+                     name=f"layered-aniso-{n[0]}x{n[1]}x{n[2]}-s{seed}")
+
+
+def sweep_c3(seed=3000, count=256, lo=32, hi=96):
+    """Batched sweep: ``count`` layered structures with per-axis node counts
+    uniform in [lo, hi] and source power uniform in [1e15, 1e17] W/m^3."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = tuple(int(v) for v in rng.integers(lo, hi + 1, 3))
+        pw = float(rng.uniform(1e15, 1e17))
+        out.append(layered_c0(seed=seed + 1 + i, n=n, power=pw))
+    return out

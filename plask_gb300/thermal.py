@@ -1,0 +1,516 @@
+"""``Static3D``: the 3D finite-element thermal solver, on the GPU.
+
+A drop-in for PLaSK's ``thermal.static.Static3D``
+(solvers/thermal/static/therm3d.hpp:27-139, python/therm_python.cpp:136-151,
+plask/common/fem/python.hpp:31-41): the same attribute names, defaults,
+boundary-condition lists, receiver and providers.  The computation runs in
+``libplgpu_fem3d.so``; this module only converts between PLaSK-style inputs
+and the library's arrays.
+
+Geometry: PLaSK asks its geometry tree for the material at every element
+midpoint.  Here ``geometry`` is any object with ``materials`` (a
+:class:`MaterialTable`) and ``material_ids(mesh)`` returning one material id
+per element (canonical shape), e.g. :class:`StructureGeometry`.
+"""
+from __future__ import annotations
+
+import dataclasses
+import logging
+
+import numpy as np
+
+from . import _native
+from .mesh import RectangularMesh3D, mesh_index, to_mesh_order
+
+log = logging.getLogger("plask_gb300.thermal")
+
+ComputationError = _native.ComputationError
+BadInput = _native.BadInput
+
+
+@dataclasses.dataclass
+class MaterialTable:
+    """Materials of a structure: k_xy(T, h) = k300 (300/T)^p h^hexp, k_z = kz_ratio k_xy."""
+
+    k300: np.ndarray
+    p: np.ndarray
+    kz_ratio: np.ndarray | None = None
+    hexp: np.ndarray | None = None
+    empty: np.ndarray | None = None
+
+    def __post_init__(self):
+        self.k300 = np.asarray(self.k300, np.float64)
+        n = self.k300.size
+        self.p = np.asarray(self.p, np.float64)
+        self.kz_ratio = np.ones(n) if self.kz_ratio is None else np.asarray(self.kz_ratio, np.float64)
+        self.hexp = np.zeros(n) if self.hexp is None else np.asarray(self.hexp, np.float64)
+        self.empty = np.zeros(n, bool) if self.empty is None else np.asarray(self.empty, bool)
+
+    def thermk(self, m, T, h=None):
+        kxy = self.k300[m] * (300.0 / np.asarray(T)) ** self.p[m]
+        if h is not None and np.any(self.hexp[m] != 0):
+            kxy = kxy * np.asarray(h) ** self.hexp[m]
+        return kxy, kxy * self.kz_ratio[m]
+
+
+class StructureGeometry:
+    """Geometry given directly as element material ids on a fixed mesh (or a callable of midpoints)."""
+
+    def __init__(self, materials: MaterialTable, mat=None, material_at=None, leaf_height=None):
+        self.materials = materials
+        self._mat = None if mat is None else np.asarray(mat, np.int32)
+        self._at = material_at
+        self._leaf = leaf_height
+
+    def material_ids(self, mesh: RectangularMesh3D):
+        if self._mat is not None:
+            if self._mat.shape != mesh.element_shape:
+                raise BadInput(-1, f"material ids of shape {self._mat.shape} do not fit the mesh {mesh.element_shape}")
+            return self._mat
+        if self._at is None:
+            raise BadInput(-1, "geometry has neither material ids nor a material function")
+        mids = mesh.element_midpoints()
+        return np.asarray(self._at(mids[..., 0], mids[..., 1], mids[..., 2]), np.int32)
+
+    def leaf_height(self, mesh):
+        return None if self._leaf is None else np.asarray(self._leaf, np.float64)
+
+    @classmethod
+    def from_structure(cls, s):
+        return cls(MaterialTable(s.k300, s.p, s.kz_ratio, s.hexp, s.empty), mat=s.mat)
+
+
+class BoundaryConditions:
+    """Ordered list of (place, value) pairs (BoundaryConditions, boundary_conditions.hpp)."""
+
+    def __init__(self, owner, kind, nvals):
+        self._owner = owner
+        self._kind = kind
+        self._nvals = nvals
+        self._items = []
+
+    def _norm(self, value):
+        if self._nvals == 1:
+            return (float(value),)
+        if isinstance(value, dict):
+            keys = ("coeff", "ambient") if self._kind == _native.BC_CONVECTION else ("emissivity", "ambient")
+            return tuple(float(value[k]) for k in keys)
+        return tuple(float(v) for v in value)
+
+    def append(self, place, value):
+        self._items.append((place, self._norm(value)))
+        self._owner._bc_changed()
+
+    def insert(self, index, place, value):
+        self._items.insert(index, (place, self._norm(value)))
+        self._owner._bc_changed()
+
+    def clear(self):
+        self._items.clear()
+        self._owner._bc_changed()
+
+    def __delitem__(self, i):
+        del self._items[i]
+        self._owner._bc_changed()
+
+    def __getitem__(self, i):
+        return self._items[i]
+
+    def __len__(self):
+        return len(self._items)
+
+    def __iter__(self):
+        return iter(self._items)
+
+
+@dataclasses.dataclass
+class IterativeParams:
+    """``solver.iterative`` (plask/common/fem/iterative_matrix.hpp:25-94)."""
+
+    accelerator: str = "cg"
+    preconditioner: str = "ic"
+    maxit: int = 1000
+    maxerr: float = 1e-6
+    noconv: str = "warning"
+    nfact: int = 10
+    ns1: int = 5
+    ns2: int = 100000
+    lvfill: int = 0
+    ltrunc: int = 0
+    ndeg: int = 1
+    omega: float = 1.0
+    converged: bool = True
+    iters: int = 0
+    err: float = 0.0
+
+
+class Receiver:
+    """``inHeat``: heat density [W/m^3]; a constant, an element array, or a callable of midpoints."""
+
+    def __init__(self, owner, default=0.0):
+        self._owner = owner
+        self._value = default
+
+    def attach(self, value):
+        self._value = value
+        self._owner._heat_changed()
+
+    def __call__(self, mesh: RectangularMesh3D):
+        v = self._value
+        if hasattr(v, "__call__") and not isinstance(v, np.ndarray):
+            mids = mesh.element_midpoints()
+            return np.broadcast_to(np.asarray(v(mids[..., 0], mids[..., 1], mids[..., 2]), np.float64),
+                                   mesh.element_shape)
+        arr = np.asarray(v, np.float64)
+        return np.broadcast_to(arr, mesh.element_shape)
+
+
+class Provider:
+    def __init__(self, fn):
+        self._fn = fn
+
+    def __call__(self, mesh=None, interpolation="linear"):
+        return self._fn(mesh, interpolation)
+
+
+def _interp_axis(axis, x):
+    """Bracketing indices and weights of points x on an increasing axis (clamped)."""
+    i = np.clip(np.searchsorted(axis, x, side="right") - 1, 0, axis.size - 2)
+    w = (x - axis[i]) / (axis[i + 1] - axis[i])
+    inside = (x >= axis[0]) & (x <= axis[-1])
+    return i, np.clip(w, 0.0, 1.0), inside
+
+
+class Static3D:
+    """Finite element thermal solver for 3D geometry, computed on the GPU.
+
+    Attributes (therm_python.cpp:136-151, fem/python.hpp:31-41, therm3d.cpp:20-33):
+    ``geometry``, ``mesh``, ``inittemp`` (300 K), ``maxerr`` (0.05 K),
+    ``algorithm`` ("iterative"; also "cholesky", "gauss", "gpu-pcg",
+    "gpu-mixed", "gpu-learned"), ``iterative`` (maxit, maxerr, noconv, ...),
+    ``empty_elements`` ("default", "exclude", "include"), the four
+    boundary-condition lists, ``inHeat``/``inHeatDensity`` and the providers
+    ``outTemperature``, ``outHeatFlux``, ``outThermalConductivity``.
+
+    Extra GPU knobs: ``rtol`` (FP64 relative residual of every linear solve,
+    default 1e-14) and ``bc_compat`` (True: the reference's placement of 3D
+    face boundary terms).
+    """
+
+    def __init__(self, name=""):
+        self.name = name
+        self._geometry = None
+        self._mesh = None
+        self.inittemp = 300.0
+        self.maxerr = 0.05
+        self._algorithm = "iterative"
+        self.iterative = IterativeParams()
+        self._empty_elements = "default"
+        self.rtol = 1e-14
+        self.bc_compat = True
+        self.temperature_boundary = BoundaryConditions(self, _native.BC_TEMPERATURE, 1)
+        self.heatflux_boundary = BoundaryConditions(self, _native.BC_HEATFLUX, 1)
+        self.convection_boundary = BoundaryConditions(self, _native.BC_CONVECTION, 2)
+        self.radiation_boundary = BoundaryConditions(self, _native.BC_RADIATION, 2)
+        self._inHeat = Receiver(self)
+        self.outTemperature = Provider(self._get_temperatures)
+        self.outHeatFlux = Provider(self._get_heat_fluxes)
+        self.outThermalConductivity = Provider(self._get_conductivity)
+        self._fem = None
+        self._elements_dirty = True
+        self._bc_dirty = True
+        self._heat_dirty = True
+        self._toterr = 0.0
+        self.stats = {}
+        self.loop_log = []
+
+    # ---------------------------------------------------------------- properties
+    @property
+    def id(self):
+        return f"{self.name}:thermal.Static3D" if self.name else "thermal.Static3D"
+
+    @property
+    def geometry(self):
+        return self._geometry
+
+    @geometry.setter
+    def geometry(self, g):
+        self._geometry = g
+        self.invalidate()
+        self._elements_dirty = True
+
+    @property
+    def mesh(self):
+        return self._mesh
+
+    @mesh.setter
+    def mesh(self, m):
+        self._mesh = m
+        self.invalidate()
+        self._fem = None
+
+    @property
+    def algorithm(self):
+        return self._algorithm
+
+    @algorithm.setter
+    def algorithm(self, a):
+        if a not in _native.ALGORITHMS:
+            raise BadInput(-1, f"unknown algorithm {a!r}")
+        self._algorithm = a
+
+    @property
+    def empty_elements(self):
+        return self._empty_elements
+
+    @empty_elements.setter
+    def empty_elements(self, v):
+        if v not in _native.EMPTY:
+            raise BadInput(-1, f"unknown empty_elements {v!r}")
+        self._empty_elements = v
+        self.invalidate()
+
+    @property
+    def inHeat(self):
+        return self._inHeat
+
+    @inHeat.setter
+    def inHeat(self, v):
+        self._inHeat.attach(v)
+
+    inHeatDensity = inHeat
+
+    @property
+    def err(self):
+        """Maximum estimated error of the last compute() (therm3d.hpp:111)."""
+        return self._toterr
+
+    # ---------------------------------------------------------------- lifecycle
+    def _bc_changed(self):
+        self._bc_dirty = True
+
+    def _heat_changed(self):
+        self._heat_dirty = True
+
+    def initialize(self):
+        if self._geometry is None:
+            raise BadInput(-1, f"{self.id}: No geometry specified")
+        if self._mesh is None:
+            raise BadInput(-1, f"{self.id}: No mesh specified")
+        if self._fem is None:
+            self._fem = _native.Fem3D(self._mesh.axes, self._mesh.ordering)
+            self._fem.set_log_callback(self._log)
+            self._elements_dirty = self._bc_dirty = self._heat_dirty = True
+        fem = self._fem
+        if self._elements_dirty:
+            mt = self._geometry.materials
+            fem.set_materials(mt.k300, mt.p, mt.kz_ratio, mt.hexp, mt.empty)
+            mat = self._geometry.material_ids(self._mesh)
+            leaf = self._geometry.leaf_height(self._mesh)
+            order = self._mesh.ordering
+            fem.set_elements(to_mesh_order(mat, order), to_mesh_order(self._inHeat(self._mesh), order),
+                             None if leaf is None else to_mesh_order(leaf, order))
+            self._elements_dirty = False
+            self._heat_dirty = False
+        elif self._heat_dirty:
+            fem.set_heat(to_mesh_order(self._inHeat(self._mesh), self._mesh.ordering))
+            self._heat_dirty = False
+        if self._bc_dirty:
+            for kind, lst in ((_native.BC_TEMPERATURE, self.temperature_boundary),
+                              (_native.BC_HEATFLUX, self.heatflux_boundary),
+                              (_native.BC_CONVECTION, self.convection_boundary),
+                              (_native.BC_RADIATION, self.radiation_boundary)):
+                fem.clear_bc(kind)
+                for place, vals in lst:
+                    nodes = place.nodes(self._mesh) if hasattr(place, "nodes") else np.asarray(place, np.int64)
+                    fem.add_bc(kind, nodes, *vals)
+            self._bc_dirty = False
+        it = self.iterative
+        maxit = it.maxit if self._algorithm == "iterative" and it.maxit != 1000 else 0
+        fem.set_solver(self._algorithm, self.rtol, maxit, it.noconv, self._empty_elements, self.bc_compat)
+        fem.set_loop(self.inittemp, self.maxerr)
+
+    def invalidate(self):
+        """Forget the computed temperatures (therm3d.cpp:118-122)."""
+        if self._fem is not None:
+            self._fem.invalidate()
+        self._elements_dirty = True
+
+    def _log(self, level, msg):
+        if msg.startswith("Loop "):
+            self.loop_log.append(msg)
+        lvl = {2: logging.WARNING, 3: logging.INFO, 4: logging.INFO}.get(level, logging.DEBUG)
+        log.log(lvl, "%s: %s", self.id, msg)
+
+    # ---------------------------------------------------------------- computation
+    def compute(self, loops=0):
+        """Run thermal calculations; returns the maximum temperature correction (therm3d.cpp:281-340)."""
+        self.initialize()
+        self.loop_log = []
+        tot, st = self._fem.compute(loops)
+        self._toterr = tot
+        self.stats = st
+        self.iterative.converged = bool(st["converged"])
+        self.iterative.iters = st["inner_iterations"]
+        self.iterative.err = st["last_rel_residual"]
+        return tot
+
+    # ---------------------------------------------------------------- results
+    def temperatures(self):
+        """Nodal temperatures in the solver's numbering (masked mesh, mesh order)."""
+        self.initialize()
+        return self._fem.temperature()
+
+    def _full_temperature(self):
+        """Canonical (n2, n1, n0) temperature with NaN at nodes outside the masked mesh."""
+        t = self._fem.temperature()
+        n = len(self._mesh)
+        canon_idx = self._mesh.index_array().ravel()
+        full = np.full(n, np.nan)
+        if t.size == n:
+            full = t[canon_idx]
+        else:
+            nn, _ = self._fem.sizes()
+            # masked numbering: active nodes in mesh order
+            act = self._active_mask_mesh_order()
+            vals = np.full(n, np.nan)
+            vals[np.flatnonzero(act)] = t
+            full = vals[canon_idx]
+        return full.reshape(self._mesh.shape)
+
+    def _active_mask_mesh_order(self):
+        mesh = self._mesh
+        mat = self._geometry.material_ids(mesh)
+        mt = self._geometry.materials
+        excl = self._empty_elements in ("exclude", "excluded") or (
+            self._empty_elements == "default" and self._algorithm != "iterative")
+        act_el = ~mt.empty[mat] if excl else np.ones(mat.shape, bool)
+        n2, n1, n0 = mesh.shape
+        used = np.zeros(mesh.shape, bool)
+        for ck in (0, 1):
+            for cj in (0, 1):
+                for ci in (0, 1):
+                    used[ck:n2 - 1 + ck, cj:n1 - 1 + cj, ci:n0 - 1 + ci] |= act_el
+        return to_mesh_order(used, mesh.ordering)
+
+    def _get_temperatures(self, dst_mesh, interpolation="linear"):
+        """Temperatures on a destination mesh (therm3d.cpp:387-395): trilinear, 300 K outside."""
+        if self._fem is None:
+            n = len(dst_mesh) if dst_mesh is not None else 0
+            return np.full(n, self.inittemp)
+        T = self._full_temperature()
+        if dst_mesh is None:
+            return T
+        pts = _points(dst_mesh)
+        return _trilinear(self._mesh.axes, T, pts, fill=300.0)
+
+    def heat_fluxes(self):
+        """Per-element heat flux [W/m^2], canonical (ne2, ne1, ne0, 3) (saveHeatFluxes)."""
+        self.initialize()
+        q = self._fem.heat_flux()
+        eidx = self._mesh.element_index_array().ravel()
+        return q[eidx].reshape(self._mesh.element_shape + (3,))
+
+    def _get_heat_fluxes(self, dst_mesh, interpolation="linear"):
+        """Heat flux on a destination mesh (therm3d.cpp:398-411): linear over element midpoints, 0 outside."""
+        if self._fem is None:
+            n = len(dst_mesh) if dst_mesh is not None else 0
+            return np.zeros((n, 3))
+        q = np.nan_to_num(self.heat_fluxes())
+        if dst_mesh is None:
+            return q
+        mids = [0.5 * (a[1:] + a[:-1]) for a in self._mesh.axes]
+        pts = _points(dst_mesh)
+        out = np.stack([_trilinear(mids, q[..., c], pts, fill=0.0, clamp=True, box=self._mesh.axes)
+                        for c in range(3)], axis=-1)
+        return out
+
+    def _get_conductivity(self, dst_mesh, interpolation="linear"):
+        """(k_xy, k_z) of the element holding each point (therm3d.cpp:421-435)."""
+        self.initialize()
+        k = self._fem.conductivity()
+        eidx = self._mesh.element_index_array().ravel()
+        k = k[eidx].reshape(self._mesh.element_shape + (2,))
+        if dst_mesh is None:
+            return k
+        pts = _points(dst_mesh)
+        idx = []
+        ok = np.ones(len(pts), bool)
+        for d, a in enumerate(self._mesh.axes):
+            u = np.searchsorted(a, pts[:, d], side="left")  # findUpIndex
+            ok &= (u > 0) & (u < a.size)
+            idx.append(np.clip(u - 1, 0, a.size - 2))
+        out = k[idx[2], idx[1], idx[0]]
+        out[~ok] = np.nan
+        return out
+
+    def thickness(self):
+        """Layer-run thickness per element, canonical shape (onInitialize, therm3d.cpp:81-113)."""
+        self.initialize()
+        th = self._fem.thickness()
+        eidx = self._mesh.element_index_array().ravel()
+        return th[eidx].reshape(self._mesh.element_shape)
+
+
+def _points(dst):
+    if isinstance(dst, RectangularMesh3D):
+        Z, Y, X = np.meshgrid(dst.axis2, dst.axis1, dst.axis0, indexing="ij")
+        pts = np.stack([X, Y, Z], axis=-1).reshape(-1, 3)
+        order = dst.index_array().ravel()
+        out = np.empty_like(pts)
+        out[order] = pts
+        return out
+    return np.asarray(dst, np.float64).reshape(-1, 3)
+
+
+def _trilinear(axes, F, pts, fill, clamp=False, box=None):
+    """Trilinear interpolation of canonical F (n2, n1, n0) at points (m, 3)."""
+    ii, ww, ok = [], [], np.ones(len(pts), bool)
+    for d in range(3):
+        a = axes[d]
+        if a.size == 1:
+            i = np.zeros(len(pts), np.int64)
+            w = np.zeros(len(pts))
+            inside = np.ones(len(pts), bool)
+        else:
+            i, w, inside = _interp_axis(a, pts[:, d])
+        if clamp:
+            b = box[d]
+            inside = (pts[:, d] >= b[0]) & (pts[:, d] <= b[-1])
+        ii.append(i)
+        ww.append(w)
+        ok &= inside
+    out = np.zeros(len(pts))
+    for ck in (0, 1):
+        for cj in (0, 1):
+            for ci in (0, 1):
+                wt = (ww[0] if ci else 1 - ww[0]) * (ww[1] if cj else 1 - ww[1]) * (ww[2] if ck else 1 - ww[2])
+                k = np.minimum(ii[2] + ck, F.shape[0] - 1)
+                j = np.minimum(ii[1] + cj, F.shape[1] - 1)
+                i = np.minimum(ii[0] + ci, F.shape[2] - 1)
+                out += wt * F[k, j, i]
+    out[~ok] = fill
+    return out
+
+
+def solver_for_structure(s, ordering="best", algorithm="gpu-mixed", name="", **kw):
+    """A configured :class:`Static3D` for a generated structure (plask_gb300.structures)."""
+    mesh = RectangularMesh3D(*s.axes, ordering=ordering)
+    sv = Static3D(name)
+    sv.geometry = StructureGeometry.from_structure(s)
+    sv.mesh = mesh
+    sv.inHeat = s.heat
+    sv.inittemp = s.inittemp
+    sv.maxerr = s.maxerr
+    sv.algorithm = algorithm
+    for side, v in s.temperature:
+        sv.temperature_boundary.append(RectangularMesh3D.side(side), v)
+    for side, v in s.heatflux:
+        sv.heatflux_boundary.append(RectangularMesh3D.side(side), v)
+    for side, h, ta in s.convection:
+        sv.convection_boundary.append(RectangularMesh3D.side(side), {"coeff": h, "ambient": ta})
+    for side, e, ta in s.radiation:
+        sv.radiation_boundary.append(RectangularMesh3D.side(side), {"emissivity": e, "ambient": ta})
+    for k, v in kw.items():
+        setattr(sv, k, v)
+    return sv

@@ -1,0 +1,74 @@
+"""GPU solver against the FP64 oracle (band Cholesky, a restatement of therm3d.cpp).
+
+Parity bar: max |dT| <= 1e-6 K against the oracle, the same number of outer
+k(T) iterations, and the same toterr to 1e-6 K."""
+import numpy as np
+import pytest
+
+from oracle import fem3d as O
+from plask_gb300 import structures as S
+from plask_gb300 import thermal as TH
+
+pytestmark = pytest.mark.gpu
+
+TOL_T = 1e-6  # K
+
+
+def _gpu(s, order, algorithm, **kw):
+    sv = TH.solver_for_structure(s, ordering=order, algorithm=algorithm, **kw)
+    tot = sv.compute()
+    return sv, sv._full_temperature(), tot
+
+
+CASES = [
+    ("c0", lambda: S.layered_c0(seed=3, n=(10, 12, 16)), "201"),
+    ("c0-012", lambda: S.layered_c0(seed=4, n=(9, 9, 14)), "012"),
+    ("c1", lambda: S.layered_c1(seed=5, n=(12, 10, 18)), "201"),
+    ("c1-210", lambda: S.layered_c1(seed=6, n=(11, 13, 15)), "210"),
+]
+
+
+@pytest.mark.parametrize("algorithm", ["gpu-pcg", "gpu-mixed", "cholesky", "iterative"])
+@pytest.mark.parametrize("name,make,order", CASES, ids=[c[0] for c in CASES])
+def test_compute_matches_oracle(name, make, order, algorithm):
+    s = make()
+    To, tot_o, rec = O.compute(O.from_structure(s, order=order))
+    sv, T, tot = _gpu(s, order, algorithm)
+    assert sv.stats["loops"] == len(rec)
+    assert np.max(np.abs(T - To)) <= TOL_T
+    assert abs(tot - tot_o) <= TOL_T
+    assert abs(sv.stats["max_t"] - rec[-1].maxT) <= TOL_T
+
+
+def test_outer_iterations_one_by_one():
+    """compute(1) repeatedly follows the oracle's loop body step by step (therm3d.cpp:311-333)."""
+    s = S.layered_c1(seed=8, n=(10, 9, 15))
+    order = "201"
+    p = O.from_structure(s, order=order)
+    sv = TH.solver_for_structure(s, ordering=order, algorithm="gpu-mixed")
+    To = np.full(p.shape, 300.0)
+    for loop in range(4):
+        err = sv.compute(1)
+        To_next, _ = O.outer_step(p, To)
+        T = sv._full_temperature()
+        assert np.max(np.abs(T - To_next)) <= TOL_T
+        assert abs(err - np.max(np.abs(To_next - To))) <= TOL_T
+        assert sv.stats["total_loops"] == loop + 1
+        To = To_next
+
+
+def test_heat_flux_conductivity_thickness_match_oracle():
+    s = S.layered_c1(seed=9, n=(9, 11, 16))
+    order = "201"
+    p = O.from_structure(s, order=order)
+    To, _, _ = O.compute(p)
+    sv, T, _ = _gpu(s, order, "gpu-mixed")
+    q_o = O.heat_fluxes(p, To)
+    q = sv.heat_fluxes()
+    scale = np.max(np.abs(q_o))
+    assert np.max(np.abs(q - q_o)) <= 1e-6 * scale
+    assert np.allclose(sv.thickness(), O.element_thickness(p), rtol=0, atol=1e-12)
+    kxy, kz = O.element_k(p, To)
+    k = sv.outThermalConductivity()
+    assert np.allclose(k[..., 0].ravel(), kxy, rtol=1e-9)
+    assert np.allclose(k[..., 1].ravel(), kz, rtol=1e-9)
