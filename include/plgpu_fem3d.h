@@ -89,6 +89,7 @@ typedef struct plgpu_stats {
     double last_rel_residual; /* FP64 ||b - A T|| / ||b|| of the last solve */
     double solve_ms;        /* device time of the linear solves [ms] */
     double total_ms;        /* device time of the whole call [ms] */
+    long long kernel_launches; /* CUDA kernels this library launched during the call */
 } plgpu_stats;
 
 /* Create a solver on a rectilinear mesh.  Replaces mesh setup and
@@ -185,6 +186,23 @@ int plgpu_fem3d_get_thickness(plgpu_fem3d* h, double* out);
 
 /* The CUDA stream the handle launches on (cudaStream_t), for event timing. */
 void* plgpu_fem3d_stream(plgpu_fem3d* h);
+
+/* y = A x with the system matrix of the current temperature field
+   (FemMatrix::mult, plask/common/fem/matrix.hpp:84-89): the stiffness matrix
+   of setMatrix after Dirichlet elimination (identity rows and zero couplings
+   for Dirichlet nodes), including convective face terms.  x and y are full
+   node arrays in mesh order.  precision: 64 (FP64 operator) or 32 (the FP32
+   operator of the inner solver, result widened to double). */
+int plgpu_fem3d_mult(plgpu_fem3d* h, int precision, const double* x, double* y);
+
+/* Time the operator kernel (one matrix-free stiffness application, the
+   inner kernel of every CG iteration) on the handle's stream with CUDA
+   events: `reps` launches on the current coefficients, optionally with the
+   L2 cache flushed before each launch.  precision: 32 or 64.
+   *avg_ms: mean launch duration; *bytes_per_launch: algorithmic bytes of
+   one launch (read x, write y, the element conductivities). */
+int plgpu_fem3d_time_operator(plgpu_fem3d* h, int precision, int reps, int flush_l2, double* avg_ms,
+                              double* bytes_per_launch);
 
 /* Receive the solver's log lines (Solver::writelog, plask/log/log.hpp:27-42).
    level follows PLaSK's LogLevel numbering (2 warning, 3 info, 4 result,

@@ -241,6 +241,28 @@ def assemble(prob: Problem, T, thickness=None, node_id=None, n_active=None):
     Returns (A, F, node_id, n_active) where A is a symmetric scipy CSR matrix over the
     masked-mesh numbering and F the load vector.
     """
+    ids, K, F, node_id, n_active = element_terms(prob, T, thickness, node_id, n_active)
+    rows, cols, data = [], [], []
+    for (a, b), v in K.items():
+        ra, cb = ids[a], ids[b]
+        rows.append(ra); cols.append(cb); data.append(v)
+        if a != b:
+            rows.append(cb); cols.append(ra); data.append(v)
+    A = sp.csr_matrix((np.concatenate(data), (np.concatenate(rows), np.concatenate(cols))),
+                      shape=(n_active, n_active))
+    Fv = np.zeros(n_active)
+    for a in range(8):
+        np.add.at(Fv, ids[a], F[a])
+    return A, Fv, node_id, n_active
+
+
+def element_terms(prob: Problem, T, thickness=None, node_id=None, n_active=None):
+    """Per-element stiffness entries and loads of setMatrix (therm3d.cpp:186-268).
+
+    Returns (ids, K, F, node_id, n_active): ids (8, ne) masked node ids of the
+    active elements' corners, K {(a, b): values} for b <= a (lower triangle of
+    K_e including the boundary-face terms) and F [8 arrays] the element loads.
+    """
     shape = prob.shape
     n2, n1, n0 = shape
     if node_id is None:
@@ -327,18 +349,7 @@ def assemble(prob: Problem, T, thickness=None, node_id=None, n_active=None):
             return -0.25e-12 * area * v[0] * SB * (t * t - a * a)
         faces(has, vals, rad, None)
 
-    rows, cols, data = [], [], []
-    for (a, b), v in K.items():
-        ra, cb = ids[a], ids[b]
-        rows.append(ra); cols.append(cb); data.append(v)
-        if a != b:
-            rows.append(cb); cols.append(ra); data.append(v)
-    A = sp.csr_matrix((np.concatenate(data), (np.concatenate(rows), np.concatenate(cols))),
-                      shape=(n_active, n_active))
-    Fv = np.zeros(n_active)
-    for a in range(8):
-        np.add.at(Fv, ids[a], F[a])
-    return A, Fv, node_id, n_active
+    return ids, K, F, node_id, n_active
 
 
 def dirichlet_values(prob: Problem, node_id, n_active):

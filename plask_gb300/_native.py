@@ -37,6 +37,7 @@ class Stats(C.Structure):
         ("last_rel_residual", C.c_double),
         ("solve_ms", C.c_double),
         ("total_ms", C.c_double),
+        ("kernel_launches", C.c_longlong),
     ]
 
     def as_dict(self):
@@ -73,6 +74,8 @@ SIGNATURES = {
     "plgpu_fem3d_get_thickness": (C.c_int, [_h, _dp]),
     "plgpu_fem3d_stream": (C.c_void_p, [_h]),
     "plgpu_fem3d_set_log_callback": (C.c_int, [_h, LOG_CB, C.c_void_p]),
+    "plgpu_fem3d_time_operator": (C.c_int, [_h, C.c_int, C.c_int, C.c_int, _dp, _dp]),
+    "plgpu_fem3d_mult": (C.c_int, [_h, C.c_int, _dp, _dp]),
 }
 
 _lib = None
@@ -251,6 +254,20 @@ class Fem3D:
         out = np.empty(ne)
         self._check(self._lib.plgpu_fem3d_get_thickness(self._h, _ptr(out, C.c_double)))
         return out
+
+    def mult(self, x, precision=64):
+        """y = A x with the current system matrix; x, y full node arrays in mesh order."""
+        xv = _f64(x).ravel()
+        y = np.empty_like(xv)
+        self._check(self._lib.plgpu_fem3d_mult(self._h, int(precision), _ptr(xv, C.c_double), _ptr(y, C.c_double)))
+        return y
+
+    def time_operator(self, precision=32, reps=20, flush_l2=True):
+        """(mean ms per launch, algorithmic bytes per launch) of the stiffness-operator kernel."""
+        ms, by = C.c_double(0.0), C.c_double(0.0)
+        self._check(self._lib.plgpu_fem3d_time_operator(self._h, int(precision), int(reps), 1 if flush_l2 else 0,
+                                                        C.byref(ms), C.byref(by)))
+        return ms.value, by.value
 
     def stream(self):
         return self._lib.plgpu_fem3d_stream(self._h)

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -95,6 +96,7 @@ struct plgpu_fem3d {
     int sm_count = 0;
 
     DevBuf h64[3], r64[3], h32[3], r32[3], z64;
+    DevBuf zf64, zr64, zf32, zr32;  // dz / 48 and 1 / (48 dz) per element layer
     GridT<double> g64{};
     GridT<float> g32{};
 
@@ -163,7 +165,24 @@ struct plgpu_fem3d {
 
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
 
+    // CUDA graphs of CG chunks: one per (precision, chunk length)
+    struct ChunkGraph {
+        int len = 0;
+        bool fp64 = false;
+        cudaGraphExec_t exec = nullptr;
+        long long kernels = 0;
+    };
+    std::vector<ChunkGraph> graphs;
+    bool use_graphs = true;
+
+    void invalidate_graphs() {
+        for (auto& g : graphs)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+        graphs.clear();
+    }
+
     ~plgpu_fem3d() {
+        invalidate_graphs();
         if (h_ctl) cudaFreeHost(h_ctl);
         for (cudaEvent_t e : {ev0, ev1, ev2, ev3})
             if (e) cudaEventDestroy(e);
@@ -214,6 +233,8 @@ struct plgpu_fem3d {
         ck(cudaGetDevice(&dev), "cudaGetDevice");
         ck(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
         cfg.stream = stream;
+        cfg.sm_count = sm_count;
+        if (const char* e = std::getenv("PLGPU_NO_GRAPHS")) use_graphs = !(e[0] == '1');
         cfg.vec_blocks = sm_count * 4;
         if (cfg.vec_blocks > kMaxPartialBlocks) cfg.vec_blocks = kMaxPartialBlocks;
         // choose z-planes per operator block so that the block count stays within the partial slots
@@ -236,6 +257,21 @@ struct plgpu_fem3d {
             upload(r32[d], rf, stream);
         }
         upload(z64, ax[2], stream);
+        {
+            std::vector<double> zf(n[2] - 1), zr(n[2] - 1);
+            std::vector<float> zff(n[2] - 1), zrf(n[2] - 1);
+            for (int k = 0; k < n[2] - 1; ++k) {
+                const double dz = ax[2][k + 1] - ax[2][k];
+                zf[k] = dz / 48.0;
+                zr[k] = 1.0 / (48.0 * dz);
+                zff[k] = (float)zf[k];
+                zrf[k] = (float)zr[k];
+            }
+            upload(zf64, zf, stream);
+            upload(zr64, zr, stream);
+            upload(zf32, zff, stream);
+            upload(zr32, zrf, stream);
+        }
         g64 = GridT<double>{n[0], n[1], n[2], N, h64[0].as<double>(), h64[1].as<double>(), h64[2].as<double>(),
                             r64[0].as<double>(), r64[1].as<double>(), r64[2].as<double>()};
         g32 = GridT<float>{n[0], n[1], n[2], N, h32[0].as<float>(), h32[1].as<float>(), h32[2].as<float>(),
@@ -318,6 +354,7 @@ struct plgpu_fem3d {
             kz64.alloc((size_t)N * 8);
             kz32.alloc((size_t)N * 4);
         }
+        invalidate_graphs();
         invalidate_solution();
     }
 
@@ -440,8 +477,7 @@ struct plgpu_fem3d {
         // thickness of layer runs
         launch_thickness(cfg, n[0], n[1], n[2], d_mat.as<int>(), z64.as<double>(), d_th.as<double>());
         // temperatures = inittemp
-        std::vector<double> t0((size_t)N, inittemp);
-        ck(cudaMemcpyAsync(T.p, t0.data(), (size_t)N * 8, cudaMemcpyHostToDevice, stream), "H2D T");
+        launch_fill(cfg, N, T.as<double>(), inittemp);
         ck(cudaStreamSynchronize(stream), "sync");
         loopno = 0;
         initialized = true;
@@ -467,6 +503,7 @@ struct plgpu_fem3d {
     }
 
     void materialize_bc() {
+        invalidate_graphs();  // the surface operator's device arrays are reallocated below
         // Dirichlet set: v_first eliminates, v_last stays in the row (matrix.hpp:132-145)
         std::unordered_map<long long, std::pair<double, double>> dval;
         std::vector<long long> dorder;
@@ -695,6 +732,20 @@ struct plgpu_fem3d {
     // ---------------------------------------------------------------------------------
     // the linear solves
 
+    // y = A x (or a variant, see MODE_*) with the optimised operator and the current coefficients
+    void op64(const double* x, double* y, const double* rhs, int mode) {
+        launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), x, y, k64.as<double>(),
+                        aniso ? kz64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(), rhs, partials.as<double>(),
+                        mode, d_ctl.as<SolveCtl>());
+    }
+    void op32(const float* x, float* y, int mode) {
+        launch_operator(cfg, g32, zf32.as<float>(), zr32.as<float>(), x, y, k32.as<float>(),
+                        aniso ? kz32.as<float>() : nullptr, aniso, dmask.as<uint32_t>(), (const float*)nullptr,
+                        partials.as<double>(), mode, d_ctl.as<SolveCtl>());
+    }
+    void opR(const double* x, double* y, int mode) { op64(x, y, nullptr, mode); }
+    void opR(const float* x, float* y, int mode) { op32(x, y, mode); }
+
     SolveCtl read_ctl() {
         ck(cudaMemcpyAsync(h_ctl, d_ctl.p, sizeof(SolveCtl), cudaMemcpyDeviceToHost, stream), "D2H ctl");
         ck(cudaStreamSynchronize(stream), "sync");
@@ -712,14 +763,41 @@ struct plgpu_fem3d {
                        const R* minv, int& status, int& iters, int cap) {
         SolveCtl* ctl = d_ctl.as<SolveCtl>();
         double* part = partials.as<double>();
-        const int slot0 = apply_blocks(cfg, n[0], n[1], n[2]);
-        int ch = chunk;
-        for (;;) {
-            for (int it = 0; it < ch; ++it) {
-                launch_apply(cfg, g, p, q, kx, kz, aniso, dmask.as<uint32_t>(), (const R*)nullptr, part, MODE_CG, ctl);
+        const int slot0 = op_blocks(cfg, n[0], n[1], n[2], sizeof(R) == 8);
+        auto enqueue = [&](int len) {
+            for (int it = 0; it < len; ++it) {
+                opR(p, q, MODE_CG);
                 launch_surface(cfg, s, p, q, part, slot0, MODE_CG, ctl);
                 launch_cg_update(cfg, N, x, r, p, q, minv, part, ctl);
                 launch_cg_direction(cfg, N, p, r, minv, ctl);
+            }
+        };
+        int ch = chunk;
+        for (;;) {
+            if (use_graphs) {
+                ChunkGraph* gr = nullptr;
+                for (auto& g : graphs)
+                    if (g.len == ch && g.fp64 == (sizeof(R) == 8)) gr = &g;
+                if (!gr) {
+                    ChunkGraph g;
+                    g.len = ch;
+                    g.fp64 = sizeof(R) == 8;
+                    cudaGraph_t graph = nullptr;
+                    ck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+                    const long long before = launch_count();
+                    enqueue(ch);
+                    g.kernels = launch_count() - before;
+                    count_launches(-g.kernels);  // captured, not run
+                    ck(cudaStreamEndCapture(stream, &graph), "end capture");
+                    ck(cudaGraphInstantiate(&g.exec, graph, 0), "graph instantiate");
+                    cudaGraphDestroy(graph);
+                    graphs.push_back(g);
+                    gr = &graphs.back();
+                }
+                ck(cudaGraphLaunch(gr->exec, stream), "graph launch");
+                count_launches(gr->kernels);
+            } else {
+                enqueue(ch);
             }
             ck(cudaGetLastError(), "launch");
             SolveCtl c = read_ctl();
@@ -763,8 +841,7 @@ struct plgpu_fem3d {
 
     // r64 = b - A T (Dirichlet columns eliminated)
     void residual64() {
-        launch_apply(cfg, g64, T.as<double>(), r64v.as<double>(), k64.as<double>(), aniso ? kz64.as<double>() : nullptr,
-                     aniso, dmask.as<uint32_t>(), b.as<double>(), partials.as<double>(), MODE_RESID, nullptr);
+        op64(T.as<double>(), r64v.as<double>(), b.as<double>(), MODE_RESID);
         launch_surface(cfg, s64, T.as<double>(), r64v.as<double>(), partials.as<double>(), 0, MODE_RESID,
                        d_ctl.as<SolveCtl>());
     }
@@ -824,6 +901,7 @@ struct plgpu_fem3d {
     double compute(int loops, plgpu_stats* st) {
         if (!initialized) initialize();
         if (bc_dirty) materialize_bc();
+        const long long launches0 = launch_count();
         ck(cudaEventRecord(ev0, stream), "event");
         if (heat_dirty) build_static_load();
         log(3, "Running thermal calculations");
@@ -840,9 +918,7 @@ struct plgpu_fem3d {
                         aniso ? kz32.as<float>() : nullptr, aniso);
             launch_diag(cfg, g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, s64,
                         dmask.as<uint32_t>(), diag.as<double>(), minv64.as<double>(), minv32.as<float>());
-            launch_apply(cfg, g64, vD.as<double>(), b.as<double>(), k64.as<double>(),
-                         aniso ? kz64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(), F.as<double>(),
-                         partials.as<double>(), MODE_RHS, nullptr);
+            op64(vD.as<double>(), b.as<double>(), F.as<double>(), MODE_RHS);
             launch_radiation(cfg, rad_rows, rad_row.as<int>(), rad_ptr.as<int>(), rad_src.as<int>(),
                              rad_coef.as<double>(), rad_tamb.as<double>(), T.as<double>(), b.as<double>());
             launch_set_dirichlet(cfg, (int)(d_didx.bytes / sizeof(int)), d_didx.as<int>(), d_dval.as<double>(),
@@ -901,8 +977,75 @@ struct plgpu_fem3d {
             st->last_rel_residual = relres;
             st->solve_ms = solve_ms;
             st->total_ms = tot;
+            st->kernel_launches = launch_count() - launches0;
         }
         return toterr;
+    }
+
+    // ---------------------------------------------------------------------------------
+    // timing of the operator kernel (the CG-mode stencil application) on the current state
+
+    void time_operator(int precision, int reps, int flush_l2, double* avg_ms, double* bytes) {
+        if (!initialized) initialize();
+        if (bc_dirty) materialize_bc();
+        if (reps <= 0) throw ArgError("reps must be positive");
+        // coefficients of the current temperature, a deterministic input vector
+        launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab, k64.as<double>(),
+                    k32.as<float>(), aniso ? kz64.as<double>() : nullptr, aniso ? kz32.as<float>() : nullptr, aniso);
+        launch_fill(cfg, N, p64.as<double>(), 1.0);
+        launch_norm2(cfg, N, p64.as<double>(), p32.as<float>(), partials.as<double>(), d_ctl.as<SolveCtl>(), 4);
+        SolveCtl* ctl = d_ctl.as<SolveCtl>();
+        ck(cudaMemsetAsync(&ctl->status, 0, sizeof(int), stream), "memset");  // SOLVE_RUNNING
+        DevBuf flush;
+        if (flush_l2) flush.alloc((size_t)512 << 20);  // well above the 126 MiB L2
+        float total = 0.f;
+        for (int r = 0; r < reps; ++r) {
+            if (flush_l2) ck(cudaMemsetAsync(flush.p, r & 0xff, flush.bytes, stream), "flush");
+            ck(cudaEventRecord(ev2, stream), "event");
+            if (precision == 64)
+                op64(p64.as<double>(), q64.as<double>(), nullptr, MODE_CG);
+            else
+                op32(p32.as<float>(), q32.as<float>(), MODE_CG);
+            ck(cudaEventRecord(ev3, stream), "event");
+            ck(cudaEventSynchronize(ev3), "sync");
+            float ms = 0.f;
+            ck(cudaEventElapsedTime(&ms, ev2, ev3), "elapsed");
+            total += ms;
+        }
+        ck(cudaGetLastError(), "launch");
+        *avg_ms = total / reps;
+        const double w = precision == 64 ? 8.0 : 4.0;
+        // algorithmic bytes: read x, write y, one (isotropic) or two conductivity words per element
+        *bytes = 2.0 * w * (double)N + 4.0 * (aniso ? 2.0 : 1.0) * (double)NE;
+    }
+
+    // y = A x with the system matrix of the current temperature (FemMatrix::mult, matrix.hpp:89):
+    // after Dirichlet elimination, including the convective face terms.  Mesh-order arrays.
+    void mult(int precision, const double* xin, double* yout) {
+        if (!initialized) initialize();
+        if (bc_dirty) materialize_bc();
+        launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab, k64.as<double>(),
+                    k32.as<float>(), aniso ? kz64.as<double>() : nullptr, aniso ? kz32.as<float>() : nullptr, aniso);
+        DevBuf tmp;
+        tmp.alloc((size_t)N * 8);
+        ck(cudaMemcpyAsync(tmp.p, xin, (size_t)N * 8, cudaMemcpyHostToDevice, stream), "H2D x");
+        launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], n[1], n[2], ns[0], ns[1], ns[2], tmp.as<double>(),
+                                   p64.as<double>(), 0.0);
+        if (precision == 64) {
+            op64(p64.as<double>(), q64.as<double>(), nullptr, MODE_MULT);
+            launch_surface(cfg, s64, p64.as<double>(), q64.as<double>(), partials.as<double>(), 0, MODE_MULT,
+                           d_ctl.as<SolveCtl>());
+        } else {
+            launch_norm2(cfg, N, p64.as<double>(), p32.as<float>(), partials.as<double>(), d_ctl.as<SolveCtl>(), 4);
+            op32(p32.as<float>(), q32.as<float>(), MODE_MULT);
+            launch_surface(cfg, s32, p32.as<float>(), q32.as<float>(), partials.as<double>(), 0, MODE_MULT,
+                           d_ctl.as<SolveCtl>());
+            launch_widen(cfg, N, q32.as<float>(), q64.as<double>());
+        }
+        launch_to_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], (long long)n[0] * n[1], ns[0], ns[1], ns[2], 1,
+                                 q64.as<double>(), tmp.as<double>());
+        ck(cudaMemcpyAsync(yout, tmp.p, (size_t)N * 8, cudaMemcpyDeviceToHost, stream), "D2H y");
+        ck(cudaStreamSynchronize(stream), "sync");
     }
 
     // ---------------------------------------------------------------------------------
@@ -1161,6 +1304,23 @@ int plgpu_fem3d_get_thickness(plgpu_fem3d* h, double* out) {
 }
 
 void* plgpu_fem3d_stream(plgpu_fem3d* h) { return h ? (void*)h->stream : nullptr; }
+
+int plgpu_fem3d_mult(plgpu_fem3d* h, int precision, const double* x, double* y) {
+    return guarded(h, [&] {
+        if (precision != 32 && precision != 64) throw ArgError("precision must be 32 or 64");
+        if (!x || !y) throw ArgError("null vector");
+        h->mult(precision, x, y);
+    });
+}
+
+int plgpu_fem3d_time_operator(plgpu_fem3d* h, int precision, int reps, int flush_l2, double* avg_ms,
+                              double* bytes_per_launch) {
+    return guarded(h, [&] {
+        if (precision != 32 && precision != 64) throw ArgError("precision must be 32 or 64");
+        if (!avg_ms || !bytes_per_launch) throw ArgError("null output");
+        h->time_operator(precision, reps, flush_l2, avg_ms, bytes_per_launch);
+    });
+}
 
 int plgpu_fem3d_set_log_callback(plgpu_fem3d* h, void (*cb)(void*, int, const char*), void* user) {
     return guarded(h, [&] {

@@ -15,6 +15,7 @@
 //
 // All reductions are deterministic: every block writes one partial per value
 // and the last block to arrive sums the partials in a fixed order.
+#include <atomic>
 #include <cfloat>
 #include <cstdint>
 
@@ -233,6 +234,8 @@ __global__ void __launch_bounds__(256) k_surface(const SurfaceT<R> s, const R* _
         if (MODE == MODE_CG) {
             y[n] += acc;
             dot += (double)x[n] * (double)acc;
+        } else if (MODE == MODE_MULT) {
+            y[n] += acc;
         } else {
             y[n] -= acc;
         }
@@ -266,16 +269,19 @@ __global__ void __launch_bounds__(256) k_cg_update(long long N, R* __restrict__ 
                                                    SolveCtl* __restrict__ ctl) {
     if (ctl->status != SOLVE_RUNNING) return;
     const R alpha = R(ctl->alpha);
-    double rz = 0.0, rr = 0.0;
+    // per-thread partial sums in R (a thread sees a few tens of entries); FP64 from the block level on
+    R rz = R(0), rr = R(0);
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
         const R pn = p[n];
         x[n] += alpha * pn;
-        const R rn = r[n] - alpha * q[n];
+        const R mn = minv[n];
+        // the operator leaves A p on Dirichlet rows: their residual is kept at zero (M^-1 = 0 marks them)
+        const R rn = mn != R(0) ? r[n] - alpha * q[n] : R(0);
         r[n] = rn;
-        rz += (double)rn * (double)(minv[n] * rn);
-        rr += (double)rn * (double)rn;
+        rz += rn * (mn * rn);
+        rr += rn * rn;
     }
-    double v[2] = {rz, rr};
+    double v[2] = {(double)rz, (double)rr};
     write_partial<2, OpSum>(v, partials, blockIdx.x);
     if (arrive_last(&ctl->arrive[1], gridDim.x)) {
         reduce_partials<2, OpSum>(v, partials, gridDim.x);
@@ -322,16 +328,16 @@ __global__ void __launch_bounds__(256) k_cg_start(long long N, R* __restrict__ x
                                                   R* __restrict__ p, const R* __restrict__ minv,
                                                   double* __restrict__ partials, SolveCtl* __restrict__ ctl,
                                                   double rtol, int ref_slot, int maxit, int stall_limit) {
-    double rz = 0.0, rr = 0.0;
+    R rz = R(0), rr = R(0);
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
         const R rn = r[n];
         const R zn = minv[n] * rn;
         p[n] = zn;
         if (ZERO_X) x[n] = R(0);
-        rz += (double)rn * (double)zn;
-        rr += (double)rn * (double)rn;
+        rz += rn * zn;
+        rr += rn * rn;
     }
-    double v[2] = {rz, rr};
+    double v[2] = {(double)rz, (double)rr};
     write_partial<2, OpSum>(v, partials, blockIdx.x);
     if (arrive_last(&ctl->arrive[1], gridDim.x)) {
         reduce_partials<2, OpSum>(v, partials, gridDim.x);
@@ -376,6 +382,11 @@ __global__ void __launch_bounds__(256) k_norm2(long long N, const double* __rest
         reduce_partials<1, OpSum>(w, partials, gridDim.x);
         if (linear_tid() == 0) ctl->red[slot] = w[0];
     }
+}
+
+__global__ void __launch_bounds__(256) k_fill(long long N, double* __restrict__ v, double value) {
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x)
+        v[n] = value;
 }
 
 // T += d (FP64 accumulation of an FP32 correction)
@@ -486,8 +497,9 @@ __global__ void __launch_bounds__(256) k_invert_diag(long long N, const double* 
                                                      const uint32_t* __restrict__ dmask, double* __restrict__ minv64,
                                                      float* __restrict__ minv32) {
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+        // Dirichlet (and decoupled) rows: M^-1 = 0, so that residual and search direction stay zero there
         double d = diag[n];
-        double v = (is_dir(dmask, n) || !(d > 0.0)) ? 1.0 : 1.0 / d;
+        double v = (is_dir(dmask, n) || !(d > 0.0)) ? 0.0 : 1.0 / d;
         minv64[n] = v;
         minv32[n] = (float)v;
     }
@@ -673,6 +685,18 @@ __global__ void k_scatter(long long n, const long long* __restrict__ idx, const 
 // ----------------------------------------------------------------------------------------
 // launchers
 
+// Every kernel launch goes through launch_kernel so that the number of launches
+// can be reported (plgpu_stats.kernel_launches).
+static std::atomic<long long> g_launches{0};
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+template <typename... KArgs, typename... Args>
+static inline void launch(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t stream, Args... args) {
+    launch_kernel(kern, grid, block, stream, args...);
+}
+
 static inline int grid_for(long long n, int threads, int cap) {
     long long b = (n + threads - 1) / threads;
     if (b < 1) b = 1;
@@ -690,10 +714,10 @@ static void launch_apply_any(const LaunchCfg& c, const GridT<R>& g, const R* x, 
 #define PLGPU_APPLY_CASE(MODEV)                                                                                          \
     if (mode == MODEV) {                                                                                                 \
         if (aniso)                                                                                                       \
-            k_apply_gather<R, true, MODEV><<<grid, block, 0, c.stream>>>(g, x, y, kxy, kz, dmask, rhs, partials, planes,  \
+            launch(k_apply_gather<R, true, MODEV>, grid, block, c.stream, g, x, y, kxy, kz, dmask, rhs, partials, planes,  \
                                                                          ctl);                                           \
         else                                                                                                             \
-            k_apply_gather<R, false, MODEV><<<grid, block, 0, c.stream>>>(g, x, y, kxy, kz, dmask, rhs, partials, planes, \
+            launch(k_apply_gather<R, false, MODEV>, grid, block, c.stream, g, x, y, kxy, kz, dmask, rhs, partials, planes, \
                                                                           ctl);                                          \
         return;                                                                                                          \
     }
@@ -724,10 +748,13 @@ static void launch_surface_any(const LaunchCfg& c, const SurfaceT<R>& s, const R
                                int mode, SolveCtl* ctl) {
     const int blocks = mode == MODE_CG ? surface_blocks(s.nrows) : grid_for(s.nrows, 256, 1024);
     if (mode == MODE_CG) {
-        k_surface<R, MODE_CG><<<blocks, 256, 0, c.stream>>>(s, x, y, partials, slot0, slot0 + blocks, ctl);
+        launch(k_surface<R, MODE_CG>, blocks, 256, c.stream, s, x, y, partials, slot0, slot0 + blocks, ctl);
+    } else if (mode == MODE_MULT) {
+        if (s.nrows == 0) return;
+        launch(k_surface<R, MODE_MULT>, blocks, 256, c.stream, s, x, y, partials, slot0, slot0 + blocks, ctl);
     } else {
         if (s.nrows == 0) return;
-        k_surface<R, MODE_RESID><<<blocks, 256, 0, c.stream>>>(s, x, y, partials, slot0, slot0 + blocks, ctl);
+        launch(k_surface<R, MODE_RESID>, blocks, 256, c.stream, s, x, y, partials, slot0, slot0 + blocks, ctl);
     }
 }
 int surface_blocks(int nrows) { return grid_for(nrows, 256, 64); }
@@ -745,7 +772,7 @@ int vec_blocks(const LaunchCfg& c, long long N) { return grid_for(N, 256, c.vec_
 template <typename R>
 static void cg_update_any(const LaunchCfg& c, long long N, R* x, R* r, const R* p, const R* q, const R* minv,
                           double* partials, SolveCtl* ctl) {
-    k_cg_update<R><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, x, r, p, q, minv, partials, ctl);
+    launch(k_cg_update<R>, vec_blocks(c, N), 256, c.stream, N, x, r, p, q, minv, partials, ctl);
 }
 void launch_cg_update(const LaunchCfg& c, long long N, double* x, double* r, const double* p, const double* q,
                       const double* minv, double* partials, SolveCtl* ctl) {
@@ -757,111 +784,121 @@ void launch_cg_update(const LaunchCfg& c, long long N, float* x, float* r, const
 }
 void launch_cg_direction(const LaunchCfg& c, long long N, double* p, const double* r, const double* minv,
                          const SolveCtl* ctl) {
-    k_cg_direction<double><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, p, r, minv, ctl);
+    launch(k_cg_direction<double>, vec_blocks(c, N), 256, c.stream, N, p, r, minv, ctl);
 }
 void launch_cg_direction(const LaunchCfg& c, long long N, float* p, const float* r, const float* minv,
                          const SolveCtl* ctl) {
-    k_cg_direction<float><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, p, r, minv, ctl);
+    launch(k_cg_direction<float>, vec_blocks(c, N), 256, c.stream, N, p, r, minv, ctl);
 }
 void launch_cg_start(const LaunchCfg& c, long long N, double* x, bool zero_x, const double* r, double* p,
                      const double* minv, double* partials, SolveCtl* ctl, double rtol, int ref_slot, int maxit,
                      int stall_limit) {
     if (zero_x)
-        k_cg_start<double, true><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, x, r, p, minv, partials, ctl, rtol, ref_slot,
+        launch(k_cg_start<double, true>, vec_blocks(c, N), 256, c.stream, N, x, r, p, minv, partials, ctl, rtol, ref_slot,
                                                                          maxit, stall_limit);
     else
-        k_cg_start<double, false><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, x, r, p, minv, partials, ctl, rtol,
+        launch(k_cg_start<double, false>, vec_blocks(c, N), 256, c.stream, N, x, r, p, minv, partials, ctl, rtol,
                                                                           ref_slot, maxit, stall_limit);
 }
 void launch_cg_start(const LaunchCfg& c, long long N, float* x, bool zero_x, const float* r, float* p,
                      const float* minv, double* partials, SolveCtl* ctl, double rtol, int ref_slot, int maxit,
                      int stall_limit) {
     if (zero_x)
-        k_cg_start<float, true><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, x, r, p, minv, partials, ctl, rtol, ref_slot,
+        launch(k_cg_start<float, true>, vec_blocks(c, N), 256, c.stream, N, x, r, p, minv, partials, ctl, rtol, ref_slot,
                                                                         maxit, stall_limit);
     else
-        k_cg_start<float, false><<<vec_blocks(c, N), 256, 0, c.stream>>>(N, x, r, p, minv, partials, ctl, rtol, ref_slot,
+        launch(k_cg_start<float, false>, vec_blocks(c, N), 256, c.stream, N, x, r, p, minv, partials, ctl, rtol, ref_slot,
                                                                          maxit, stall_limit);
 }
 void launch_norm2(const LaunchCfg& c, long long N, const double* v, float* v32, double* partials, SolveCtl* ctl,
                   int slot) {
-    k_norm2<<<vec_blocks(c, N), 256, 0, c.stream>>>(N, v, v32, partials, ctl, slot);
+    launch(k_norm2, vec_blocks(c, N), 256, c.stream, N, v, v32, partials, ctl, slot);
+}
+__global__ void __launch_bounds__(256) k_widen(long long N, const float* __restrict__ a, double* __restrict__ b) {
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x)
+        b[n] = (double)a[n];
+}
+void launch_widen(const LaunchCfg& c, long long N, const float* a, double* b) {
+    launch(k_widen, vec_blocks(c, N), 256, c.stream, N, a, b);
+}
+void launch_fill(const LaunchCfg& c, long long N, double* v, double value) {
+    launch(k_fill, vec_blocks(c, N), 256, c.stream, N, v, value);
 }
 void launch_add_correction(const LaunchCfg& c, long long N, double* T, const float* d) {
-    k_add_correction<<<vec_blocks(c, N), 256, 0, c.stream>>>(N, T, d);
+    launch(k_add_correction, vec_blocks(c, N), 256, c.stream, N, T, d);
 }
 void launch_thickness(const LaunchCfg& c, int n0, int n1, int n2, const int* mat, const double* z, double* th) {
     dim3 block(32, 8);
     dim3 grid((n0 + 30) / 32, (n1 + 6) / 8);
-    k_thickness<<<grid, block, 0, c.stream>>>(n0, n1, n2, mat, z, th);
+    launch(k_thickness, grid, block, c.stream, n0, n1, n2, mat, z, th);
 }
 void launch_coef(const LaunchCfg& c, int n0, int n1, int n2, const double* T, const int* mat, const double* th,
                  const MatTable& tab, double* k64, float* k32, double* kz64, float* kz32, bool aniso) {
     const long long N = (long long)n0 * n1 * n2;
     if (aniso)
-        k_coef<true><<<vec_blocks(c, N), 256, 0, c.stream>>>(n0, n1, n2, T, mat, th, tab, k64, k32, kz64, kz32);
+        launch(k_coef<true>, vec_blocks(c, N), 256, c.stream, n0, n1, n2, T, mat, th, tab, k64, k32, kz64, kz32);
     else
-        k_coef<false><<<vec_blocks(c, N), 256, 0, c.stream>>>(n0, n1, n2, T, mat, th, tab, k64, k32, kz64, kz32);
+        launch(k_coef<false>, vec_blocks(c, N), 256, c.stream, n0, n1, n2, T, mat, th, tab, k64, k32, kz64, kz32);
 }
 void launch_diag(const LaunchCfg& c, const GridT<double>& g, const double* kxy, const double* kz, bool aniso,
                  const SurfaceT<double>& s, const uint32_t* dmask, double* diag, double* minv64, float* minv32) {
     if (aniso)
-        k_diag<true><<<vec_blocks(c, g.N), 256, 0, c.stream>>>(g, kxy, kz, diag);
+        launch(k_diag<true>, vec_blocks(c, g.N), 256, c.stream, g, kxy, kz, diag);
     else
-        k_diag<false><<<vec_blocks(c, g.N), 256, 0, c.stream>>>(g, kxy, kz, diag);
-    if (s.nrows > 0) k_surface_diag<<<grid_for(s.nrows, 256, 1024), 256, 0, c.stream>>>(s, diag);
-    k_invert_diag<<<vec_blocks(c, g.N), 256, 0, c.stream>>>(g.N, diag, dmask, minv64, minv32);
+        launch(k_diag<false>, vec_blocks(c, g.N), 256, c.stream, g, kxy, kz, diag);
+    if (s.nrows > 0) launch(k_surface_diag, grid_for(s.nrows, 256, 1024), 256, c.stream, s, diag);
+    launch(k_invert_diag, vec_blocks(c, g.N), 256, c.stream, g.N, diag, dmask, minv64, minv32);
 }
 void launch_heat_load(const LaunchCfg& c, const GridT<double>& g, const double* q, const int* mat, const MatTable& tab,
                       double* F) {
-    k_heat_load<<<vec_blocks(c, g.N), 256, 0, c.stream>>>(g, q, mat, tab, F);
+    launch(k_heat_load, vec_blocks(c, g.N), 256, c.stream, g, q, mat, tab, F);
 }
 void launch_scatter_add(const LaunchCfg& c, int n, const int* idx, const double* val, double* F) {
-    if (n > 0) k_scatter_add<<<grid_for(n, 256, 1024), 256, 0, c.stream>>>(n, idx, val, F);
+    if (n > 0) launch(k_scatter_add, grid_for(n, 256, 1024), 256, c.stream, n, idx, val, F);
 }
 void launch_set_dirichlet(const LaunchCfg& c, int n, const int* idx, const double* v, double* b, double* T) {
-    if (n > 0) k_set_dirichlet<<<grid_for(n, 256, 1024), 256, 0, c.stream>>>(n, idx, v, b, T);
+    if (n > 0) launch(k_set_dirichlet, grid_for(n, 256, 1024), 256, c.stream, n, idx, v, b, T);
 }
 void launch_radiation(const LaunchCfg& c, int nrows, const int* row, const int* ptr, const int* src, const double* coef,
                       const double* tamb, const double* T, double* b) {
-    if (nrows > 0) k_radiation<<<grid_for(nrows, 256, 1024), 256, 0, c.stream>>>(nrows, row, ptr, src, coef, tamb, T, b);
+    if (nrows > 0) launch(k_radiation, grid_for(nrows, 256, 1024), 256, c.stream, nrows, row, ptr, src, coef, tamb, T, b);
 }
 void launch_err(const LaunchCfg& c, long long N, const double* T, const double* T0, const uint32_t* inactive,
                 double* partials, SolveCtl* ctl) {
-    k_err<<<vec_blocks(c, N), 256, 0, c.stream>>>(N, T, T0, inactive, partials, ctl);
+    launch(k_err, vec_blocks(c, N), 256, c.stream, N, T, T0, inactive, partials, ctl);
 }
 void launch_flux(const LaunchCfg& c, const GridT<double>& g, const double* T, const int* mat, const double* hleaf,
                  const MatTable& tab, double* out) {
     const long long NE = (long long)(g.n0 - 1) * (g.n1 - 1) * (g.n2 - 1);
-    k_flux<<<vec_blocks(c, NE), 256, 0, c.stream>>>(g, T, mat, hleaf, tab, out);
+    launch(k_flux, vec_blocks(c, NE), 256, c.stream, g, T, mat, hleaf, tab, out);
 }
 void launch_conductivity(const LaunchCfg& c, int n0, int n1, int n2, const double* T, const int* mat, const double* th,
                          const MatTable& tab, double* out) {
     const long long NE = (long long)(n0 - 1) * (n1 - 1) * (n2 - 1);
-    k_conductivity<<<vec_blocks(c, NE), 256, 0, c.stream>>>(n0, n1, n2, T, mat, th, tab, out);
+    launch(k_conductivity, vec_blocks(c, NE), 256, c.stream, n0, n1, n2, T, mat, th, tab, out);
 }
 
 void launch_from_mesh_order_i32(const LaunchCfg& c, int n0, int n1, int n2, int m0, int m1, int m2, long long s0,
                                 long long s1, long long s2, const int* src, int* dst, int fill) {
     const long long N = (long long)n0 * n1 * n2;
-    k_from_mesh_order<int><<<vec_blocks(c, N), 256, 0, c.stream>>>(n0, n1, n2, m0, m1, m2, s0, s1, s2, src, dst, fill);
+    launch(k_from_mesh_order<int>, vec_blocks(c, N), 256, c.stream, n0, n1, n2, m0, m1, m2, s0, s1, s2, src, dst, fill);
 }
 void launch_from_mesh_order_f64(const LaunchCfg& c, int n0, int n1, int n2, int m0, int m1, int m2, long long s0,
                                 long long s1, long long s2, const double* src, double* dst, double fill) {
     const long long N = (long long)n0 * n1 * n2;
-    k_from_mesh_order<double><<<vec_blocks(c, N), 256, 0, c.stream>>>(n0, n1, n2, m0, m1, m2, s0, s1, s2, src, dst,
+    launch(k_from_mesh_order<double>, vec_blocks(c, N), 256, c.stream, n0, n1, n2, m0, m1, m2, s0, s1, s2, src, dst,
                                                                       fill);
 }
 void launch_to_mesh_order_f64(const LaunchCfg& c, int m0, int m1, int m2, long long c1, long long c2, long long s0,
                               long long s1, long long s2, int comps, const double* src, double* dst) {
     const long long M = (long long)m0 * m1 * m2;
-    k_to_mesh_order<double><<<vec_blocks(c, M), 256, 0, c.stream>>>(m0, m1, m2, c1, c2, s0, s1, s2, comps, src, dst);
+    launch(k_to_mesh_order<double>, vec_blocks(c, M), 256, c.stream, m0, m1, m2, c1, c2, s0, s1, s2, comps, src, dst);
 }
 void launch_gather(const LaunchCfg& c, long long n, const long long* idx, const double* in, double* out) {
-    if (n > 0) k_gather<<<vec_blocks(c, n), 256, 0, c.stream>>>(n, idx, in, out);
+    if (n > 0) launch(k_gather, vec_blocks(c, n), 256, c.stream, n, idx, in, out);
 }
 void launch_scatter(const LaunchCfg& c, long long n, const long long* idx, const double* in, double* out) {
-    if (n > 0) k_scatter<<<vec_blocks(c, n), 256, 0, c.stream>>>(n, idx, in, out);
+    if (n > 0) launch(k_scatter, vec_blocks(c, n), 256, c.stream, n, idx, in, out);
 }
 
 }  // namespace plgpu

@@ -8,7 +8,21 @@
 
 namespace plgpu {
 
-enum { MODE_CG = 0, MODE_RESID = 1, MODE_RHS = 2 };
+// MODE_CG:    y = A x, Dirichlet rows y = x (x is zero on Dirichlet nodes in CG)
+// MODE_RESID: y = rhs - A x, x masked to zero on Dirichlet nodes, Dirichlet rows y = rhs - x
+// MODE_RHS:   y = rhs - A x with the full operator (Dirichlet rows fixed up afterwards)
+// MODE_MULT:  y = A x, x masked to zero on Dirichlet nodes, Dirichlet rows y = x
+enum { MODE_CG = 0, MODE_RESID = 1, MODE_RHS = 2, MODE_MULT = 3 };
+
+void count_launch();
+void count_launches(long long n);  // kernels run by a replayed CUDA graph
+
+// Launch a kernel on a stream and count it.
+template <typename... KArgs, typename... Args>
+inline void launch_kernel(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t stream, Args... args) {
+    kern<<<grid, block, 0, stream>>>(args...);
+    count_launch();
+}
 
 // Material table in device memory (one entry per material id).
 struct MatTable {
@@ -21,10 +35,12 @@ struct MatTable {
 
 struct LaunchCfg {
     cudaStream_t stream;
+    int sm_count;      // streaming multiprocessors of the device
     int vec_blocks;    // grid size cap of streaming kernels (a multiple of the SM count)
     int apply_planes;  // z-planes per block of the operator kernels
 };
 
+long long launch_count();  // kernels launched by this library so far (all handles)
 int apply_blocks(const LaunchCfg& c, int n0, int n1, int n2);
 int surface_blocks(int nrows);
 int vec_blocks(const LaunchCfg& c, long long N);
@@ -35,6 +51,16 @@ void launch_apply(const LaunchCfg& c, const GridT<double>& g, const double* x, d
 void launch_apply(const LaunchCfg& c, const GridT<float>& g, const float* x, float* y, const float* kxy,
                   const float* kz, bool aniso, const uint32_t* dmask, const float* rhs, double* partials, int mode,
                   const SolveCtl* ctl);
+// Optimised operator (fem3d_operator.cu).  zf[k] = dz_k / 48, zr[k] = 1 / (48 dz_k).
+// number of blocks (= partial-sum slots written in MODE_CG) of one operator launch
+int op_blocks(const LaunchCfg& c, int n0, int n1, int n2, bool fp64);
+void launch_operator(const LaunchCfg& c, const GridT<float>& g, const float* zf, const float* zr, const float* x,
+                     float* y, const float* kxy, const float* kz, bool aniso, const uint32_t* dmask, const float* rhs,
+                     double* partials, int mode, const SolveCtl* ctl);
+void launch_operator(const LaunchCfg& c, const GridT<double>& g, const double* zf, const double* zr, const double* x,
+                     double* y, const double* kxy, const double* kz, bool aniso, const uint32_t* dmask,
+                     const double* rhs, double* partials, int mode, const SolveCtl* ctl);
+
 void launch_surface(const LaunchCfg& c, const SurfaceT<double>& s, const double* x, double* y, double* partials,
                     int slot0, int mode, SolveCtl* ctl);
 void launch_surface(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, double* partials,
@@ -55,6 +81,8 @@ void launch_cg_start(const LaunchCfg& c, long long N, float* x, bool zero_x, con
                      int stall_limit);
 void launch_norm2(const LaunchCfg& c, long long N, const double* v, float* v32, double* partials, SolveCtl* ctl,
                   int slot);
+void launch_fill(const LaunchCfg& c, long long N, double* v, double value);
+void launch_widen(const LaunchCfg& c, long long N, const float* a, double* b);
 void launch_add_correction(const LaunchCfg& c, long long N, double* T, const float* d);
 void launch_thickness(const LaunchCfg& c, int n0, int n1, int n2, const int* mat, const double* z, double* th);
 void launch_coef(const LaunchCfg& c, int n0, int n1, int n2, const double* T, const int* mat, const double* th,

@@ -1,0 +1,330 @@
+// Matrix-free stiffness operator for sm_103a: y = A x for the trilinear-hex FEM
+// Laplacian with per-element conductivities (PLaSK therm3d.cpp:226-237, 270-275).
+//
+// Element algebra.  With X, Y, Z the scaled conductances of an element
+// (X = kx dy dz / dx, ...), its 8x8 stiffness is
+//     K_e = X (A (x) M (x) M) + Y (M (x) A (x) M) + Z (M (x) M (x) A),
+//     A = [[1,-1],[-1,1]],  M = [[2,1],[1,2]] / 6.
+// Writing M = (1/4) e e^T + (1/12) d d^T with e = (1,1), d = (-1,1) turns every
+// term into a sum of rank-one products of the 2-point sum/difference vectors, so
+//     K_e = H^T diag(lambda) H,
+// H being the 8-point sum/difference butterfly (three stages of 4 butterflies)
+// and, for the moments m = (mx, my, mz) in {0,1}^3 (1 = difference):
+//     lambda_000 = 0,  lambda_100 = X/16,  lambda_010 = Y/16,  lambda_001 = Z/16,
+//     lambda_110 = (X+Y)/48,  lambda_101 = (X+Z)/48,  lambda_011 = (Y+Z)/48,
+//     lambda_111 = (X+Y+Z)/144.
+// One element costs ~60 adds/multiplies instead of the ~200 of the explicit 8x8 form.
+//
+// Work layout.  Threads march along z (axis 2).  A warp covers 32 consecutive
+// node columns in x (one per lane; lane l holds column i0 - 1 + l) and each
+// thread R + 2 consecutive rows in y, so that every element it needs for its R
+// output rows and the 30 interior lanes is computed inside the warp: x(i+1)
+// comes from the next lane by shuffle, the contributions of an element to its
+// i+1 corners go to the next lane by shuffle.  No shared memory, no barriers.
+// Per output node: ~1.16 elements computed, 1 coalesced load of x, 1 of the
+// conductivity (2 when anisotropic), 1 store.
+#include <algorithm>
+#include <cstdint>
+
+#include "fem3d_device.cuh"
+#include "fem3d_kernels.h"
+
+namespace plgpu {
+
+template <typename R>
+struct OpArgs {
+    GridT<R> g;
+    const R* x;
+    R* y;
+    const R* kxy;
+    const R* kz;
+    const uint32_t* dmask;
+    const R* rhs;
+    double* partials;
+    const SolveCtl* ctl;
+    const R* zf;       // per element layer: dz / 48      (n2 - 1)
+    const R* zr;       // per element layer: 1 / (48 dz)  (n2 - 1)
+    int zchunk;        // planes per block along z
+};
+
+__device__ __forceinline__ bool dir_bit(const uint32_t* __restrict__ m, long long n) {
+    return (__ldg(m + (n >> 5)) >> (n & 31)) & 1u;
+}
+
+// warp-level sum helpers for the partial dot product
+__device__ __forceinline__ double warp_sum_d(double v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename R, int RR, bool ANISO, int MODE>
+__global__ void __launch_bounds__(128) k_apply_haar(const OpArgs<R> a) {
+    if (MODE == MODE_CG && a.ctl != nullptr && a.ctl->status != SOLVE_RUNNING) return;
+    const int n0 = a.g.n0, n1 = a.g.n1, n2 = a.g.n2;
+    const int s2 = n0 * n1;  // N < 2^31 (checked on the host)
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int i = blockIdx.x * 30 - 1 + lane;                      // node column of this lane
+    const int jb = (blockIdx.y * (blockDim.x >> 5) + warp) * RR;   // first output row of the warp
+    const int k0 = blockIdx.z * a.zchunk;
+    const int k1 = min(k0 + a.zchunk, n2);
+    const bool out_lane = lane >= 1 && lane <= 30 && i < n0;
+    const bool have_i = i >= 0 && i < n0;
+    const bool elem_i = i >= 0 && i < n0 - 1;
+
+    // in-plane offsets of the node rows (-1: outside the mesh) and element rows (-1: no element)
+    int noff[RR + 2], eoff[RR + 1];
+#pragma unroll
+    for (int r = 0; r < RR + 2; ++r) {
+        const int j = jb - 1 + r;
+        noff[r] = (have_i && j >= 0 && j < n1) ? i + n0 * j : -1;
+    }
+    // geometry of the element column (i, jb - 1 + e): X = k gx zf, Y = k gy zf, Z = kz gz zr
+    R gx[RR + 1], gy[RR + 1], gz[RR + 1];
+    {
+        const R dx = elem_i ? a.g.h0[i] : R(0);
+        const R rdx = elem_i ? a.g.r0[i] : R(0);
+#pragma unroll
+        for (int e = 0; e <= RR; ++e) {
+            const int j = jb - 1 + e;
+            const bool ok = elem_i && j >= 0 && j < n1 - 1;
+            eoff[e] = ok ? i + n0 * j : -1;
+            const R dy = ok ? a.g.h1[j] : R(0);
+            const R rdy = ok ? a.g.r1[j] : R(0);
+            gx[e] = dy * rdx;
+            gy[e] = dx * rdy;
+            gz[e] = dx * dy;
+        }
+    }
+
+    auto load_x = [&](int k, R(&xv)[RR + 2]) {
+        const bool kin = k >= 0 && k < n2;
+        const R* base = a.x + (long long)s2 * (kin ? k : 0);
+#pragma unroll
+        for (int r = 0; r < RR + 2; ++r) {
+            R v = R(0);
+            if (kin && noff[r] >= 0) {
+                v = base[noff[r]];
+                if ((MODE == MODE_RESID || MODE == MODE_MULT) && dir_bit(a.dmask, (long long)s2 * k + noff[r])) v = R(0);
+            }
+            xv[r] = v;
+        }
+    };
+    auto load_k = [&](int k, R(&kk)[RR + 1], R(&kv)[RR + 1]) {
+        const bool kin = k >= 0 && k < n2 - 1;
+        const long long b = (long long)s2 * (kin ? k : 0);
+#pragma unroll
+        for (int e = 0; e <= RR; ++e) {
+            R v = R(0), w = R(0);
+            if (kin && eoff[e] >= 0) {
+                v = a.kxy[b + eoff[e]];
+                if (ANISO) w = a.kz[b + eoff[e]];
+            }
+            kk[e] = v;
+            kv[e] = ANISO ? w : v;
+        }
+    };
+
+    R acc[RR], nxt[RR];  // outputs of plane k (rows 1..RR) and partial plane k + 1
+#pragma unroll
+    for (int r = 0; r < RR; ++r) acc[r] = nxt[r] = R(0);
+
+    R dot = R(0);  // per-thread partial of (x, A x); FP64 from the warp level on
+    const int kstart = max(k0 - 1, 0);
+    R xlo[RR + 2], xlo_p[RR + 2], xhi[RR + 2], xnx[RR + 2];
+    R kk[RR + 1], kv[RR + 1], kkn[RR + 1], kvn[RR + 1];
+    load_x(kstart, xlo);
+    load_x(kstart + 1, xhi);
+    load_k(kstart, kk, kv);
+#pragma unroll
+    for (int r = 0; r < RR + 2; ++r) xlo_p[r] = __shfl_down_sync(0xffffffffu, xlo[r], 1);
+
+    for (int k = kstart; k < k1; ++k) {
+        // prefetch the next plane and the next element layer while this layer is computed
+        load_x(k + 2, xnx);
+        load_k(k + 1, kkn, kvn);
+        R xhi_p[RR + 2];
+#pragma unroll
+        for (int r = 0; r < RR + 2; ++r) xhi_p[r] = __shfl_down_sync(0xffffffffu, xhi[r], 1);
+        const int kl = min(k, n2 - 2);
+        const R zf = a.zf[kl], zr = a.zr[kl];
+#pragma unroll
+        for (int e = 0; e <= RR; ++e) {
+            // lambda weights (X/48, Y/48, Z/48 scaled); zero conductivity gives zero contributions
+            const R X = kk[e] * gx[e] * zf;
+            const R Y = kk[e] * gy[e] * zf;
+            const R Z = kv[e] * gz[e] * zr;
+            const R l100 = R(3) * X, l010 = R(3) * Y, l001 = R(3) * Z;
+            const R l110 = X + Y, l101 = X + Z, l011 = Y + Z;
+            const R l111 = (X + Y + Z) * R(1.0 / 3.0);
+            // corners c = ci + 2 cj + 4 ck
+            const R c0 = xlo[e], c1 = xlo_p[e], c2 = xlo[e + 1], c3 = xlo_p[e + 1];
+            const R c4 = xhi[e], c5 = xhi_p[e], c6 = xhi[e + 1], c7 = xhi_p[e + 1];
+            // forward butterfly: x, then y, then z
+            const R sx0 = c0 + c1, dx0 = c1 - c0, sx1 = c2 + c3, dx1 = c3 - c2;
+            const R sx2 = c4 + c5, dx2 = c5 - c4, sx3 = c6 + c7, dx3 = c7 - c6;
+            const R ss0 = sx0 + sx1, sd0 = sx1 - sx0, ss1 = sx2 + sx3, sd1 = sx3 - sx2;
+            const R ds0 = dx0 + dx1, dd0 = dx1 - dx0, ds1 = dx2 + dx3, dd1 = dx3 - dx2;
+            const R m001 = (ss1 - ss0) * l001;
+            const R m010 = (sd0 + sd1) * l010, m011 = (sd1 - sd0) * l011;
+            const R m100 = (ds0 + ds1) * l100, m101 = (ds1 - ds0) * l101;
+            const R m110 = (dd0 + dd1) * l110, m111 = (dd1 - dd0) * l111;
+            // transposed butterfly: z, then y, then x (m000 = 0)
+            const R tsd0 = m010 - m011, tsd1 = m010 + m011;
+            const R tds0 = m100 - m101, tds1 = m100 + m101;
+            const R tdd0 = m110 - m111, tdd1 = m110 + m111;
+            const R ys0 = -m001 - tsd0, ys1 = tsd0 - m001, ys2 = m001 - tsd1, ys3 = m001 + tsd1;
+            const R yd0 = tds0 - tdd0, yd1 = tds0 + tdd0, yd2 = tds1 - tdd1, yd3 = tds1 + tdd1;
+            // own column (ci = 0): node rows e (cj = 0) and e + 1 (cj = 1); output rows are 1..RR
+            if (e >= 1) {
+                acc[e - 1] += ys0 - yd0;
+                nxt[e - 1] += ys2 - yd2;
+            }
+            if (e + 1 <= RR) {
+                acc[e] += ys1 - yd1;
+                nxt[e] += ys3 - yd3;
+            }
+            // column i + 1 (ci = 1): to the next lane
+            const R u0 = __shfl_up_sync(0xffffffffu, ys0 + yd0, 1);
+            const R u1 = __shfl_up_sync(0xffffffffu, ys1 + yd1, 1);
+            const R u2 = __shfl_up_sync(0xffffffffu, ys2 + yd2, 1);
+            const R u3 = __shfl_up_sync(0xffffffffu, ys3 + yd3, 1);
+            if (e >= 1) {
+                acc[e - 1] += u0;
+                nxt[e - 1] += u2;
+            }
+            if (e + 1 <= RR) {
+                acc[e] += u1;
+                nxt[e] += u3;
+            }
+        }
+        // plane k is complete
+        if (k >= k0) {
+            const long long pb = (long long)s2 * k;
+#pragma unroll
+            for (int r = 1; r <= RR; ++r) {
+                if (out_lane && noff[r] >= 0) {
+                    const long long n = pb + noff[r];
+                    R out;
+                    if (MODE == MODE_CG) {
+                        // Dirichlet rows: x is zero there and M^-1 = 0 keeps the CG residual zero
+                        out = acc[r - 1];
+                        dot += xlo[r] * out;
+                    } else if (MODE == MODE_RESID) {
+                        out = dir_bit(a.dmask, n) ? R(a.rhs[n] - a.x[n]) : R(a.rhs[n] - acc[r - 1]);
+                    } else if (MODE == MODE_MULT) {
+                        out = dir_bit(a.dmask, n) ? a.x[n] : acc[r - 1];
+                    } else {
+                        out = a.rhs[n] - acc[r - 1];
+                    }
+                    a.y[n] = out;
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < RR; ++r) {
+            acc[r] = nxt[r];
+            nxt[r] = R(0);
+        }
+#pragma unroll
+        for (int r = 0; r < RR + 2; ++r) {
+            xlo[r] = xhi[r];
+            xlo_p[r] = xhi_p[r];
+            xhi[r] = xnx[r];
+        }
+#pragma unroll
+        for (int e = 0; e <= RR; ++e) {
+            kk[e] = kkn[e];
+            kv[e] = kvn[e];
+        }
+    }
+    if (MODE == MODE_CG) {
+        // block partial of (x, y)
+        __shared__ double sh[4];
+        const double dw = warp_sum_d((double)dot);
+        if (lane == 0) sh[warp] = dw;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[w];
+            a.partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s;
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------------------
+
+namespace {
+constexpr int kWarps = 4;
+template <typename R>
+struct Rows;
+template <>
+struct Rows<float> {
+    static constexpr int value = 8;  // 167 registers, no spills
+};
+template <>
+struct Rows<double> {
+    static constexpr int value = 4;  // FP64 needs twice the registers per value
+};
+}  // namespace
+
+template <typename R>
+static void op_grid(const LaunchCfg& c, int n0, int n1, int n2, dim3& grid, int& zchunk) {
+    constexpr int kRows = Rows<R>::value;
+    const int gx = (n0 + 29) / 30;
+    const int gy = (n1 + kRows * kWarps - 1) / (kRows * kWarps);
+    // enough z-chunks for ~4 blocks per SM, each chunk at least 8 planes
+    int chunks = (c.sm_count * 4 + gx * gy - 1) / (gx * gy);
+    chunks = max(1, min(chunks, (n2 + 7) / 8));
+    while ((long long)gx * gy * chunks > kMaxPartialBlocks - 256) --chunks;
+    zchunk = (n2 + chunks - 1) / chunks;
+    chunks = (n2 + zchunk - 1) / zchunk;
+    grid = dim3(gx, gy, chunks);
+}
+
+int op_blocks(const LaunchCfg& c, int n0, int n1, int n2, bool fp64) {
+    dim3 g;
+    int z;
+    if (fp64)
+        op_grid<double>(c, n0, n1, n2, g, z);
+    else
+        op_grid<float>(c, n0, n1, n2, g, z);
+    return (int)(g.x * g.y * g.z);
+}
+
+template <typename R>
+static void op_launch(const LaunchCfg& c, const GridT<R>& g, const R* zf, const R* zr, const R* x, R* y, const R* kxy,
+                      const R* kz, bool aniso, const uint32_t* dmask, const R* rhs, double* partials, int mode,
+                      const SolveCtl* ctl) {
+    constexpr int kRows = Rows<R>::value;
+    dim3 grid;
+    int zchunk;
+    op_grid<R>(c, g.n0, g.n1, g.n2, grid, zchunk);
+    OpArgs<R> a{g, x, y, kxy, kz, dmask, rhs, partials, ctl, zf, zr, zchunk};
+#define PLGPU_OP(MODEV)                                                                                       \
+    if (mode == MODEV) {                                                                                      \
+        if (aniso)                                                                                            \
+            launch_kernel(k_apply_haar<R, kRows, true, MODEV>, grid, dim3(32 * kWarps), c.stream, a);         \
+        else                                                                                                  \
+            launch_kernel(k_apply_haar<R, kRows, false, MODEV>, grid, dim3(32 * kWarps), c.stream, a);        \
+        return;                                                                                               \
+    }
+    PLGPU_OP(MODE_CG)
+    PLGPU_OP(MODE_RESID)
+    PLGPU_OP(MODE_RHS)
+    PLGPU_OP(MODE_MULT)
+#undef PLGPU_OP
+}
+
+void launch_operator(const LaunchCfg& c, const GridT<float>& g, const float* zf, const float* zr, const float* x,
+                     float* y, const float* kxy, const float* kz, bool aniso, const uint32_t* dmask, const float* rhs,
+                     double* partials, int mode, const SolveCtl* ctl) {
+    op_launch<float>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl);
+}
+void launch_operator(const LaunchCfg& c, const GridT<double>& g, const double* zf, const double* zr, const double* x,
+                     double* y, const double* kxy, const double* kz, bool aniso, const uint32_t* dmask,
+                     const double* rhs, double* partials, int mode, const SolveCtl* ctl) {
+    op_launch<double>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl);
+}
+
+}  // namespace plgpu
