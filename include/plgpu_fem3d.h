@@ -195,6 +195,24 @@ void* plgpu_fem3d_stream(plgpu_fem3d* h);
    operator of the inner solver, result widened to double). */
 int plgpu_fem3d_mult(plgpu_fem3d* h, int precision, const double* x, double* y);
 
+/* The same product as plgpu_fem3d_mult, for callers that must not allocate
+   device memory during the call: a host framework that has reserved the whole
+   GPU for its own allocator (cudaMalloc then fails), or a latency-critical loop
+   on other streams that cannot afford the device-wide synchronisation that
+   cudaMalloc and cudaFree may cause.  No counterpart in the reference: it only
+   changes where the staging buffer lives.
+   - Allocates nothing: no cudaMalloc, cudaFree or allocating library call.  The
+     device staging buffer is a file-scope array of 2,097,152 doubles (16 MiB)
+     that every GPU loading this library keeps until the process exits; meshes
+     with more nodes are rejected with PLGPU_ERR_ARG.
+   - The handle must already be set up on the device (PLGPU_ERR_STATE otherwise):
+     call plgpu_fem3d_compute or plgpu_fem3d_mult on it once first.
+   - The first call on a device looks up the array's device address
+     (cudaGetSymbolAddress); make that first call before any stream capture.
+   - All calls share the array, which keeps the last call's contents; calls that
+     overlap on the GPU (two handles on two streams at once) race on it. */
+int plgpu_fem3d_mult_noalloc(plgpu_fem3d* h, int precision, const double* x, double* y);
+
 /* Time the operator kernel (one matrix-free stiffness application, the
    inner kernel of every CG iteration) on the handle's stream with CUDA
    events: `reps` launches on the current coefficients, optionally with the

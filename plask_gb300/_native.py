@@ -76,6 +76,7 @@ SIGNATURES = {
     "plgpu_fem3d_set_log_callback": (C.c_int, [_h, LOG_CB, C.c_void_p]),
     "plgpu_fem3d_time_operator": (C.c_int, [_h, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     "plgpu_fem3d_mult": (C.c_int, [_h, C.c_int, _dp, _dp]),
+    "plgpu_fem3d_mult_noalloc": (C.c_int, [_h, C.c_int, _dp, _dp]),
 }
 
 _lib = None
@@ -260,6 +261,17 @@ class Fem3D:
         xv = _f64(x).ravel()
         y = np.empty_like(xv)
         self._check(self._lib.plgpu_fem3d_mult(self._h, int(precision), _ptr(xv, C.c_double), _ptr(y, C.c_double)))
+        return y
+
+    def mult_noalloc(self, x, precision=64):
+        """A x like :meth:`mult`, staged in the library's static device buffer (no device allocation).
+
+        For callers that cannot allocate device memory during the call; meshes of at most
+        2,097,152 nodes, handle already set up by compute() or mult()."""
+        xv = _f64(x).ravel()
+        y = np.empty_like(xv)
+        self._check(self._lib.plgpu_fem3d_mult_noalloc(self._h, int(precision), _ptr(xv, C.c_double),
+                                                       _ptr(y, C.c_double)))
         return y
 
     def time_operator(self, precision=32, reps=20, flush_l2=True):

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
@@ -1048,6 +1049,8 @@ struct plgpu_fem3d {
         ck(cudaStreamSynchronize(stream), "sync");
     }
 
+    void mult_noalloc(int precision, const double* xin, double* yout);
+
     // ---------------------------------------------------------------------------------
     // outputs
 
@@ -1121,6 +1124,76 @@ struct plgpu_fem3d {
         ck(cudaStreamSynchronize(stream), "sync");
     }
 };
+
+// ---------------------------------------------------------------------------------------
+// Multiply without allocation.
+//
+// Some callers cannot allocate device memory at the moment they need A x: a host
+// framework that has reserved the whole GPU for its own caching allocator (cudaMalloc
+// fails), or a latency-critical loop on other streams that cannot afford the
+// device-wide synchronisation cudaMalloc and cudaFree may cause.  plgpu_fem3d_mult stages the vectors in a
+// buffer it allocates per call; plgpu_fem3d_mult_noalloc stages them in the
+// file-scope array below instead, which every GPU that loads this library keeps for
+// the life of the process (16 MiB).
+//
+// The array is shared by all calls and all handles and keeps the last call's
+// contents.  Nothing in it needs to start at zero: every word a call reads is
+// written by the same call first.  Calls that overlap on the GPU (two handles on
+// two streams at the same time) race on it.
+
+namespace {
+constexpr size_t kNoAllocMaxNodes = size_t(1) << 21;  // 2,097,152 nodes
+__device__ __align__(256) double g_noalloc_stage[kNoAllocMaxNodes];
+
+std::mutex g_noalloc_mutex;
+double* g_noalloc_ptr[64] = {};  // device address of g_noalloc_stage, per device
+
+// Device address of the staging array on the current device.  Obtained once per
+// device with cudaGetSymbolAddress (host code cannot use the symbol itself: in host
+// code its name stands for a host-side shadow, not a device address).
+double* noalloc_stage() {
+    int dev = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= 64) throw StateError("device index out of range for the no-allocation multiply");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        ck(cudaGetSymbolAddress(&p, g_noalloc_stage), "cudaGetSymbolAddress");
+        g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    return g_noalloc_ptr[dev];
+}
+}  // namespace
+
+void plgpu_fem3d::mult_noalloc(int precision, const double* xin, double* yout) {
+    if ((size_t)N > kNoAllocMaxNodes)
+        throw ArgError("plgpu_fem3d_mult_noalloc handles meshes of at most " + std::to_string(kNoAllocMaxNodes) +
+                       " nodes; this mesh has " + std::to_string(N) + " (use plgpu_fem3d_mult)");
+    if (!initialized || bc_dirty)
+        throw StateError("plgpu_fem3d_mult_noalloc needs a handle whose mesh, materials and boundary conditions "
+                         "are already set up on the device: call plgpu_fem3d_compute or plgpu_fem3d_mult once first");
+    double* stage = noalloc_stage();
+    launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab, k64.as<double>(),
+                k32.as<float>(), aniso ? kz64.as<double>() : nullptr, aniso ? kz32.as<float>() : nullptr, aniso);
+    ck(cudaMemcpyAsync(stage, xin, (size_t)N * 8, cudaMemcpyHostToDevice, stream), "H2D x");
+    launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], n[1], n[2], ns[0], ns[1], ns[2], stage, p64.as<double>(),
+                               0.0);
+    if (precision == 64) {
+        op64(p64.as<double>(), q64.as<double>(), nullptr, MODE_MULT);
+        launch_surface(cfg, s64, p64.as<double>(), q64.as<double>(), partials.as<double>(), 0, MODE_MULT,
+                       d_ctl.as<SolveCtl>());
+    } else {
+        launch_norm2(cfg, N, p64.as<double>(), p32.as<float>(), partials.as<double>(), d_ctl.as<SolveCtl>(), 4);
+        op32(p32.as<float>(), q32.as<float>(), MODE_MULT);
+        launch_surface(cfg, s32, p32.as<float>(), q32.as<float>(), partials.as<double>(), 0, MODE_MULT,
+                       d_ctl.as<SolveCtl>());
+        launch_widen(cfg, N, q32.as<float>(), q64.as<double>());
+    }
+    launch_to_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], (long long)n[0] * n[1], ns[0], ns[1], ns[2], 1,
+                             q64.as<double>(), stage);
+    ck(cudaMemcpyAsync(yout, stage, (size_t)N * 8, cudaMemcpyDeviceToHost, stream), "D2H y");
+    ck(cudaStreamSynchronize(stream), "sync");
+}
 
 // ---------------------------------------------------------------------------------------
 // C ABI
@@ -1310,6 +1383,14 @@ int plgpu_fem3d_mult(plgpu_fem3d* h, int precision, const double* x, double* y) 
         if (precision != 32 && precision != 64) throw ArgError("precision must be 32 or 64");
         if (!x || !y) throw ArgError("null vector");
         h->mult(precision, x, y);
+    });
+}
+
+int plgpu_fem3d_mult_noalloc(plgpu_fem3d* h, int precision, const double* x, double* y) {
+    return guarded(h, [&] {
+        if (precision != 32 && precision != 64) throw ArgError("precision must be 32 or 64");
+        if (!x || !y) throw ArgError("null vector");
+        h->mult_noalloc(precision, x, y);
     });
 }
 
