@@ -58,7 +58,7 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 template <typename R, int RR, bool ANISO, int MODE>
-__global__ void __launch_bounds__(128) k_apply_haar(const OpArgs<R> a) {
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 2) k_apply_haar(const OpArgs<R> a) {
     if (MODE == MODE_CG && a.ctl != nullptr && a.ctl->status != SOLVE_RUNNING) return;
     const int n0 = a.g.n0, n1 = a.g.n1, n2 = a.g.n2;
     const int s2 = n0 * n1;  // N < 2^31 (checked on the host)
@@ -260,7 +260,7 @@ template <typename R>
 struct Rows;
 template <>
 struct Rows<float> {
-    static constexpr int value = 8;  // 167 registers, no spills
+    static constexpr int value = 6;  // fits 128 registers (4 blocks of 128 threads per SM) without spills
 };
 template <>
 struct Rows<double> {
@@ -273,9 +273,16 @@ static void op_grid(const LaunchCfg& c, int n0, int n1, int n2, dim3& grid, int&
     constexpr int kRows = Rows<R>::value;
     const int gx = (n0 + 29) / 30;
     const int gy = (n1 + kRows * kWarps - 1) / (kRows * kWarps);
-    // enough z-chunks for ~4 blocks per SM, each chunk at least 8 planes
-    int chunks = (c.sm_count * 4 + gx * gy - 1) / (gx * gy);
-    chunks = max(1, min(chunks, (n2 + 7) / 8));
+    // z-chunks: fill whole waves of resident blocks (4 per SM in FP32, 2 in FP64),
+    // each chunk at least 8 planes (one extra element layer is recomputed per chunk)
+    const int resident = c.sm_count * (sizeof(R) == 4 ? 4 : 2);
+    const int maxchunks = max(1, (n2 + 7) / 8);
+    int chunks = 1;
+    for (int waves = 1; waves <= 8; ++waves) {
+        const int want = (waves * resident) / (gx * gy);
+        if (want >= 1 && want <= maxchunks) chunks = want;
+        if (want > maxchunks) break;
+    }
     while ((long long)gx * gy * chunks > kMaxPartialBlocks - 256) --chunks;
     zchunk = (n2 + chunks - 1) / chunks;
     chunks = (n2 + zchunk - 1) / zchunk;
