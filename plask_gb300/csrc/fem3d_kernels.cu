@@ -261,7 +261,10 @@ __global__ void __launch_bounds__(256) k_surface(const SurfaceT<R> s, const R* _
 }
 
 // x += alpha p; r -= alpha q; then (r, M^-1 r) and (r, r); the last block sets beta
-// and the convergence status.
+// and the convergence status.  Convergence and stagnation are judged on the
+// Jacobi-scaled residual (r, M^-1 r): every row counts relative to its own diagonal,
+// so rows of weakly conducting regions (a p-n junction under 1e9 S/m contacts, an
+// oxide aperture) are converged as tightly as the rest.
 template <typename R>
 __global__ void __launch_bounds__(256) k_cg_update(long long N, R* __restrict__ x, R* __restrict__ r,
                                                    const R* __restrict__ p, const R* __restrict__ q,
@@ -294,13 +297,14 @@ __global__ void __launch_bounds__(256) k_cg_update(long long N, R* __restrict__ 
             ctl->rr = rrn;
             if (!isfinite(rrn) || !isfinite(rzn)) {
                 ctl->status = SOLVE_NONFINITE;
-            } else if (rrn <= ctl->tol2) {
+            } else if ((ctl->plain ? rrn : rzn) <= ctl->tol2) {
                 ctl->status = SOLVE_CONVERGED;
             } else if (ctl->iter >= ctl->maxit) {
                 ctl->status = SOLVE_MAXIT;
             } else {
-                if (rrn < 0.81 * ctl->best_rr) {  // residual norm fell by 10 %
-                    ctl->best_rr = rrn;
+                const double m = ctl->plain ? rrn : rzn;
+                if (m < 0.81 * ctl->best_rr) {  // residual norm fell by 10 %
+                    ctl->best_rr = m;
                     ctl->stall = 0;
                 } else if (++ctl->stall > ctl->stall_limit) {
                     ctl->status = SOLVE_STAGNATED;
@@ -321,8 +325,9 @@ __global__ void __launch_bounds__(256) k_cg_direction(long long N, R* __restrict
 }
 
 // Start a solve: r is the initial residual.  ZERO_X: x = 0 (correction solves).
-// p = M^-1 r; rz = (r, M^-1 r); rr = (r, r).  Stop threshold tol2 = rtol^2 * ref
-// where ref = ctl->red[ref_slot] if ref_slot >= 0, else the initial rr.
+// p = M^-1 r; rz = (r, M^-1 r); rr = (r, r).  Stop threshold on rz: tol2 = rtol^2 * ref
+// where ref = ctl->red[ref_slot] (a scaled norm ||v||^2_{M^-1}) if ref_slot >= 0, else the
+// initial rz.
 template <typename R, bool ZERO_X>
 __global__ void __launch_bounds__(256) k_cg_start(long long N, R* __restrict__ x, const R* __restrict__ r,
                                                   R* __restrict__ p, const R* __restrict__ minv,
@@ -342,12 +347,13 @@ __global__ void __launch_bounds__(256) k_cg_start(long long N, R* __restrict__ x
     if (arrive_last(&ctl->arrive[1], gridDim.x)) {
         reduce_partials<2, OpSum>(v, partials, gridDim.x);
         if (linear_tid() == 0) {
-            const double ref = ref_slot >= 0 ? ctl->red[ref_slot] : v[1];
+            const double m0 = ctl->plain ? v[1] : v[0];
+            const double ref = ref_slot >= 0 ? ctl->red[ref_slot] : m0;
             ctl->rz = v[0];
             ctl->rz_old = v[0];
             ctl->rr = v[1];
             ctl->tol2 = rtol * rtol * ref;
-            ctl->best_rr = v[1];
+            ctl->best_rr = m0;
             ctl->iter = 0;
             ctl->maxit = maxit;
             ctl->stall = 0;
@@ -357,7 +363,7 @@ __global__ void __launch_bounds__(256) k_cg_start(long long N, R* __restrict__ x
             ctl->pq = 0.0;
             if (!isfinite(v[0]) || !isfinite(v[1]))
                 ctl->status = SOLVE_NONFINITE;
-            else if (v[1] <= ctl->tol2 || v[1] == 0.0)
+            else if (m0 <= ctl->tol2 || v[1] == 0.0)
                 ctl->status = SOLVE_CONVERGED;
             else if (!(v[0] > 0.0))
                 ctl->status = SOLVE_BREAKDOWN;
@@ -367,20 +373,80 @@ __global__ void __launch_bounds__(256) k_cg_start(long long N, R* __restrict__ x
     }
 }
 
-// ||v||^2 into ctl->red[slot]; optionally also writes a float copy of v.
+// Flexible CG (truncated to one previous direction) with a variable preconditioner z = P(r):
+//   alpha = (z, r) / (p, A p),  beta = -(z', A p) / (p, A p),  p' = z' + beta p.
+// k_fcg_dots reduces (z, r) and (z, q) with q = A p of the last direction; its last
+// block stores (z, r) as the next alpha's numerator and beta.  At the start
+// (first = 1) there is no previous direction: beta = 0.
+__global__ void __launch_bounds__(256) k_fcg_dots(long long N, const float* __restrict__ z, const float* __restrict__ r,
+                                                  const float* __restrict__ q, double* __restrict__ partials,
+                                                  SolveCtl* __restrict__ ctl, int first) {
+    if (ctl->status != SOLVE_RUNNING) return;
+    float zr = 0.f, zq = 0.f;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+        const float zn = z[n];
+        zr += zn * r[n];
+        if (!first) zq += zn * q[n];
+    }
+    double v[2] = {(double)zr, (double)zq};
+    write_partial<2, OpSum>(v, partials, blockIdx.x);
+    if (arrive_last(&ctl->arrive[1], gridDim.x)) {
+        reduce_partials<2, OpSum>(v, partials, gridDim.x);
+        if (linear_tid() == 0) {
+            ctl->rz = v[0];
+            ctl->beta = first ? 0.0 : -v[1] / ctl->pq;
+            if (!isfinite(v[0]) || !isfinite(ctl->beta))
+                ctl->status = SOLVE_NONFINITE;
+            else if (!(v[0] > 0.0))
+                ctl->status = SOLVE_STAGNATED;  // the preconditioned direction is not a descent direction
+        }
+    }
+}
+
+// p = z + beta p
+__global__ void __launch_bounds__(256) k_fcg_direction(long long N, float* __restrict__ p, const float* __restrict__ z,
+                                                       const SolveCtl* __restrict__ ctl) {
+    if (ctl->status != SOLVE_RUNNING) return;
+    const float beta = (float)ctl->beta;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x)
+        p[n] = z[n] + beta * p[n];
+}
+
+// ||v||^2 (or sum w v^2 with weights w) into ctl->red[slot]; optionally also writes a
+// float copy of v.
 __global__ void __launch_bounds__(256) k_norm2(long long N, const double* __restrict__ v, float* __restrict__ v32,
-                                               double* __restrict__ partials, SolveCtl* __restrict__ ctl, int slot) {
+                                               const double* __restrict__ w, double* __restrict__ partials,
+                                               SolveCtl* __restrict__ ctl, int slot) {
     double s = 0.0;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
         const double a = v[n];
         if (v32) v32[n] = (float)a;
-        s += a * a;
+        s += w ? w[n] * (a * a) : a * a;
     }
-    double w[1] = {s};
-    write_partial<1, OpSum>(w, partials, blockIdx.x);
+    double acc[1] = {s};
+    write_partial<1, OpSum>(acc, partials, blockIdx.x);
     if (arrive_last(&ctl->arrive[2], gridDim.x)) {
-        reduce_partials<1, OpSum>(w, partials, gridDim.x);
-        if (linear_tid() == 0) ctl->red[slot] = w[0];
+        reduce_partials<1, OpSum>(acc, partials, gridDim.x);
+        if (linear_tid() == 0) ctl->red[slot] = acc[0];
+    }
+}
+
+// sum over free rows (M^-1 > 0) of A_nn x_n^2 (or (A_nn x_n)^2 with `squared`) into
+// ctl->red[slot]: the scale of the rounding floor of b - A x in the Jacobi-scaled (plain) norm
+__global__ void __launch_bounds__(256) k_diag_norm2(long long N, const double* __restrict__ x,
+                                                    const double* __restrict__ minv, int squared,
+                                                    double* __restrict__ partials, SolveCtl* __restrict__ ctl,
+                                                    int slot) {
+    double s = 0.0;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+        const double m = minv[n];
+        if (m > 0.0) s += squared ? (x[n] * x[n]) / (m * m) : (x[n] * x[n]) / m;
+    }
+    double acc[1] = {s};
+    write_partial<1, OpSum>(acc, partials, blockIdx.x);
+    if (arrive_last(&ctl->arrive[2], gridDim.x)) {
+        reduce_partials<1, OpSum>(acc, partials, gridDim.x);
+        if (linear_tid() == 0) ctl->red[slot] = acc[0];
     }
 }
 
@@ -810,9 +876,20 @@ void launch_cg_start(const LaunchCfg& c, long long N, float* x, bool zero_x, con
         launch(k_cg_start<float, false>, vec_blocks(c, N), 256, c.stream, N, x, r, p, minv, partials, ctl, rtol, ref_slot,
                                                                          maxit, stall_limit);
 }
+void launch_fcg_dots(const LaunchCfg& c, long long N, const float* z, const float* r, const float* q, double* partials,
+                     SolveCtl* ctl, int first) {
+    launch(k_fcg_dots, vec_blocks(c, N), 256, c.stream, N, z, r, q, partials, ctl, first);
+}
+void launch_fcg_direction(const LaunchCfg& c, long long N, float* p, const float* z, const SolveCtl* ctl) {
+    launch(k_fcg_direction, vec_blocks(c, N), 256, c.stream, N, p, z, ctl);
+}
+void launch_diag_norm2(const LaunchCfg& c, long long N, const double* x, const double* minv, int squared,
+                       double* partials, SolveCtl* ctl, int slot) {
+    launch(k_diag_norm2, vec_blocks(c, N), 256, c.stream, N, x, minv, squared, partials, ctl, slot);
+}
 void launch_norm2(const LaunchCfg& c, long long N, const double* v, float* v32, double* partials, SolveCtl* ctl,
-                  int slot) {
-    launch(k_norm2, vec_blocks(c, N), 256, c.stream, N, v, v32, partials, ctl, slot);
+                  int slot, const double* w) {
+    launch(k_norm2, vec_blocks(c, N), 256, c.stream, N, v, v32, w, partials, ctl, slot);
 }
 __global__ void __launch_bounds__(256) k_widen(long long N, const float* __restrict__ a, double* __restrict__ b) {
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x)

@@ -79,8 +79,15 @@ void launch_cg_start(const LaunchCfg& c, long long N, double* x, bool zero_x, co
 void launch_cg_start(const LaunchCfg& c, long long N, float* x, bool zero_x, const float* r, float* p,
                      const float* minv, double* partials, SolveCtl* ctl, double rtol, int ref_slot, int maxit,
                      int stall_limit);
+void launch_fcg_dots(const LaunchCfg& c, long long N, const float* z, const float* r, const float* q, double* partials,
+                     SolveCtl* ctl, int first);
+void launch_fcg_direction(const LaunchCfg& c, long long N, float* p, const float* z, const SolveCtl* ctl);
+// red[slot] = sum over rows with minv > 0 of x^2 / minv (= A_nn x_n^2), or of (A_nn x_n)^2
+void launch_diag_norm2(const LaunchCfg& c, long long N, const double* x, const double* minv, int squared,
+                       double* partials, SolveCtl* ctl, int slot);
+// red[slot] = ||v||^2, or sum w v^2 when w is given (w = M^-1: the Jacobi-scaled norm)
 void launch_norm2(const LaunchCfg& c, long long N, const double* v, float* v32, double* partials, SolveCtl* ctl,
-                  int slot);
+                  int slot, const double* w = nullptr);
 void launch_fill(const LaunchCfg& c, long long N, double* v, double value);
 void launch_widen(const LaunchCfg& c, long long N, const float* a, double* b);
 void launch_add_correction(const LaunchCfg& c, long long N, double* T, const float* d);

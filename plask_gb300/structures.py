@@ -217,3 +217,120 @@ def sweep_c3(seed=3000, count=256, lo=32, hi=96):
         pw = float(rng.uniform(1e15, 1e17))
         out.append(layered_c0(seed=seed + 1 + i, n=n, power=pw))
     return out
+
+
+@dataclasses.dataclass
+class ElecStructure:
+    """Everything one Shockley3D solve needs, in plain arrays.
+
+    * ``axes``: node coordinates in um (axis 2 vertical)
+    * ``mat``: int32 element material ids, shape (n2-1, n1-1, n0-1), axis 0 fastest
+    * ``cond_xy``, ``cond_z``: per-material conductivity tensor (S/m); ``eps``:
+      relative permittivity; ``empty``: EMPTY materials; ``noheat``: no Joule heat
+    * ``junction``: element junction number + 1 (0 outside), same shape as ``mat``
+    * ``beta`` (1/V), ``js`` (A/m^2): per junction
+    * ``voltage``: [(node mask (n2, n1, n0), volts)] in list order
+    * ``symmetric``: (axis 0, axis 1) mirror symmetry at the low end, which doubles
+      the reference's total current and heat per symmetric direction
+    * ``thermal``: the matching Static3D structure of a coupled problem, or None
+    """
+
+    axes: tuple
+    mat: np.ndarray
+    cond_xy: np.ndarray
+    cond_z: np.ndarray
+    eps: np.ndarray
+    empty: np.ndarray
+    noheat: np.ndarray
+    junction: np.ndarray
+    beta: list
+    js: list
+    voltage: list
+    symmetric: tuple = (False, False)
+    maxerr: float = 0.05
+    thermal: Structure | None = None
+    name: str = ""
+
+    @property
+    def shape(self):
+        return tuple(len(a) for a in self.axes[::-1])
+
+    def element_cond(self):
+        """(ne2, ne1, ne0, 2) table conductivities per element."""
+        return np.stack([self.cond_xy[self.mat], self.cond_z[self.mat]], axis=-1)
+
+
+def _divide(points, parts):
+    """Every interval between consecutive points split into ``parts`` equal cells."""
+    out = [points[0]]
+    for a, b in zip(points[:-1], points[1:]):
+        out.extend(a + (b - a) * np.arange(1, parts + 1) / parts)
+    return np.asarray(out, np.float64)
+
+
+def shockley_diode(prediv=(3, 3, 2), junction_eps=12.9):
+    """A p-n junction between two ideal conductors, 1000 x 1000 um, 0.02 um thick:
+    300 um conductor blocks (1e9 S/m) on both sides of the junction and 700 x 700 x 1 um
+    contacts at the top (0 V on its top face) and bottom (1 V on its bottom face),
+    surrounded by air.  Each interval between object edges is divided into ``prediv``
+    equal cells.  With beta = 10 1/V and js = 1 A/m^2 the current is
+    1e-9 S js (e^beta - 1) mA with S = 1e6 um^2, and the Joule heat that times 1 V.
+    """
+    x = _divide([-500.0, -350.0, 350.0, 500.0], prediv[0])
+    y = _divide([-500.0, -350.0, 350.0, 500.0], prediv[1])
+    zb = [0.0, 1.0, 301.0, 301.02, 601.02, 602.02]
+    z = _divide(zb, prediv[2])
+    ne = (len(z) - 1, len(y) - 1, len(x) - 1)
+    xm, ym, zm = (0.5 * (a[1:] + a[:-1]) for a in (x, y, z))
+    mat = np.zeros(ne, np.int32)  # conductor
+    in_contact = (np.abs(xm)[None, :] < 350.0) & (np.abs(ym)[:, None] < 350.0)
+    for k, zc in enumerate(zm):
+        if zc < 1.0 or zc > 601.02:
+            mat[k] = np.where(in_contact, 0, 2)
+        elif 301.0 < zc < 301.02:
+            mat[k] = 1
+    junction = (mat == 1).astype(np.int32)
+    shape = (len(z), len(y), len(x))
+    on_contact = (np.abs(x)[None, :] <= 350.0) & (np.abs(y)[:, None] <= 350.0)
+    top = np.zeros(shape, bool)
+    top[-1] = on_contact
+    bottom = np.zeros(shape, bool)
+    bottom[0] = on_contact
+    return ElecStructure(axes=(x, y, z), mat=mat, cond_xy=np.array([1e9, 5.0, 0.55e-14]),
+                         cond_z=np.array([1e9, 5.0, 0.55e-14]), eps=np.array([1.0, junction_eps, 1.0]),
+                         empty=np.array([False, False, True]), noheat=np.zeros(3, bool), junction=junction,
+                         beta=[10.0], js=[1.0], voltage=[(top, 0.0), (bottom, 1.0)], maxerr=1e-3,
+                         name=f"shockley-diode-{prediv[0]}{prediv[1]}{prediv[2]}")
+
+
+def shockley_c4(seed=4000, n=(200, 200, 120), voltage=None, n_layers=12, contact_radius=6.0):
+    """Coupled thermal-electrical case: the layered generator with a 20 nm junction
+    layer (js = 1 A/m^2, beta = 18 1/V), per-layer electrical conductivity log-uniform
+    in 1e-1..1e5 S/m, ``voltage`` (uniform in 1.6..2.2 V when None) on a top disc contact
+    of radius 6 um at x = y = 0 (a quarter of the device: symmetric in axes 0 and 1)
+    and 0 V on the bottom face.  The thermal structure has the bottom at 300 K and no
+    heat sources of its own: its heat comes from the electrical solution."""
+    rng = np.random.default_rng(seed)
+    nl = _fit_layers(n, n_layers)
+    d = _layered(rng, n, nl, 0.02, True, 0.0, 0.0)
+    x0, x1, z = d["axes"]
+    layer_of = d["mat"][:, 0, 0]
+    dz = np.diff(z)
+    thickness = np.array([dz[layer_of == m].sum() for m in range(nl + 1)])
+    thickness[0] = np.inf  # the substrate
+    junction_layer = int(np.argmin(np.abs(thickness - 0.02)))
+    n_mat = nl + 1
+    sigma = np.exp(rng.uniform(math.log(1e-1), math.log(1e5), n_mat))
+    volts = float(rng.uniform(1.6, 2.2)) if voltage is None else float(voltage)
+    mat = d["mat"]
+    junction = (mat == junction_layer).astype(np.int32)
+    shape = (len(z), len(x1), len(x0))
+    top = np.zeros(shape, bool)
+    top[-1] = (x0[None, :] ** 2 + x1[:, None] ** 2) <= contact_radius ** 2
+    bottom = np.zeros(shape, bool)
+    bottom[0] = True
+    thermal = Structure(**d, temperature=[("bottom", 300.0)], name=f"shockley-thermal-{n[0]}x{n[1]}x{n[2]}-s{seed}")
+    return ElecStructure(axes=(x0, x1, z), mat=mat, cond_xy=sigma, cond_z=sigma.copy(), eps=np.full(n_mat, 12.0),
+                         empty=np.zeros(n_mat, bool), noheat=np.zeros(n_mat, bool), junction=junction, beta=[18.0],
+                         js=[1.0], voltage=[(top, volts), (bottom, 0.0)], symmetric=(True, True), maxerr=0.1,
+                         thermal=thermal, name=f"shockley-{n[0]}x{n[1]}x{n[2]}-s{seed}")

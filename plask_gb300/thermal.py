@@ -193,7 +193,8 @@ class Static3D:
     ``outTemperature``, ``outHeatFlux``, ``outThermalConductivity``.
 
     Extra GPU knobs: ``rtol`` (FP64 relative residual of every linear solve,
-    default 1e-14) and ``bc_compat`` (True: the reference's placement of 3D
+    default 1e-14), ``residual_norm`` ("plain": 2-norm, the default; "scaled":
+    Jacobi-weighted, for strong conductivity contrast) and ``bc_compat`` (True: the reference's placement of 3D
     face boundary terms).
     """
 
@@ -207,6 +208,7 @@ class Static3D:
         self.iterative = IterativeParams()
         self._empty_elements = "default"
         self.rtol = 1e-14
+        self.residual_norm = "plain"
         self.bc_compat = True
         self.temperature_boundary = BoundaryConditions(self, _native.BC_TEMPERATURE, 1)
         self.heatflux_boundary = BoundaryConditions(self, _native.BC_HEATFLUX, 1)
@@ -223,6 +225,7 @@ class Static3D:
         self._toterr = 0.0
         self.stats = {}
         self.loop_log = []
+        self._preconditioner = None
 
     # ---------------------------------------------------------------- properties
     @property
@@ -271,6 +274,17 @@ class Static3D:
         self.invalidate()
 
     @property
+    def preconditioner(self):
+        """Learned preconditioner (plask_gb300._native.UNet) used by algorithm "gpu-learned"."""
+        return self._preconditioner
+
+    @preconditioner.setter
+    def preconditioner(self, net):
+        self._preconditioner = net
+        if self._fem is not None:
+            _native.attach_preconditioner(self._fem, net)
+
+    @property
     def inHeat(self):
         return self._inHeat
 
@@ -301,6 +315,8 @@ class Static3D:
             self._fem = _native.Fem3D(self._mesh.axes, self._mesh.ordering)
             self._fem.set_log_callback(self._log)
             self._elements_dirty = self._bc_dirty = self._heat_dirty = True
+            if self._preconditioner is not None:
+                _native.attach_preconditioner(self._fem, self._preconditioner)
         fem = self._fem
         if self._elements_dirty:
             mt = self._geometry.materials
@@ -328,6 +344,7 @@ class Static3D:
         it = self.iterative
         maxit = it.maxit if self._algorithm == "iterative" and it.maxit != 1000 else 0
         fem.set_solver(self._algorithm, self.rtol, maxit, it.noconv, self._empty_elements, self.bc_compat)
+        fem.set_residual_norm(self.residual_norm)
         fem.set_loop(self.inittemp, self.maxerr)
 
     def invalidate(self):
