@@ -15,92 +15,16 @@
 //
 // All reductions are deterministic: every block writes one partial per value
 // and the last block to arrive sums the partials in a fixed order.
+#include <algorithm>
 #include <atomic>
 #include <cfloat>
 #include <cstdint>
 
 #include "fem3d_device.cuh"
 #include "fem3d_kernels.h"
+#include "fem3d_reduce.cuh"
 
 namespace plgpu {
-
-// ----------------------------------------------------------------------------------------
-// reductions
-
-struct OpSum {
-    __device__ static double init() { return 0.0; }
-    __device__ static double op(double a, double b) { return a + b; }
-};
-struct OpMax {
-    __device__ static double init() { return -DBL_MAX; }
-    __device__ static double op(double a, double b) { return a > b ? a : b; }
-};
-
-__device__ __forceinline__ int linear_tid() {
-    return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
-}
-__device__ __forceinline__ int block_threads() { return blockDim.x * blockDim.y * blockDim.z; }
-__device__ __forceinline__ int linear_bid() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
-
-// Block-wide reduction of NV values; the result is valid in every thread.
-template <int NV, typename Op>
-__device__ void block_reduce(double (&v)[NV]) {
-    __shared__ double sh[NV][32];
-    const int t = linear_tid(), lane = t & 31, warp = t >> 5, nw = (block_threads() + 31) >> 5;
-#pragma unroll
-    for (int i = 0; i < NV; ++i)
-        for (int o = 16; o; o >>= 1) v[i] = Op::op(v[i], __shfl_xor_sync(0xffffffffu, v[i], o));
-    if (lane == 0) {
-#pragma unroll
-        for (int i = 0; i < NV; ++i) sh[i][warp] = v[i];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < NV; ++i) {
-        double w = lane < nw ? sh[i][lane] : Op::init();
-        for (int o = 16; o; o >>= 1) w = Op::op(w, __shfl_xor_sync(0xffffffffu, w, o));
-        v[i] = w;
-    }
-    __syncthreads();
-}
-
-// Write this block's reduced values to partials[i * kMaxPartialBlocks + slot].
-template <int NV, typename Op>
-__device__ void write_partial(double (&v)[NV], double* partials, int slot) {
-    block_reduce<NV, Op>(v);
-    if (linear_tid() == 0) {
-#pragma unroll
-        for (int i = 0; i < NV; ++i) partials[(size_t)i * kMaxPartialBlocks + slot] = v[i];
-    }
-}
-
-// Count this block's arrival; true in the last of `expected` arriving blocks.
-__device__ bool arrive_last(unsigned int* counter, unsigned int expected) {
-    __shared__ int last;
-    __threadfence();
-    __syncthreads();
-    if (linear_tid() == 0) {
-        unsigned int prev = atomicAdd(counter, 1u);
-        last = (prev == expected - 1u);
-        if (last) *counter = 0u;  // ready for the next launch
-    }
-    __syncthreads();
-    if (last) __threadfence();
-    return last != 0;
-}
-
-// Sum partial slots [0, nslots) in a fixed order (valid in every thread).
-template <int NV, typename Op>
-__device__ void reduce_partials(double (&v)[NV], const double* partials, int nslots) {
-    const int t = linear_tid(), nt = block_threads();
-#pragma unroll
-    for (int i = 0; i < NV; ++i) {
-        double a = Op::init();
-        for (int s = t; s < nslots; s += nt) a = Op::op(a, __ldcg(partials + (size_t)i * kMaxPartialBlocks + s));
-        v[i] = a;
-    }
-    block_reduce<NV, Op>(v);
-}
 
 __device__ __forceinline__ bool is_dir(const uint32_t* __restrict__ dmask, long long n) {
     return (__ldg(dmask + (n >> 5)) >> (n & 31)) & 1u;
@@ -218,45 +142,37 @@ __global__ void __launch_bounds__(256) k_apply_gather(const GridT<R> g, const R*
 }
 
 // Convective face terms: a sparse symmetric operator on free nodes.
-// MODE_CG:    y[row] += S x; partial (x, S x); the last block finishes (p, A p) over
-//             all partial slots and sets alpha = rz / pq.
+// MODE_MULT:  y[row] += S x
 // MODE_RESID: y[row] -= S x
-template <typename R, int MODE>
-__global__ void __launch_bounds__(256) k_surface(const SurfaceT<R> s, const R* __restrict__ x, R* __restrict__ y,
-                                                 double* __restrict__ partials, int slot0, int nslots,
-                                                 SolveCtl* __restrict__ ctl) {
-    if (MODE == MODE_CG && ctl->status != SOLVE_RUNNING) return;
+// MODE_CG (before the operator): y[row] = S x and this block's partial of (x, S x); the
+// operator adds its stencil to these rows and finishes the dot product.
+template <typename R>
+__global__ void __launch_bounds__(256) k_surface_cg(const SurfaceT<R> s, const R* __restrict__ x, R* __restrict__ y,
+                                                    double* __restrict__ partials, int slot0,
+                                                    const SolveCtl* __restrict__ ctl) {
+    if (ctl->status != SOLVE_RUNNING) return;
     double dot = 0.0;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < s.nrows; r += gridDim.x * blockDim.x) {
         const int n = s.row[r];
         R acc = R(0);
         for (int q = s.ptr[r]; q < s.ptr[r + 1]; ++q) acc += s.val[q] * x[s.col[q]];
-        if (MODE == MODE_CG) {
-            y[n] += acc;
-            dot += (double)x[n] * (double)acc;
-        } else if (MODE == MODE_MULT) {
-            y[n] += acc;
-        } else {
-            y[n] -= acc;
-        }
+        y[n] = acc;
+        dot += (double)x[n] * (double)acc;
     }
-    if (MODE == MODE_CG) {
-        double v[1] = {dot};
-        write_partial<1, OpSum>(v, partials, slot0 + blockIdx.x);
-        if (arrive_last(&ctl->arrive[0], gridDim.x)) {
-            reduce_partials<1, OpSum>(v, partials, nslots);
-            if (linear_tid() == 0) {
-                const double pq = v[0];
-                ctl->pq = pq;
-                if (!isfinite(pq)) {
-                    ctl->status = SOLVE_NONFINITE;
-                } else if (!(pq > 0.0)) {
-                    ctl->status = SOLVE_BREAKDOWN;
-                } else {
-                    ctl->alpha = ctl->rz / pq;
-                }
-            }
-        }
+    double v[1] = {dot};
+    write_partial<1, OpSum>(v, partials, slot0 + blockIdx.x);
+}
+
+template <typename R, int MODE>
+__global__ void __launch_bounds__(256) k_surface(const SurfaceT<R> s, const R* __restrict__ x, R* __restrict__ y) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < s.nrows; r += gridDim.x * blockDim.x) {
+        const int n = s.row[r];
+        R acc = R(0);
+        for (int q = s.ptr[r]; q < s.ptr[r + 1]; ++q) acc += s.val[q] * x[s.col[q]];
+        if (MODE == MODE_MULT)
+            y[n] += acc;
+        else
+            y[n] -= acc;
     }
 }
 
@@ -312,6 +228,100 @@ __global__ void __launch_bounds__(256) k_cg_update(long long N, R* __restrict__ 
             }
         }
     }
+}
+
+// FP32 forms of k_cg_update and k_cg_direction with 16-byte accesses: thread t
+// handles the float4 groups t, t + stride, ...; the last N % 4 entries by the first
+// threads.  Same arithmetic per entry as the scalar kernels.
+__device__ __forceinline__ void cg_update_one(float& x, float& r, float p, float q, float m, float alpha, float& rz,
+                                              float& rr) {
+    x += alpha * p;
+    const float rn = m != 0.f ? r - alpha * q : 0.f;
+    r = rn;
+    rz += rn * (m * rn);
+    rr += rn * rn;
+}
+
+__global__ void __launch_bounds__(256) k_cg_update_v4(long long N, float* __restrict__ x, float* __restrict__ r,
+                                                      const float* __restrict__ p, const float* __restrict__ q,
+                                                      const float* __restrict__ minv, double* __restrict__ partials,
+                                                      SolveCtl* __restrict__ ctl) {
+    if (ctl->status != SOLVE_RUNNING) return;
+    const float alpha = (float)ctl->alpha;
+    float rz = 0.f, rr = 0.f;
+    const long long N4 = N >> 2, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    float4* x4 = reinterpret_cast<float4*>(x);
+    float4* r4 = reinterpret_cast<float4*>(r);
+    const float4* p4 = reinterpret_cast<const float4*>(p);
+    const float4* q4 = reinterpret_cast<const float4*>(q);
+    const float4* m4 = reinterpret_cast<const float4*>(minv);
+    for (long long v = t0; v < N4; v += stride) {
+        const float4 pn = p4[v], qn = q4[v], mn = m4[v];
+        float4 xn = x4[v], rn = r4[v];
+        cg_update_one(xn.x, rn.x, pn.x, qn.x, mn.x, alpha, rz, rr);
+        cg_update_one(xn.y, rn.y, pn.y, qn.y, mn.y, alpha, rz, rr);
+        cg_update_one(xn.z, rn.z, pn.z, qn.z, mn.z, alpha, rz, rr);
+        cg_update_one(xn.w, rn.w, pn.w, qn.w, mn.w, alpha, rz, rr);
+        x4[v] = xn;
+        r4[v] = rn;
+    }
+    for (long long n = (N4 << 2) + t0; n < N; n += stride) {
+        float xn = x[n], rn = r[n];
+        cg_update_one(xn, rn, p[n], q[n], minv[n], alpha, rz, rr);
+        x[n] = xn;
+        r[n] = rn;
+    }
+    double v[2] = {(double)rz, (double)rr};
+    write_partial<2, OpSum>(v, partials, blockIdx.x);
+    if (arrive_last(&ctl->arrive[1], gridDim.x)) {
+        reduce_partials<2, OpSum>(v, partials, gridDim.x);
+        if (linear_tid() == 0) {
+            const double rzn = v[0], rrn = v[1];
+            ctl->iter += 1;
+            ctl->rz_old = ctl->rz;
+            ctl->beta = rzn / ctl->rz;
+            ctl->rz = rzn;
+            ctl->rr = rrn;
+            if (!isfinite(rrn) || !isfinite(rzn)) {
+                ctl->status = SOLVE_NONFINITE;
+            } else if ((ctl->plain ? rrn : rzn) <= ctl->tol2) {
+                ctl->status = SOLVE_CONVERGED;
+            } else if (ctl->iter >= ctl->maxit) {
+                ctl->status = SOLVE_MAXIT;
+            } else {
+                const double m = ctl->plain ? rrn : rzn;
+                if (m < 0.81 * ctl->best_rr) {  // residual norm fell by 10 %
+                    ctl->best_rr = m;
+                    ctl->stall = 0;
+                } else if (++ctl->stall > ctl->stall_limit) {
+                    ctl->status = SOLVE_STAGNATED;
+                }
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_cg_direction_v4(long long N, float* __restrict__ p,
+                                                         const float* __restrict__ r, const float* __restrict__ minv,
+                                                         const SolveCtl* __restrict__ ctl) {
+    if (ctl->status != SOLVE_RUNNING) return;
+    const float beta = (float)ctl->beta;
+    const long long N4 = N >> 2, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    float4* p4 = reinterpret_cast<float4*>(p);
+    const float4* r4 = reinterpret_cast<const float4*>(r);
+    const float4* m4 = reinterpret_cast<const float4*>(minv);
+    for (long long v = t0; v < N4; v += stride) {
+        const float4 rn = r4[v], mn = m4[v];
+        float4 pn = p4[v];
+        pn.x = mn.x * rn.x + beta * pn.x;
+        pn.y = mn.y * rn.y + beta * pn.y;
+        pn.z = mn.z * rn.z + beta * pn.z;
+        pn.w = mn.w * rn.w + beta * pn.w;
+        p4[v] = pn;
+    }
+    for (long long n = (N4 << 2) + t0; n < N; n += stride) p[n] = minv[n] * r[n] + beta * p[n];
 }
 
 // p = M^-1 r + beta p
@@ -810,27 +820,35 @@ void launch_apply(const LaunchCfg& c, const GridT<float>& g, const float* x, flo
 }
 
 template <typename R>
-static void launch_surface_any(const LaunchCfg& c, const SurfaceT<R>& s, const R* x, R* y, double* partials, int slot0,
-                               int mode, SolveCtl* ctl) {
-    const int blocks = mode == MODE_CG ? surface_blocks(s.nrows) : grid_for(s.nrows, 256, 1024);
-    if (mode == MODE_CG) {
-        launch(k_surface<R, MODE_CG>, blocks, 256, c.stream, s, x, y, partials, slot0, slot0 + blocks, ctl);
-    } else if (mode == MODE_MULT) {
-        if (s.nrows == 0) return;
-        launch(k_surface<R, MODE_MULT>, blocks, 256, c.stream, s, x, y, partials, slot0, slot0 + blocks, ctl);
-    } else {
-        if (s.nrows == 0) return;
-        launch(k_surface<R, MODE_RESID>, blocks, 256, c.stream, s, x, y, partials, slot0, slot0 + blocks, ctl);
-    }
+static void launch_surface_any(const LaunchCfg& c, const SurfaceT<R>& s, const R* x, R* y, int mode) {
+    if (s.nrows == 0) return;
+    const int blocks = grid_for(s.nrows, 256, 1024);
+    if (mode == MODE_MULT)
+        launch(k_surface<R, MODE_MULT>, blocks, 256, c.stream, s, x, y);
+    else if (mode == MODE_RESID)
+        launch(k_surface<R, MODE_RESID>, blocks, 256, c.stream, s, x, y);
 }
-int surface_blocks(int nrows) { return grid_for(nrows, 256, 64); }
-void launch_surface(const LaunchCfg& c, const SurfaceT<double>& s, const double* x, double* y, double* partials,
-                    int slot0, int mode, SolveCtl* ctl) {
-    launch_surface_any<double>(c, s, x, y, partials, slot0, mode, ctl);
+int surface_cg_blocks(int nrows) { return nrows > 0 ? grid_for(nrows, 256, 256) : 0; }
+template <typename R>
+static int surface_cg_any(const LaunchCfg& c, const SurfaceT<R>& s, const R* x, R* y, double* partials, int slot0,
+                          const SolveCtl* ctl) {
+    const int blocks = surface_cg_blocks(s.nrows);
+    if (blocks > 0) launch(k_surface_cg<R>, blocks, 256, c.stream, s, x, y, partials, slot0, ctl);
+    return blocks;
 }
-void launch_surface(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, double* partials, int slot0,
-                    int mode, SolveCtl* ctl) {
-    launch_surface_any<float>(c, s, x, y, partials, slot0, mode, ctl);
+int launch_surface_cg(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, double* partials,
+                      int slot0, const SolveCtl* ctl) {
+    return surface_cg_any<float>(c, s, x, y, partials, slot0, ctl);
+}
+int launch_surface_cg(const LaunchCfg& c, const SurfaceT<double>& s, const double* x, double* y, double* partials,
+                      int slot0, const SolveCtl* ctl) {
+    return surface_cg_any<double>(c, s, x, y, partials, slot0, ctl);
+}
+void launch_surface(const LaunchCfg& c, const SurfaceT<double>& s, const double* x, double* y, int mode) {
+    launch_surface_any<double>(c, s, x, y, mode);
+}
+void launch_surface(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, int mode) {
+    launch_surface_any<float>(c, s, x, y, mode);
 }
 
 int vec_blocks(const LaunchCfg& c, long long N) { return grid_for(N, 256, c.vec_blocks); }
@@ -844,9 +862,30 @@ void launch_cg_update(const LaunchCfg& c, long long N, double* x, double* r, con
                       const double* minv, double* partials, SolveCtl* ctl) {
     cg_update_any(c, N, x, r, p, q, minv, partials, ctl);
 }
+// Grid of the 16-byte FP32 vector kernels: exactly the blocks that are resident at once
+// (one wave, no partial second wave), each thread striding over float4 groups.
+template <typename Kern>
+static int resident_per_sm(Kern kern) {
+    static int occ = 0;  // per kernel (one instantiation per kernel type)
+    if (occ == 0) {
+        int v = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, 256, 0) != cudaSuccess || v < 1) v = 1;
+        occ = v;
+    }
+    return occ;
+}
+template <typename Kern>
+static int vec4_blocks(const LaunchCfg& c, long long N, Kern kern) {
+    return grid_for((N + 3) / 4, 256, std::min(c.sm_count * resident_per_sm(kern), kMaxPartialBlocks));
+}
+// Occupancy queries outside any stream capture (called when a handle is created).
+void prime_launch_shapes() {
+    resident_per_sm(k_cg_update_v4);
+    resident_per_sm(k_cg_direction_v4);
+}
 void launch_cg_update(const LaunchCfg& c, long long N, float* x, float* r, const float* p, const float* q,
                       const float* minv, double* partials, SolveCtl* ctl) {
-    cg_update_any(c, N, x, r, p, q, minv, partials, ctl);
+    launch(k_cg_update_v4, vec4_blocks(c, N, k_cg_update_v4), 256, c.stream, N, x, r, p, q, minv, partials, ctl);
 }
 void launch_cg_direction(const LaunchCfg& c, long long N, double* p, const double* r, const double* minv,
                          const SolveCtl* ctl) {
@@ -854,7 +893,7 @@ void launch_cg_direction(const LaunchCfg& c, long long N, double* p, const doubl
 }
 void launch_cg_direction(const LaunchCfg& c, long long N, float* p, const float* r, const float* minv,
                          const SolveCtl* ctl) {
-    launch(k_cg_direction<float>, vec_blocks(c, N), 256, c.stream, N, p, r, minv, ctl);
+    launch(k_cg_direction_v4, vec4_blocks(c, N, k_cg_direction_v4), 256, c.stream, N, p, r, minv, ctl);
 }
 void launch_cg_start(const LaunchCfg& c, long long N, double* x, bool zero_x, const double* r, double* p,
                      const double* minv, double* partials, SolveCtl* ctl, double rtol, int ref_slot, int maxit,

@@ -41,8 +41,8 @@ struct LaunchCfg {
 };
 
 long long launch_count();  // kernels launched by this library so far (all handles)
+void prime_launch_shapes();  // occupancy-derived grid sizes, queried before any graph capture
 int apply_blocks(const LaunchCfg& c, int n0, int n1, int n2);
-int surface_blocks(int nrows);
 int vec_blocks(const LaunchCfg& c, long long N);
 
 void launch_apply(const LaunchCfg& c, const GridT<double>& g, const double* x, double* y, const double* kxy,
@@ -54,17 +54,28 @@ void launch_apply(const LaunchCfg& c, const GridT<float>& g, const float* x, flo
 // Optimised operator (fem3d_operator.cu).  zf[k] = dz_k / 48, zr[k] = 1 / (48 dz_k).
 // number of blocks (= partial-sum slots written in MODE_CG) of one operator launch
 int op_blocks(const LaunchCfg& c, int n0, int n1, int n2, bool fp64);
+// MODE_CG: y = A x, where nodes flagged in smask add the S x that k_surface (launched
+// just before, launch_surface_cg) left in y; the last block sums the operator's partials
+// and the sslots surface partials after them into (x, A x) and sets alpha = rz / (x, A x)
+// (or the breakdown / non-finite status).
 void launch_operator(const LaunchCfg& c, const GridT<float>& g, const float* zf, const float* zr, const float* x,
                      float* y, const float* kxy, const float* kz, bool aniso, const uint32_t* dmask, const float* rhs,
-                     double* partials, int mode, const SolveCtl* ctl);
+                     double* partials, int mode, SolveCtl* ctl, const uint32_t* smask = nullptr, int sslots = 0);
 void launch_operator(const LaunchCfg& c, const GridT<double>& g, const double* zf, const double* zr, const double* x,
                      double* y, const double* kxy, const double* kz, bool aniso, const uint32_t* dmask,
-                     const double* rhs, double* partials, int mode, const SolveCtl* ctl);
+                     const double* rhs, double* partials, int mode, SolveCtl* ctl, const uint32_t* smask = nullptr,
+                     int sslots = 0);
+// CG step, first half: y[row] = S x on the surface rows and block partials of (x, S x) in
+// slots slot0..slot0 + surface_cg_blocks - 1; returns the number of slots used.
+int launch_surface_cg(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, double* partials,
+                      int slot0, const SolveCtl* ctl);
+int launch_surface_cg(const LaunchCfg& c, const SurfaceT<double>& s, const double* x, double* y, double* partials,
+                      int slot0, const SolveCtl* ctl);
+int surface_cg_blocks(int nrows);
 
-void launch_surface(const LaunchCfg& c, const SurfaceT<double>& s, const double* x, double* y, double* partials,
-                    int slot0, int mode, SolveCtl* ctl);
-void launch_surface(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, double* partials,
-                    int slot0, int mode, SolveCtl* ctl);
+// convective face terms in MODE_MULT (y += S x) or MODE_RESID (y -= S x)
+void launch_surface(const LaunchCfg& c, const SurfaceT<double>& s, const double* x, double* y, int mode);
+void launch_surface(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, int mode);
 void launch_cg_update(const LaunchCfg& c, long long N, double* x, double* r, const double* p, const double* q,
                       const double* minv, double* partials, SolveCtl* ctl);
 void launch_cg_update(const LaunchCfg& c, long long N, float* x, float* r, const float* p, const float* q,

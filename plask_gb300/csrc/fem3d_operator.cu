@@ -28,6 +28,7 @@
 
 #include "fem3d_device.cuh"
 #include "fem3d_kernels.h"
+#include "fem3d_reduce.cuh"
 
 namespace plgpu {
 
@@ -41,10 +42,14 @@ struct OpArgs {
     const uint32_t* dmask;
     const R* rhs;
     double* partials;
-    const SolveCtl* ctl;
+    SolveCtl* ctl;
     const R* zf;       // per element layer: dz / 48      (n2 - 1)
     const R* zr;       // per element layer: 1 / (48 dz)  (n2 - 1)
     int zchunk;        // planes per block along z
+    // MODE_CG: nodes with a convective surface row (bit set) already hold S x in y,
+    // written by k_surface, whose block partials of (x, S x) follow the operator's
+    const uint32_t* smask;
+    int sslots;
 };
 
 __device__ __forceinline__ bool dir_bit(const uint32_t* __restrict__ m, long long n) {
@@ -210,6 +215,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 2) k_apply_haar(cons
                         // Dirichlet rows: x is zero there and M^-1 = 0 keeps the CG residual zero
                         out = acc[r - 1];
                         dot += xlo[r] * out;
+                        if (a.smask != nullptr && dir_bit(a.smask, n)) out += a.y[n];
                     } else if (MODE == MODE_RESID) {
                         out = dir_bit(a.dmask, n) ? R(a.rhs[n] - a.x[n]) : R(a.rhs[n] - acc[r - 1]);
                     } else if (MODE == MODE_MULT) {
@@ -239,15 +245,24 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 2) k_apply_haar(cons
         }
     }
     if (MODE == MODE_CG) {
-        // block partial of (x, y)
-        __shared__ double sh[4];
-        const double dw = warp_sum_d((double)dot);
-        if (lane == 0) sh[warp] = dw;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double s = 0.0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[w];
-            a.partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s;
+        const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+        // (x, A x): block partial, then the last block to finish adds the surface kernel's
+        // partials and sets the step length
+        double v[1] = {(double)dot};
+        write_partial<1, OpSum>(v, a.partials, bid);
+        const int nblocks = gridDim.x * gridDim.y * gridDim.z;
+        if (arrive_last(&a.ctl->arrive[0], nblocks)) {
+            reduce_partials<1, OpSum>(v, a.partials, nblocks + a.sslots);
+            if (threadIdx.x == 0) {
+                const double pq = v[0];
+                a.ctl->pq = pq;
+                if (!isfinite(pq))
+                    a.ctl->status = SOLVE_NONFINITE;
+                else if (!(pq > 0.0))
+                    a.ctl->status = SOLVE_BREAKDOWN;
+                else
+                    a.ctl->alpha = a.ctl->rz / pq;
+            }
         }
     }
 }
@@ -302,12 +317,12 @@ int op_blocks(const LaunchCfg& c, int n0, int n1, int n2, bool fp64) {
 template <typename R>
 static void op_launch(const LaunchCfg& c, const GridT<R>& g, const R* zf, const R* zr, const R* x, R* y, const R* kxy,
                       const R* kz, bool aniso, const uint32_t* dmask, const R* rhs, double* partials, int mode,
-                      const SolveCtl* ctl) {
+                      SolveCtl* ctl, const uint32_t* smask, int sslots) {
     constexpr int kRows = Rows<R>::value;
     dim3 grid;
     int zchunk;
     op_grid<R>(c, g.n0, g.n1, g.n2, grid, zchunk);
-    OpArgs<R> a{g, x, y, kxy, kz, dmask, rhs, partials, ctl, zf, zr, zchunk};
+    OpArgs<R> a{g, x, y, kxy, kz, dmask, rhs, partials, ctl, zf, zr, zchunk, smask, sslots};
 #define PLGPU_OP(MODEV)                                                                                       \
     if (mode == MODEV) {                                                                                      \
         if (aniso)                                                                                            \
@@ -325,13 +340,14 @@ static void op_launch(const LaunchCfg& c, const GridT<R>& g, const R* zf, const 
 
 void launch_operator(const LaunchCfg& c, const GridT<float>& g, const float* zf, const float* zr, const float* x,
                      float* y, const float* kxy, const float* kz, bool aniso, const uint32_t* dmask, const float* rhs,
-                     double* partials, int mode, const SolveCtl* ctl) {
-    op_launch<float>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl);
+                     double* partials, int mode, SolveCtl* ctl, const uint32_t* smask, int sslots) {
+    op_launch<float>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, smask, sslots);
 }
 void launch_operator(const LaunchCfg& c, const GridT<double>& g, const double* zf, const double* zr, const double* x,
                      double* y, const double* kxy, const double* kz, bool aniso, const uint32_t* dmask,
-                     const double* rhs, double* partials, int mode, const SolveCtl* ctl) {
-    op_launch<double>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl);
+                     const double* rhs, double* partials, int mode, SolveCtl* ctl, const uint32_t* smask,
+                     int sslots) {
+    op_launch<double>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, smask, sslots);
 }
 
 }  // namespace plgpu
