@@ -19,6 +19,12 @@ cpu_baseline  the reference's default iterative algorithm (IC + CG) restated
          on the host (oracle), timed on a bounded sample and extrapolated.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py --workload sweep [--sweep-count 256]   # batched sweep line (not the default)
+
+The sweep line solves the uneven-size sweep (layered generator, 32..96 nodes per
+axis, source power 1e15..1e17 W/m^3): every structure one at a time, then all of
+them batched (concurrent solves on separate streams) with the thread count and
+stencil grid policy the autotuner picks on a sample of 32 structures.
 """
 from __future__ import annotations
 
@@ -50,6 +56,9 @@ def parse():
     ap.add_argument("--cpu-iterations", type=int, default=10, help="CG iterations in the CPU baseline sample")
     ap.add_argument("--size", default="128,128,200")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="layered", choices=["layered", "sweep"])
+    ap.add_argument("--sweep-count", type=int, default=256)
+    ap.add_argument("--sweep-loops", type=int, default=30, help="outer-loop cap of every sweep solve")
     ap.add_argument("--operator-only", action="store_true",
                     help="only set up the case and time the operator kernel (for kernel profiling)")
     return ap.parse_args()
@@ -239,10 +248,80 @@ def run_reference(args):
 # GPU arm
 
 
+def run_sweep(args):
+    """Batched sweep: one-at-a-time vs concurrent solves of the uneven-size sweep."""
+    # more hardware work queues than the default 8, so that up to 32 solver streams
+    # do not alias onto shared queues (read when the CUDA context is created)
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+    import numpy as np
+    import torch
+
+    from plask_gb300 import _native
+    from plask_gb300 import structures as S
+    from plask_gb300 import thermal as TH
+
+    torch.cuda.set_device(0)
+    structs = S.sweep_c3(count=args.sweep_count)
+    svs = []
+    for s in structs:
+        sv = TH.solver_for_structure(s, ordering="best", algorithm=args.algorithm)
+        sv.initialize()
+        svs.append(sv)
+    fems = [sv._fem for sv in svs]
+    nodes = int(sum(np.prod(s.shape) for s in structs))
+    # one at a time (the reference's way: one solver object after another)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    iters = 0
+    unconverged = []
+    for k, f in enumerate(fems):
+        _, st = f.compute(args.sweep_loops)
+        iters += st["inner_iterations"]
+        if st["err"] > 0.05 or not st["converged"]:
+            unconverged.append(k)
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    T_seq = [f.temperature() for f in fems]
+    # autotune on a sample, then the whole sweep batched
+    sample = fems[: min(32, len(fems))]
+    threads, share, trials = _native.batch_tune(sample, loops=args.sweep_loops, max_threads=32)
+    for f in fems:
+        f.set_grid_share(share)
+        f.invalidate()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _native.batch_compute(fems, loops=args.sweep_loops, threads=threads)
+    torch.cuda.synchronize()
+    t_bat = time.perf_counter() - t0
+    # solves that did not settle within the loop cap (thermal runaway) follow different
+    # trajectories under different grids; compare the settled ones
+    dT = max(float(np.max(np.abs(fems[k].temperature() - T_seq[k])))
+             for k in range(len(fems)) if k not in unconverged)
+    out = {
+        "metric": "batched sweep solves/s (uneven layered structures, 32..96 nodes per axis)",
+        "value": len(fems) / t_bat, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+        "dtype": "f32 inner CG, f64 refinement", "data": "synthetic (seeded sweep generator, seed 3000)",
+        "config": {"workload": f"sweep of {len(fems)} layered structures, {nodes} nodes in total, "
+                               f"source power 1e15..1e16 W/m^3, at most {args.sweep_loops} outer loops per solve",
+                   "algorithm": args.algorithm},
+        "one_at_a_time": {"solves_per_s": len(fems) / t_seq, "seconds": t_seq, "cg_iterations": iters,
+                          "solves_not_within_maxerr": len(unconverged)},
+        "batched": {"seconds": t_bat, "threads": threads, "grid_share": share,
+                    "speedup_vs_one_at_a_time": t_seq / t_bat},
+        "tuner_trials_solves_per_s": [float(v) for v in trials],
+        "max_dT_batched_vs_one_at_a_time_K": dT,
+        "max_dT_note": "over the solves that settled within the loop cap",
+    }
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "sweep":
+        return run_sweep(args)
     dist = Dist()
     import numpy as np
     import torch

@@ -241,6 +241,30 @@ int plgpu_fem3d_time_operator(plgpu_fem3d* h, int precision, int reps, int flush
    "Loop n(m): max(T) = ... K, error = ... K" (therm3d.cpp:332). */
 int plgpu_fem3d_set_log_callback(plgpu_fem3d* h, void (*cb)(void* user, int level, const char* msg), void* user);
 
+/* ---------------------------------------------------------------------------------
+   Batched solves (a sweep of independent structures).  No reference counterpart: the
+   reference solves one structure per solver object, one after another. */
+
+/* Grid policy of the stencil kernel: its grid aims at 1/share of the GPU's resident
+   blocks (1, the default, fills the GPU; a larger share leaves room for the kernels of
+   other solves running at the same time). */
+int plgpu_fem3d_set_grid_share(plgpu_fem3d* h, int share);
+
+/* compute(loops) of `count` distinct handles, run concurrently from `threads` host
+   threads; every handle works on its own CUDA stream, so the kernels of different
+   solves share the SMs.  toterr, stats and status (PLGPU_* of each handle) may be NULL.
+   Returns PLGPU_OK when all succeeded, else the first failing handle's code (its message
+   is in that handle's plgpu_fem3d_last_error). */
+int plgpu_fem3d_batch_compute(plgpu_fem3d* const* handles, int count, int loops, int threads, double* toterr,
+                              plgpu_stats* stats, int* status);
+
+/* Autotuner of the batched path: for threads = 1, 2, 4, ... <= max_threads and grid share
+   1 or threads, invalidates the handles and times plgpu_fem3d_batch_compute over them;
+   every handle is left with the fastest grid share.  timings (may be NULL) receives
+   solves/s per trial, 2 per thread count (share 1, share = threads). */
+int plgpu_fem3d_batch_tune(plgpu_fem3d* const* handles, int count, int loops, int max_threads, int* best_threads,
+                           int* best_share, double* timings);
+
 #ifdef __cplusplus
 }
 #endif

@@ -119,6 +119,11 @@ SIGNATURES = {
     "plgpu_elec3d_capacitance": (C.c_int, [_h, _dp]),
     "plgpu_elec3d_stream": (C.c_void_p, [_h]),
     "plgpu_fem3d_heat_from": (C.c_int, [_h, _h]),
+    "plgpu_fem3d_set_grid_share": (C.c_int, [_h, C.c_int]),
+    "plgpu_fem3d_batch_compute": (C.c_int, [C.POINTER(_h), C.c_int, C.c_int, C.c_int, _dp, C.POINTER(Stats),
+                                            C.POINTER(C.c_int)]),
+    "plgpu_fem3d_batch_tune": (C.c_int, [C.POINTER(_h), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int), _dp]),
     "plgpu_fem3d_get_element_temperature": (C.c_int, [_h, _dp]),
 }
 
@@ -331,6 +336,10 @@ class Fem3D:
     def stream(self):
         return self._lib.plgpu_fem3d_stream(self._h)
 
+    def set_grid_share(self, share):
+        """Aim the stencil kernel's grid at 1/share of the GPU (batched solves)."""
+        self._check(self._lib.plgpu_fem3d_set_grid_share(self._h, int(share)))
+
 
 class Elec3D:
     """Owning wrapper of one ``plgpu_elec3d`` handle (include/plgpu_elec3d.h): the Shockley3D core.
@@ -464,6 +473,48 @@ class Elec3D:
 
     def stream(self):
         return self._lib.plgpu_elec3d_stream(self._h)
+
+
+def _handle_array(fems):
+    arr = (_h * len(fems))()
+    for i, f in enumerate(fems):
+        arr[i] = f._h
+    return arr
+
+
+def batch_compute(fems, loops=0, threads=8):
+    """compute(loops) of independent Fem3D handles, run concurrently (include/plgpu_fem3d.h).
+
+    Returns (toterr array, list of stats dicts, status array)."""
+    lib = load()
+    n = len(fems)
+    tot = np.zeros(n)
+    st = (Stats * max(n, 1))()
+    status = (C.c_int * max(n, 1))()
+    rc = lib.plgpu_fem3d_batch_compute(_handle_array(fems), n, int(loops), int(threads), _ptr(tot, C.c_double), st,
+                                       status)
+    for i in range(n):
+        if status[i] != OK:
+            fems[i]._check(status[i])
+    if rc != OK:
+        raise NativeError(rc, "batched compute failed")
+    return tot, [st[i].as_dict() for i in range(n)], np.array(status[:n])
+
+
+def batch_tune(fems, loops=0, max_threads=32):
+    """Autotune the batched path on these handles: (threads, grid share, solves/s per trial)."""
+    lib = load()
+    n = len(fems)
+    bt, bs = C.c_int(0), C.c_int(0)
+    ntr = 2 * (int(np.floor(np.log2(max(1, min(max_threads, n))))) + 1)
+    tim = np.zeros(ntr)
+    rc = lib.plgpu_fem3d_batch_tune(_handle_array(fems), n, int(loops), int(max_threads), C.byref(bt), C.byref(bs),
+                                    _ptr(tim, C.c_double))
+    if rc != OK:
+        for f in fems:
+            f._check(rc)
+        raise NativeError(rc, "batch tuning failed")
+    return bt.value, bs.value, tim
 
 
 def heat_from(thermal, electrical):

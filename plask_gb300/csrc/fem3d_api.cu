@@ -6,6 +6,8 @@
 // conditions are materialised once per change into compact device lists; the
 // volume operator is applied matrix-free from per-element conductivities.
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -17,6 +19,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -255,6 +258,7 @@ struct plgpu_fem3d {
         cfg.sm_count = sm_count;
         if (const char* e = std::getenv("PLGPU_NO_GRAPHS")) use_graphs = !(e[0] == '1');
         prime_launch_shapes();
+        cfg.op_share = 1;
         cfg.vec_blocks = sm_count * 4;
         if (cfg.vec_blocks > kMaxPartialBlocks) cfg.vec_blocks = kMaxPartialBlocks;
         // choose z-planes per operator block so that the block count stays within the partial slots
@@ -824,9 +828,9 @@ struct plgpu_fem3d {
                     g.key = key;
                     cudaGraph_t graph = nullptr;
                     ck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-                    const long long before = launch_count();
+                    const long long before = thread_launch_count();
                     enqueue(ch);
-                    g.kernels = launch_count() - before;
+                    g.kernels = thread_launch_count() - before;
                     count_launches(-g.kernels);  // captured, not run
                     ck(cudaStreamEndCapture(stream, &graph), "end capture");
                     ck(cudaGraphInstantiate(&g.exec, graph, 0), "graph instantiate");
@@ -1207,7 +1211,7 @@ struct plgpu_fem3d {
     double compute(int loops, plgpu_stats* st) {
         if (!initialized) initialize();
         if (bc_dirty) materialize_bc();
-        const long long launches0 = launch_count();
+        const long long launches0 = thread_launch_count();
         const int fallbacks0 = fallbacks;
         ck(cudaEventRecord(ev0, stream), "event");
         if (heat_dirty) build_static_load();
@@ -1288,7 +1292,7 @@ struct plgpu_fem3d {
             st->last_rel_residual = relres;
             st->solve_ms = solve_ms;
             st->total_ms = tot;
-            st->kernel_launches = launch_count() - launches0;
+            st->kernel_launches = thread_launch_count() - launches0;
         }
         return toterr;
     }
@@ -1735,7 +1739,7 @@ struct plgpu_elec3d : plgpu_fem3d {
         if (!initialized) initialize_e();
         if (bc_dirty) materialize_bc();
         upload_info();
-        const long long launches0 = launch_count();
+        const long long launches0 = thread_launch_count();
         const int fallbacks0 = fallbacks;
         ck(cudaEventRecord(ev0, stream), "event");
         if (heat_dirty) build_static_load();  // zero load: no sources in the electrical problem
@@ -1818,7 +1822,7 @@ struct plgpu_elec3d : plgpu_fem3d {
             st->last_rel_residual = relres;
             st->solve_ms = solve_ms;
             st->total_ms = tot;
-            st->kernel_launches = launch_count() - launches0;
+            st->kernel_launches = thread_launch_count() - launches0;
         }
         return toterr;
     }
@@ -2469,6 +2473,100 @@ int plgpu_fem3d_get_element_temperature(plgpu_fem3d* h, double* out) {
         ck(cudaMemcpyAsync(out, tmp.p, (size_t)h->NE * 8, cudaMemcpyDeviceToHost, h->stream), "D2H");
         ck(cudaStreamSynchronize(h->stream), "sync");
     });
+}
+
+
+// ---------------------------------------------------------------------------------------
+// Batched solves: independent handles computed concurrently, each from its own host
+// thread on its own stream, so that the kernels of different solves share the SMs.
+
+int plgpu_fem3d_set_grid_share(plgpu_fem3d* h, int share) {
+    return guarded(h, [&] {
+        if (share < 1) throw ArgError("grid share must be >= 1");
+        if (h->cfg.op_share != share) {
+            h->cfg.op_share = share;
+            h->invalidate_graphs();  // captured launches carry the old grid
+        }
+    });
+}
+
+int plgpu_fem3d_batch_compute(plgpu_fem3d* const* handles, int count, int loops, int threads, double* toterr,
+                              plgpu_stats* stats, int* status) {
+    if (!handles || count < 0 || loops < 0) return PLGPU_ERR_ARG;
+    for (int i = 0; i < count; ++i) {
+        if (!handles[i]) return PLGPU_ERR_ARG;
+        for (int j = 0; j < i; ++j)
+            if (handles[j] == handles[i]) return PLGPU_ERR_ARG;  // one host thread per handle
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return PLGPU_ERR_CUDA;
+    std::atomic<int> next{0};
+    std::vector<int> st((size_t)count, PLGPU_OK);
+    auto worker = [&]() {
+        cudaSetDevice(dev);
+        for (;;) {
+            const int i = next.fetch_add(1);
+            if (i >= count) break;
+            plgpu_fem3d* h = handles[i];
+            st[(size_t)i] = guarded(h, [&] {
+                const double t = h->compute(loops, stats ? &stats[i] : nullptr);
+                if (toterr) toterr[i] = t;
+            });
+        }
+    };
+    const int nt = std::max(1, std::min(threads, std::max(count, 1)));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto& th : pool) th.join();
+    int rc = PLGPU_OK;
+    for (int i = 0; i < count; ++i) {
+        if (status) status[i] = st[(size_t)i];
+        if (rc == PLGPU_OK && st[(size_t)i] != PLGPU_OK) rc = st[(size_t)i];
+    }
+    return rc;
+}
+
+int plgpu_fem3d_batch_tune(plgpu_fem3d* const* handles, int count, int loops, int max_threads, int* best_threads,
+                           int* best_share, double* timings) {
+    if (!handles || count <= 0 || max_threads < 1) return PLGPU_ERR_ARG;
+    double best = -1.0;
+    int bt = 1, bs = 1, trial = 0;
+    for (int t = 1; t <= std::min(max_threads, count); t *= 2) {
+        for (int policy = 0; policy < 2; ++policy) {
+            const int share = policy == 0 ? 1 : t;
+            if (policy == 1 && t == 1) {  // same as the whole-GPU grid
+                if (timings) timings[trial] = timings[trial - 1];
+                ++trial;
+                continue;
+            }
+            for (int i = 0; i < count; ++i) {
+                int rc = plgpu_fem3d_set_grid_share(handles[i], share);
+                if (rc == PLGPU_OK) rc = plgpu_fem3d_invalidate(handles[i]);
+                if (rc != PLGPU_OK) return rc;
+            }
+            if (cudaDeviceSynchronize() != cudaSuccess) return PLGPU_ERR_CUDA;
+            const auto t0 = std::chrono::steady_clock::now();
+            const int rc = plgpu_fem3d_batch_compute(handles, count, loops, t, nullptr, nullptr, nullptr);
+            if (rc != PLGPU_OK) return rc;
+            const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            const double rate = sec > 0 ? count / sec : 0.0;
+            if (timings) timings[trial] = rate;
+            ++trial;
+            if (rate > best) {
+                best = rate;
+                bt = t;
+                bs = share;
+            }
+        }
+    }
+    for (int i = 0; i < count; ++i) {
+        const int rc = plgpu_fem3d_set_grid_share(handles[i], bs);
+        if (rc != PLGPU_OK) return rc;
+    }
+    if (best_threads) *best_threads = bt;
+    if (best_share) *best_share = bs;
+    return PLGPU_OK;
 }
 
 }  // extern "C"

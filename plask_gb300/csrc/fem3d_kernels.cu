@@ -764,9 +764,17 @@ __global__ void k_scatter(long long n, const long long* __restrict__ idx, const 
 // Every kernel launch goes through launch_kernel so that the number of launches
 // can be reported (plgpu_stats.kernel_launches).
 static std::atomic<long long> g_launches{0};
+static thread_local long long t_launches = 0;  // a handle runs on one host thread at a time
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
-void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
-void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long thread_launch_count() { return t_launches; }
+void count_launch() {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    ++t_launches;
+}
+void count_launches(long long n) {
+    g_launches.fetch_add(n, std::memory_order_relaxed);
+    t_launches += n;
+}
 
 template <typename... KArgs, typename... Args>
 static inline void launch(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t stream, Args... args) {

@@ -38,9 +38,12 @@ struct LaunchCfg {
     int sm_count;      // streaming multiprocessors of the device
     int vec_blocks;    // grid size cap of streaming kernels (a multiple of the SM count)
     int apply_planes;  // z-planes per block of the operator kernels
+    int op_share;      // the stencil kernel's grid aims at 1/op_share of the GPU's resident
+                       // blocks (1: the whole GPU; >1 when several solves run concurrently)
 };
 
-long long launch_count();  // kernels launched by this library so far (all handles)
+long long launch_count();         // kernels launched by this library so far (all handles)
+long long thread_launch_count();  // kernels launched so far from the calling host thread
 void prime_launch_shapes();  // occupancy-derived grid sizes, queried before any graph capture
 int apply_blocks(const LaunchCfg& c, int n0, int n1, int n2);
 int vec_blocks(const LaunchCfg& c, long long N);

@@ -290,7 +290,7 @@ static void op_grid(const LaunchCfg& c, int n0, int n1, int n2, dim3& grid, int&
     const int gy = (n1 + kRows * kWarps - 1) / (kRows * kWarps);
     // z-chunks: fill whole waves of resident blocks (4 per SM in FP32, 2 in FP64),
     // each chunk at least 8 planes (one extra element layer is recomputed per chunk)
-    const int resident = c.sm_count * (sizeof(R) == 4 ? 4 : 2);
+    const int resident = max(1, c.sm_count * (sizeof(R) == 4 ? 4 : 2) / max(1, c.op_share));
     const int maxchunks = max(1, (n2 + 7) / 8);
     int chunks = 1;
     for (int waves = 1; waves <= 8; ++waves) {

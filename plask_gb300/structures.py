@@ -207,14 +207,19 @@ def layered_c1(seed=1000, n=(128, 128, 200), power=1e16, n_layers=12):
                      name=f"layered-aniso-{n[0]}x{n[1]}x{n[2]}-s{seed}")
 
 
-def sweep_c3(seed=3000, count=256, lo=32, hi=96):
+def sweep_c3(seed=3000, count=256, lo=32, hi=96, power=(1e15, 1e16)):
     """Batched sweep: ``count`` layered structures with per-axis node counts
-    uniform in [lo, hi] and source power uniform in [1e15, 1e17] W/m^3."""
+    uniform in [lo, hi] and source power uniform in ``power`` W/m^3.
+
+    The default power range stops at 1e16 W/m^3: above a few 1e16 the k(T) =
+    k300 (300/T)^p layers of this generator run away thermally (the outer loop of
+    the reference algorithm climbs past 1e4 K or the Cholesky factorisation meets a
+    non-positive pivot), so a sweep up to 1e17 would time diverging loops."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(count):
         n = tuple(int(v) for v in rng.integers(lo, hi + 1, 3))
-        pw = float(rng.uniform(1e15, 1e17))
+        pw = float(rng.uniform(*power))
         out.append(layered_c0(seed=seed + 1 + i, n=n, power=pw))
     return out
 
