@@ -259,6 +259,7 @@ struct plgpu_fem3d {
         if (const char* e = std::getenv("PLGPU_NO_GRAPHS")) use_graphs = !(e[0] == '1');
         prime_launch_shapes();
         cfg.op_share = 1;
+        cfg.op_rows = choose_op_rows(n[1]);
         cfg.vec_blocks = sm_count * 4;
         if (cfg.vec_blocks > kMaxPartialBlocks) cfg.vec_blocks = kMaxPartialBlocks;
         // choose z-planes per operator block so that the block count stays within the partial slots

@@ -40,6 +40,7 @@ struct LaunchCfg {
     int apply_planes;  // z-planes per block of the operator kernels
     int op_share;      // the stencil kernel's grid aims at 1/op_share of the GPU's resident
                        // blocks (1: the whole GPU; >1 when several solves run concurrently)
+    int op_rows;       // FP32 stencil kernel: output rows per thread (4, 5 or 6), chosen per mesh
 };
 
 long long launch_count();         // kernels launched by this library so far (all handles)
@@ -57,6 +58,8 @@ void launch_apply(const LaunchCfg& c, const GridT<float>& g, const float* x, flo
 // Optimised operator (fem3d_operator.cu).  zf[k] = dz_k / 48, zr[k] = 1 / (48 dz_k).
 // number of blocks (= partial-sum slots written in MODE_CG) of one operator launch
 int op_blocks(const LaunchCfg& c, int n0, int n1, int n2, bool fp64);
+// FP32 stencil tile (output rows per thread) for a mesh with n1 nodes along axis 1
+int choose_op_rows(int n1);
 // MODE_CG: y = A x, where nodes flagged in smask add the S x that k_surface (launched
 // just before, launch_surface_cg) left in y; the last block sums the operator's partials
 // and the sslots surface partials after them into (x, A x) and sets alpha = rz / (x, A x)

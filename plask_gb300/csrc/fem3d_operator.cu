@@ -62,8 +62,9 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
-template <typename R, int RR, bool ANISO, int MODE>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 2) k_apply_haar(const OpArgs<R> a) {
+// MINB: blocks per SM the register budget is sized for; UNR: unrolling of the z-march
+template <typename R, int RR, bool ANISO, int MODE, int MINB = (sizeof(R) == 4 ? 4 : 2), int UNR = 1>
+__global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
     if (MODE == MODE_CG && a.ctl != nullptr && a.ctl->status != SOLVE_RUNNING) return;
     const int n0 = a.g.n0, n1 = a.g.n1, n2 = a.g.n2;
     const int s2 = n0 * n1;  // N < 2^31 (checked on the host)
@@ -144,6 +145,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 2) k_apply_haar(cons
 #pragma unroll
     for (int r = 0; r < RR + 2; ++r) xlo_p[r] = __shfl_down_sync(0xffffffffu, xlo[r], 1);
 
+#pragma unroll UNR
     for (int k = kstart; k < k1; ++k) {
         // prefetch the next plane and the next element layer while this layer is computed
         load_x(k + 2, xnx);
@@ -271,26 +273,23 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 2) k_apply_haar(cons
 
 namespace {
 constexpr int kWarps = 4;
-template <typename R>
-struct Rows;
-template <>
-struct Rows<float> {
-    static constexpr int value = 6;  // fits 128 registers (4 blocks of 128 threads per SM) without spills
-};
-template <>
-struct Rows<double> {
-    static constexpr int value = 4;  // FP64 needs twice the registers per value
-};
 }  // namespace
 
-template <typename R>
-static void op_grid(const LaunchCfg& c, int n0, int n1, int n2, dim3& grid, int& zchunk) {
-    constexpr int kRows = Rows<R>::value;
+// Output rows per thread: FP32 4, 5 or 6 (LaunchCfg::op_rows, chosen per mesh by
+// choose_op_rows; all three fit 128 registers, 4 blocks of 128 threads per SM, without
+// spills in CG mode), FP64 4 (twice the registers per value).
+static int op_rows(const LaunchCfg& c, bool fp64) {
+    if (fp64) return 4;
+    return (c.op_rows == 4 || c.op_rows == 5) ? c.op_rows : 6;
+}
+
+static void op_grid(const LaunchCfg& c, int n0, int n1, int n2, bool fp64, dim3& grid, int& zchunk) {
+    const int rows = op_rows(c, fp64);
     const int gx = (n0 + 29) / 30;
-    const int gy = (n1 + kRows * kWarps - 1) / (kRows * kWarps);
+    const int gy = (n1 + rows * kWarps - 1) / (rows * kWarps);
     // z-chunks: fill whole waves of resident blocks (4 per SM in FP32, 2 in FP64),
     // each chunk at least 8 planes (one extra element layer is recomputed per chunk)
-    const int resident = max(1, c.sm_count * (sizeof(R) == 4 ? 4 : 2) / max(1, c.op_share));
+    const int resident = max(1, c.sm_count * (fp64 ? 2 : 4) / max(1, c.op_share));
     const int maxchunks = max(1, (n2 + 7) / 8);
     int chunks = 1;
     for (int waves = 1; waves <= 8; ++waves) {
@@ -304,38 +303,69 @@ static void op_grid(const LaunchCfg& c, int n0, int n1, int n2, dim3& grid, int&
     grid = dim3(gx, gy, chunks);
 }
 
+// The FP32 tile for a mesh with n1 nodes along axis 1.  A block covers 4 warps x r rows
+// of axis 1 and computes r + 1 element rows per warp: the cost per useful row is
+// (rows covered / n1) x (r + 1) / r.  Pick the smallest (then the fewest rows on a tie).
+// The choice is a fixed function of the mesh, so results do not depend on timing
+// (the tile changes the order in which (p, A p) is summed).  Measured at 128x128x200:
+// r = 4, 5, 6 take 34.2, 34.4, 37.3 us per launch; the model picks 4.
+int choose_op_rows(int n1) {
+    int best = 6;
+    double best_cost = 1e300;
+    for (int r : {4, 5, 6}) {
+        const int per_block = r * kWarps;
+        const double covered = (double)((n1 + per_block - 1) / per_block) * per_block;
+        const double cost = covered / n1 * (r + 1) / r;
+        if (cost < best_cost - 1e-12) {
+            best_cost = cost;
+            best = r;
+        }
+    }
+    return best;
+}
+
 int op_blocks(const LaunchCfg& c, int n0, int n1, int n2, bool fp64) {
     dim3 g;
     int z;
-    if (fp64)
-        op_grid<double>(c, n0, n1, n2, g, z);
-    else
-        op_grid<float>(c, n0, n1, n2, g, z);
+    op_grid(c, n0, n1, n2, fp64, g, z);
     return (int)(g.x * g.y * g.z);
 }
 
-template <typename R>
-static void op_launch(const LaunchCfg& c, const GridT<R>& g, const R* zf, const R* zr, const R* x, R* y, const R* kxy,
-                      const R* kz, bool aniso, const uint32_t* dmask, const R* rhs, double* partials, int mode,
-                      SolveCtl* ctl, const uint32_t* smask, int sslots) {
-    constexpr int kRows = Rows<R>::value;
-    dim3 grid;
-    int zchunk;
-    op_grid<R>(c, g.n0, g.n1, g.n2, grid, zchunk);
-    OpArgs<R> a{g, x, y, kxy, kz, dmask, rhs, partials, ctl, zf, zr, zchunk, smask, sslots};
-#define PLGPU_OP(MODEV)                                                                                       \
-    if (mode == MODEV) {                                                                                      \
-        if (aniso)                                                                                            \
-            launch_kernel(k_apply_haar<R, kRows, true, MODEV>, grid, dim3(32 * kWarps), c.stream, a);         \
-        else                                                                                                  \
-            launch_kernel(k_apply_haar<R, kRows, false, MODEV>, grid, dim3(32 * kWarps), c.stream, a);        \
-        return;                                                                                               \
+template <typename R, int RR>
+static void op_launch_rows(const LaunchCfg& c, dim3 grid, const OpArgs<R>& a, bool aniso, int mode) {
+#define PLGPU_OP(MODEV)                                                                                   \
+    if (mode == MODEV) {                                                                                  \
+        if (aniso)                                                                                        \
+            launch_kernel(k_apply_haar<R, RR, true, MODEV>, grid, dim3(32 * kWarps), c.stream, a);        \
+        else                                                                                              \
+            launch_kernel(k_apply_haar<R, RR, false, MODEV>, grid, dim3(32 * kWarps), c.stream, a);       \
+        return;                                                                                           \
     }
     PLGPU_OP(MODE_CG)
     PLGPU_OP(MODE_RESID)
     PLGPU_OP(MODE_RHS)
     PLGPU_OP(MODE_MULT)
 #undef PLGPU_OP
+}
+
+template <typename R>
+static void op_launch(const LaunchCfg& c, const GridT<R>& g, const R* zf, const R* zr, const R* x, R* y, const R* kxy,
+                      const R* kz, bool aniso, const uint32_t* dmask, const R* rhs, double* partials, int mode,
+                      SolveCtl* ctl, const uint32_t* smask, int sslots) {
+    constexpr bool fp64 = sizeof(R) == 8;
+    dim3 grid;
+    int zchunk;
+    op_grid(c, g.n0, g.n1, g.n2, fp64, grid, zchunk);
+    OpArgs<R> a{g, x, y, kxy, kz, dmask, rhs, partials, ctl, zf, zr, zchunk, smask, sslots};
+    if constexpr (fp64) {
+        op_launch_rows<R, 4>(c, grid, a, aniso, mode);
+    } else {
+        switch (op_rows(c, false)) {
+            case 4: op_launch_rows<R, 4>(c, grid, a, aniso, mode); break;
+            case 5: op_launch_rows<R, 5>(c, grid, a, aniso, mode); break;
+            default: op_launch_rows<R, 6>(c, grid, a, aniso, mode); break;
+        }
+    }
 }
 
 void launch_operator(const LaunchCfg& c, const GridT<float>& g, const float* zf, const float* zr, const float* x,
