@@ -1093,11 +1093,40 @@ struct plgpu_fem3d {
                              r32v.as<float>(), p32.as<float>(), q32.as<float>(), minv32.as<float>(), st, it, m);
     }
 
+    // Largest eigenvalue of D^-1 A by 30 power iterations from noise.  On anisotropic
+    // layered meshes it reaches 4.5 (thin, wide elements), so a fixed damping such as
+    // 0.6 makes "smoothing" sweeps diverge instead of smoothing.
+    double jacobi_lambda_max(unsigned long long seed) {
+        double* sc = dscal.as<double>();
+        launch_noise(cfg, N, seed, minv32.as<float>(), x32.as<float>());
+        launch_dot(cfg, N, x32.as<float>(), x32.as<float>(), dpart.as<double>(), sc + 11);
+        launch_scale_rms(cfg, N, sc + 11, x32.as<float>());
+        double lam = 0.0;
+        for (int it = 0; it < 30; ++it) {
+            amul32(x32.as<float>(), q32.as<float>());
+            ck(cudaMemsetAsync(x32.p, 0, (size_t)N * 4, stream), "memset");
+            launch_jacobi_sweep(cfg, N, -1.f, minv32.as<float>(), q32.as<float>(), x32.as<float>());  // D^-1 A x
+            launch_dot(cfg, N, x32.as<float>(), x32.as<float>(), dpart.as<double>(), sc + 11);
+            double ss = 0.0;
+            ck(cudaMemcpyAsync(&ss, sc + 11, 8, cudaMemcpyDeviceToHost, stream), "D2H");
+            ck(cudaStreamSynchronize(stream), "sync");
+            lam = std::sqrt(ss / (double)N);  // the input had unit RMS
+            if (!(lam > 0.0) || !std::isfinite(lam)) break;
+            launch_scale_rms(cfg, N, sc + 11, x32.as<float>());
+        }
+        return lam;
+    }
+
     void train(plgpu_unet* net, int steps, float lr, unsigned long long seed, int smin, int smax, int pair_kind,
                float* losses) {
         if (steps < 0 || !(lr > 0.f) || smin < 0 || smax < smin || pair_kind < 0 || pair_kind > 1)
             throw ArgError("bad training parameters");
         prepare_matrix();
+        // damped-Jacobi smoothing with omega lambda_max = 1.2 (the power iteration
+        // approaches lambda_max from below; 1.2 keeps a 40 % margin to divergence at 2)
+        const double lmax = pair_kind == 0 ? jacobi_lambda_max(seed ^ 0x5DEECE66Dull) : 1.0;
+        const float omega = (float)(lmax > 0.0 ? 1.2 / lmax : 0.6);
+        log(5, "training pairs: lambda_max(D^-1 A) ~ %g, Jacobi damping %g", lmax, (double)omega);
         DevBuf dl;
         dl.alloc((size_t)std::max(steps, 1) * 3 * 8);
         double* sc = dscal.as<double>();
@@ -1109,7 +1138,7 @@ struct plgpu_fem3d {
             if (pair_kind == 0) {
                 for (int q = 0; q < m; ++q) {
                     amul32(x32.as<float>(), q32.as<float>());
-                    launch_jacobi_sweep(cfg, N, 0.6f, minv32.as<float>(), q32.as<float>(), x32.as<float>());
+                    launch_jacobi_sweep(cfg, N, omega, minv32.as<float>(), q32.as<float>(), x32.as<float>());
                 }
             } else if (m > 0) {
                 cg_smoothed_error(m);

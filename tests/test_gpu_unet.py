@@ -75,15 +75,21 @@ def test_gradients_match_cpu_oracle():
 
 
 def test_training_lowers_the_loss_and_weights_round_trip(tmp_path):
+    """Training on FEM-generated pairs lowers the loss on fixed validation errors (the
+    per-step training loss is too noisy a judge: every step draws a new pair)."""
+    from plask_gb300.mesh import to_mesh_order
+
     s = S.layered_c1(seed=41, n=(48, 44, 40))
     sv = TH.solver_for_structure(s, ordering="201", algorithm="gpu-learned")
     sv.initialize()
     net = _native.UNet(seed=3)
-    losses = net.train(sv._fem, steps=300, lr=2e-3, seed=5, smooth=(50, 400), pairs="jacobi")
-    first, last = float(np.mean(losses[:10])), float(np.mean(losses[-30:]))
-    print("loss first", first, "last", last)
+    val = [to_mesh_order(_smooth_error(s.shape, 100 + k), "201") for k in range(3)]
+    before = float(np.mean([net.loss_grad(sv._fem, e)[0] for e in val]))
+    losses = net.train(sv._fem, steps=400, lr=2e-3, seed=5, smooth=(50, 400), pairs="jacobi")
+    after = float(np.mean([net.loss_grad(sv._fem, e)[0] for e in val]))
+    print("validation loss before", before, "after", after)
     assert np.all(np.isfinite(losses))
-    assert last < 0.95 * first
+    assert after < 0.7 * before
     path = tmp_path / "net.bin"
     net.save(path)
     other = _native.UNet(seed=99)
