@@ -242,6 +242,26 @@ int plgpu_fem3d_time_operator(plgpu_fem3d* h, int precision, int reps, int flush
 int plgpu_fem3d_set_log_callback(plgpu_fem3d* h, void (*cb)(void* user, int level, const char* msg), void* user);
 
 /* ---------------------------------------------------------------------------------
+   Time stepping: PLaSK's thermal.dynamic.Dynamic3D (solvers/thermal/dynamic/femT3d.cpp)
+   on the same handle, mesh, materials, heat and temperature conditions. */
+
+/* Heat capacity cp [J/(kg K)] and density dens [kg/m^3] per material, timestep [ns],
+   methodparam theta (0.5 Crank-Nicolson, 0 explicit, 1 implicit), lumping (only the
+   lumped heat-capacity matrix, the reference's default, is provided: 0 is rejected),
+   rebuildfreq (rebuild A and B with k(T) every that many steps, 0 never) and logfreq
+   (femT3d.cpp:26-34, 54-66). */
+int plgpu_fem3d_set_dynamic(plgpu_fem3d* h, const double* cp, const double* dens, double timestep,
+                            double methodparam, int lumping, int rebuildfreq, int logfreq);
+
+/* DynamicThermalFem3DSolver::compute(time) (femT3d.cpp:255-315): theta-method steps of
+   A T' = B T + F while t < time + timestep / 2, from the handle's temperature, with the
+   Dirichlet nodes held at their values (the scheme setMatrix prepares; the reference's
+   step loop lets them drift by (B T)[r]).
+   *elapsed receives the solver's elapsed time [ns]; stats->loops the steps of this call,
+   stats->max_t max(T).  Only temperature boundary conditions are allowed. */
+int plgpu_fem3d_compute_dynamic(plgpu_fem3d* h, double time, double* elapsed, plgpu_stats* stats);
+
+/* ---------------------------------------------------------------------------------
    Batched solves (a sweep of independent structures).  No reference counterpart: the
    reference solves one structure per solver object, one after another. */
 

@@ -66,6 +66,8 @@ SIGNATURES = {
     "plgpu_fem3d_set_solver": (C.c_int, [_h, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int]),
     "plgpu_fem3d_set_loop": (C.c_int, [_h, C.c_double, C.c_double]),
     "plgpu_fem3d_set_residual_norm": (C.c_int, [_h, C.c_int]),
+    "plgpu_fem3d_set_dynamic": (C.c_int, [_h, _dp, _dp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int]),
+    "plgpu_fem3d_compute_dynamic": (C.c_int, [_h, C.c_double, _dp, C.POINTER(Stats)]),
     "plgpu_fem3d_compute": (C.c_int, [_h, C.c_int, _dp, C.POINTER(Stats)]),
     "plgpu_fem3d_invalidate": (C.c_int, [_h]),
     "plgpu_fem3d_sizes": (C.c_int, [_h, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
@@ -260,6 +262,20 @@ class Fem3D:
 
     def set_loop(self, inittemp=300.0, maxerr=0.05):
         self._check(self._lib.plgpu_fem3d_set_loop(self._h, float(inittemp), float(maxerr)))
+
+    def set_dynamic(self, cp, dens, timestep=0.1, methodparam=0.5, lumping=True, rebuildfreq=0, logfreq=500):
+        """Heat capacities per material and the time-stepping parameters (Dynamic3D)."""
+        c, d = _f64(cp), _f64(dens)
+        self._check(self._lib.plgpu_fem3d_set_dynamic(self._h, _ptr(c, C.c_double), _ptr(d, C.c_double),
+                                                      float(timestep), float(methodparam), 1 if lumping else 0,
+                                                      int(rebuildfreq), int(logfreq)))
+
+    def compute_dynamic(self, time):
+        """Time steps over ``time`` ns; returns (elapsed time [ns], stats dict)."""
+        el = C.c_double(0.0)
+        st = Stats()
+        self._check(self._lib.plgpu_fem3d_compute_dynamic(self._h, float(time), C.byref(el), C.byref(st)))
+        return el.value, st.as_dict()
 
     def set_residual_norm(self, norm="scaled"):
         """Residual norm of the linear solves: "scaled" (Jacobi-weighted) or "plain"."""

@@ -173,6 +173,15 @@ struct plgpu_fem3d {
     bool plain_norm = true;  // PLGPU_NORM_PLAIN: residuals in the 2-norm instead of the Jacobi-scaled norm
     int chunk = 32;
 
+    // time stepping (Dynamic3D): while dyn_active every solve sees theta K + C
+    bool dyn_active = false;
+    std::vector<double> cp_tab, dens_tab;
+    double dyn_dt = 0.1, dyn_theta = 0.5;
+    bool dyn_lumping = true;
+    int dyn_rebuild = 0, dyn_logfreq = 500;
+    double elapstime = 0.0;
+    DevBuf d_cp, d_dens, cap64, cap32, kB64, kzB64, Fel, Yb, Zb, Tscratch;
+
     // learned preconditioner
     plgpu_unet* pre = nullptr;
     std::unique_ptr<UNetWork> uw;
@@ -772,7 +781,8 @@ struct plgpu_fem3d {
             ss = launch_surface_cg(cfg, s64, x, y, partials.as<double>(), op_blocks(cfg, n[0], n[1], n[2], true), c);
         launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), x, y, k64.as<double>(),
                         aniso ? kz64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(), rhs, partials.as<double>(),
-                        mode, c, ss > 0 ? smask.as<uint32_t>() : nullptr, ss);
+                        mode, c, ss > 0 ? smask.as<uint32_t>() : nullptr, ss,
+                        dyn_active ? cap64.as<double>() : nullptr);
     }
     void op32(const float* x, float* y, int mode, SolveCtl* ctl = nullptr) {
         SolveCtl* c = ctl ? ctl : d_ctl.as<SolveCtl>();
@@ -781,7 +791,8 @@ struct plgpu_fem3d {
             ss = launch_surface_cg(cfg, s32, x, y, partials.as<double>(), op_blocks(cfg, n[0], n[1], n[2], false), c);
         launch_operator(cfg, g32, zf32.as<float>(), zr32.as<float>(), x, y, k32.as<float>(),
                         aniso ? kz32.as<float>() : nullptr, aniso, dmask.as<uint32_t>(), (const float*)nullptr,
-                        partials.as<double>(), mode, c, ss > 0 ? smask.as<uint32_t>() : nullptr, ss);
+                        partials.as<double>(), mode, c, ss > 0 ? smask.as<uint32_t>() : nullptr, ss,
+                        dyn_active ? cap32.as<float>() : nullptr);
     }
     void opR(const double* x, double* y, int mode) { op64(x, y, nullptr, mode); }
     void opR(const float* x, float* y, int mode) { op32(x, y, mode); }
@@ -886,7 +897,7 @@ struct plgpu_fem3d {
                           d_ctl.as<SolveCtl>(), 4);
         const SolveCtl c = read_ctl();
         const double floor_rel = bn > 0 ? kFloorUlps * 1.1102230246251565e-16 * std::sqrt(c.red[4]) / bn : 0.0;
-        return std::max(std::min(rtol, kChangeRtol * relres0), 2.0 * floor_rel);
+        return std::max(std::min(rtol, kChangeRtol * relres0), floor_rel);
     }
 
     // FP64 Jacobi-PCG on A T = b starting from the current T.  When the recursive
@@ -1325,6 +1336,164 @@ struct plgpu_fem3d {
             st->kernel_launches = thread_launch_count() - launches0;
         }
         return toterr;
+    }
+
+    // ---------------------------------------------------------------------------------
+    // Dynamic3D (solvers/thermal/dynamic/femT3d.cpp): theta-method time stepping with the
+    // lumped heat capacity.  setMatrix builds A = theta K + C (K scaled in place, C as the
+    // operator's diagonal shift), keeps the unscaled K for B = C - (1 - theta) K and the
+    // load F with A's Dirichlet elimination (femT3d.cpp:128-252); every step solves
+    // A T' = B T + F with the Dirichlet rows of the right-hand side (and of T) set to their
+    // values, the theta method that setMatrix prepares.  (The reference's step loop,
+    // femT3d.cpp:291-300, adds (B T)[r] to those rows, B never getting the boundary
+    // conditions, and passes the vectors through buffers that alias after the first
+    // step; on meshes whose capacity per node exceeds 1 that grows without bound.)
+
+    void dyn_set_matrix() {
+        const size_t N8 = (size_t)N * 8;
+        launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab, k64.as<double>(),
+                    k32.as<float>(), aniso ? kz64.as<double>() : nullptr, aniso ? kz32.as<float>() : nullptr, aniso);
+        ck(cudaMemcpyAsync(kB64.p, k64.p, N8, cudaMemcpyDeviceToDevice, stream), "copy k");
+        if (aniso) ck(cudaMemcpyAsync(kzB64.p, kz64.p, N8, cudaMemcpyDeviceToDevice, stream), "copy kz");
+        launch_scale4(cfg, N, dyn_theta, k64.as<double>(), k32.as<float>(), aniso ? kz64.as<double>() : nullptr,
+                      aniso ? kz32.as<float>() : nullptr);
+        launch_lumped_mass(cfg, g64, d_mat.as<int>(), d_excl.as<uint8_t>(), d_cp.as<double>(), d_dens.as<double>(),
+                           dyn_dt, cap64.as<double>(), cap32.as<float>());
+        launch_diag(cfg, g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, s64, dmask.as<uint32_t>(),
+                    diag.as<double>(), minv64.as<double>(), minv32.as<float>(), cap64.as<double>());
+        // F with the elimination of A's Dirichlet columns, the row values at the Dirichlet rows
+        op64(vD.as<double>(), Fel.as<double>(), F.as<double>(), MODE_RHS);
+        launch_set_dirichlet(cfg, (int)(d_didx.bytes / sizeof(int)), d_didx.as<int>(), d_dval.as<double>(),
+                             Fel.as<double>(), Tscratch.as<double>());
+    }
+
+    double compute_dynamic(double time, plgpu_stats* st) {
+        if (cp_tab.empty()) throw StateError("set the heat capacities first (plgpu_fem3d_set_dynamic)");
+        for (int kind = 1; kind < 4; ++kind)
+            if (!bcs[kind].empty())
+                throw ArgError("the time-stepping solver takes temperature boundary conditions only");
+        if (!initialized) {
+            initialize();
+            elapstime = 0.0;  // onInitialize, femT3d.cpp:77-81
+        }
+        if (bc_dirty) materialize_bc();
+        const size_t N8 = (size_t)N * 8;
+        kB64.alloc(N8);
+        if (aniso) kzB64.alloc(N8);
+        cap64.alloc(N8);
+        cap32.alloc((size_t)N * 4);
+        Fel.alloc(N8);
+        Yb.alloc(N8);
+        Tscratch.alloc(N8);
+        if (Zb.bytes != N8) {
+            Zb.alloc(N8);
+            ck(cudaMemsetAsync(Zb.p, 0, N8, stream), "memset");
+        }
+        upload(d_cp, cp_tab, stream);
+        upload(d_dens, dens_tab, stream);
+        const long long launches0 = thread_launch_count();
+        const int fallbacks0 = fallbacks;
+        ck(cudaEventRecord(ev0, stream), "event");
+        if (heat_dirty) build_static_load();
+        invalidate_graphs();  // captured solves carry the operator without the capacity shift
+        // The capacity terms C T dominate ||b|| while the smallest elements carry the
+        // smallest rows of A: the time steps measure residuals in the Jacobi-scaled norm.
+        struct Guard {
+            plgpu_fem3d* h;
+            bool plain;
+            ~Guard() {
+                h->dyn_active = false;
+                h->plain_norm = plain;
+                h->invalidate_graphs();
+            }
+        } guard{this, plain_norm};
+        dyn_active = true;
+        plain_norm = false;
+        log(3, "Running thermal calculations");
+        dyn_set_matrix();
+        const bool mixed = algorithm == PLGPU_ALGO_ITERATIVE || algorithm == PLGPU_ALGO_GPU_MIXED ||
+                           algorithm == PLGPU_ALGO_GPU_LEARNED;
+        const int nrows = (int)(d_didx.bytes / sizeof(int));
+        long long r = dyn_rebuild, l = dyn_logfreq;
+        int total_iters = 0, total_ref = 0, steps = 0;
+        double relres = 0.0, maxT = 0.0;
+        float solve_ms = 0.f;
+        time += dyn_dt / 2.0;
+        for (double t = 0.0; t < time; t += dyn_dt) {
+            if (dyn_rebuild && r == 0) {
+                dyn_set_matrix();
+                r = dyn_rebuild;
+            }
+            // X = B T + F = C T - (1 - theta) K T + F, then Dirichlet rows of T take X
+            launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), T.as<double>(), Yb.as<double>(),
+                            kB64.as<double>(), aniso ? kzB64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(),
+                            Zb.as<double>(), partials.as<double>(), MODE_RHS, d_ctl.as<SolveCtl>());
+            launch_dyn_rhs(cfg, N, cap64.as<double>(), T.as<double>(), Yb.as<double>(), 1.0 - dyn_theta,
+                           Fel.as<double>(), b.as<double>());
+            launch_set_dirichlet(cfg, nrows, d_didx.as<int>(), d_dval.as<double>(), b.as<double>(), T.as<double>());
+            ck(cudaEventRecord(ev2, stream), "event");
+            int status = 0, iters = 0, refs = 0;
+            if (mixed)
+                solve_mixed(status, iters, refs, relres);
+            else
+                solve_fp64(status, iters, relres);
+            ck(cudaEventRecord(ev3, stream), "event");
+            total_iters += iters;
+            total_ref += refs;
+            if (status == SOLVE_NONFINITE) throw SolveError(PLGPU_ERR_NONFINITE, "non-finite value in the linear solve");
+            if (status == SOLVE_BREAKDOWN)
+                throw SolveError(PLGPU_ERR_NOT_SPD, "system matrix is not positive definite (CG breakdown)");
+            converged = status == SOLVE_CONVERGED;
+            if (!converged) {
+                if (noconv == PLGPU_NOCONV_ERROR)
+                    throw SolveError(PLGPU_ERR_NOCONV, "failed to converge in " + std::to_string(iters) +
+                                                           " iterations (relative residual " +
+                                                           std::to_string(relres) + ")");
+                log(noconv == PLGPU_NOCONV_WARNING ? 2 : 5, "Failed to converge in %d iterations (error %g)", iters,
+                    relres);
+            }
+            float ms = 0.f;
+            ck(cudaEventSynchronize(ev3), "sync");
+            ck(cudaEventElapsedTime(&ms, ev2, ev3), "elapsed");
+            solve_ms += ms;
+            if (dyn_logfreq && l == 0) {
+                launch_err(cfg, N, T.as<double>(), T.as<double>(),
+                           any_inactive ? inactive_mask.as<uint32_t>() : nullptr, partials.as<double>(),
+                           d_ctl.as<SolveCtl>());
+                maxT = read_ctl().red[1];
+                log(4, "Time %.2f ns: max(T) = %.3f K", elapstime, maxT);
+                l = dyn_logfreq;
+            }
+            --r;
+            --l;
+            elapstime += dyn_dt;
+            ++steps;
+        }
+        elapstime -= dyn_dt;
+        launch_err(cfg, N, T.as<double>(), T.as<double>(), any_inactive ? inactive_mask.as<uint32_t>() : nullptr,
+                   partials.as<double>(), d_ctl.as<SolveCtl>());
+        maxT = read_ctl().red[1];
+        ck(cudaEventRecord(ev1, stream), "event");
+        ck(cudaEventSynchronize(ev1), "sync");
+        float tot = 0.f;
+        ck(cudaEventElapsedTime(&tot, ev0, ev1), "elapsed");
+        ++loopno;
+        if (st) {
+            st->loops = steps;
+            st->total_loops = loopno;
+            st->inner_iterations = total_iters;
+            st->refinements = total_ref;
+            st->converged = converged ? 1 : 0;
+            st->fallbacks = fallbacks - fallbacks0;
+            st->err = 0.0;
+            st->toterr = 0.0;
+            st->max_t = maxT;
+            st->last_rel_residual = relres;
+            st->solve_ms = solve_ms;
+            st->total_ms = tot;
+            st->kernel_launches = thread_launch_count() - launches0;
+        }
+        return 0.0;  // femT3d.cpp:314
     }
 
     // ---------------------------------------------------------------------------------
@@ -2597,6 +2766,40 @@ int plgpu_fem3d_batch_tune(plgpu_fem3d* const* handles, int count, int loops, in
     if (best_threads) *best_threads = bt;
     if (best_share) *best_share = bs;
     return PLGPU_OK;
+}
+
+
+// ---------------------------------------------------------------------------------------
+// Time stepping
+
+int plgpu_fem3d_set_dynamic(plgpu_fem3d* h, const double* cp, const double* dens, double timestep,
+                            double methodparam, int lumping, int rebuildfreq, int logfreq) {
+    return guarded(h, [&] {
+        if (h->n_mat == 0) throw StateError("set the material table first");
+        if (!cp || !dens) throw ArgError("cp and dens are required");
+        if (!(timestep > 0.0) || !std::isfinite(timestep)) throw ArgError("timestep must be positive");
+        if (!(methodparam >= 0.0 && methodparam <= 1.0)) throw ArgError("methodparam must be in [0, 1]");
+        if (!lumping) throw ArgError("only the lumped heat-capacity matrix is provided (lumping = true)");
+        if (rebuildfreq < 0 || logfreq < 0) throw ArgError("frequencies must be >= 0");
+        for (int m = 0; m < h->n_mat; ++m)
+            if (!std::isfinite(cp[m]) || !std::isfinite(dens[m]) || cp[m] < 0 || dens[m] < 0)
+                throw ArgError("cp and dens must be finite and >= 0");
+        h->cp_tab.assign(cp, cp + h->n_mat);
+        h->dens_tab.assign(dens, dens + h->n_mat);
+        h->dyn_dt = timestep;
+        h->dyn_theta = methodparam;
+        h->dyn_lumping = lumping != 0;
+        h->dyn_rebuild = rebuildfreq;
+        h->dyn_logfreq = logfreq;
+    });
+}
+
+int plgpu_fem3d_compute_dynamic(plgpu_fem3d* h, double time, double* elapsed, plgpu_stats* stats) {
+    return guarded(h, [&] {
+        if (!std::isfinite(time) || time < 0.0) throw ArgError("time must be finite and >= 0");
+        h->compute_dynamic(time, stats);
+        if (elapsed) *elapsed = h->elapstime;
+    });
 }
 
 }  // extern "C"

@@ -964,13 +964,19 @@ void launch_coef(const LaunchCfg& c, int n0, int n1, int n2, const double* T, co
     else
         launch(k_coef<false>, vec_blocks(c, N), 256, c.stream, n0, n1, n2, T, mat, th, tab, k64, k32, kz64, kz32);
 }
+__global__ void __launch_bounds__(256) k_add_vec(long long N, double* __restrict__ d, const double* __restrict__ s) {
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x)
+        d[n] += s[n];
+}
 void launch_diag(const LaunchCfg& c, const GridT<double>& g, const double* kxy, const double* kz, bool aniso,
-                 const SurfaceT<double>& s, const uint32_t* dmask, double* diag, double* minv64, float* minv32) {
+                 const SurfaceT<double>& s, const uint32_t* dmask, double* diag, double* minv64, float* minv32,
+                 const double* shift) {
     if (aniso)
         launch(k_diag<true>, vec_blocks(c, g.N), 256, c.stream, g, kxy, kz, diag);
     else
         launch(k_diag<false>, vec_blocks(c, g.N), 256, c.stream, g, kxy, kz, diag);
     if (s.nrows > 0) launch(k_surface_diag, grid_for(s.nrows, 256, 1024), 256, c.stream, s, diag);
+    if (shift) launch(k_add_vec, vec_blocks(c, g.N), 256, c.stream, g.N, diag, shift);
     launch(k_invert_diag, vec_blocks(c, g.N), 256, c.stream, g.N, diag, dmask, minv64, minv32);
 }
 void launch_heat_load(const LaunchCfg& c, const GridT<double>& g, const double* q, const int* mat, const MatTable& tab,

@@ -66,11 +66,12 @@ int choose_op_rows(int n1);
 // (or the breakdown / non-finite status).
 void launch_operator(const LaunchCfg& c, const GridT<float>& g, const float* zf, const float* zr, const float* x,
                      float* y, const float* kxy, const float* kz, bool aniso, const uint32_t* dmask, const float* rhs,
-                     double* partials, int mode, SolveCtl* ctl, const uint32_t* smask = nullptr, int sslots = 0);
+                     double* partials, int mode, SolveCtl* ctl, const uint32_t* smask = nullptr, int sslots = 0,
+                     const float* dshift = nullptr);
 void launch_operator(const LaunchCfg& c, const GridT<double>& g, const double* zf, const double* zr, const double* x,
                      double* y, const double* kxy, const double* kz, bool aniso, const uint32_t* dmask,
                      const double* rhs, double* partials, int mode, SolveCtl* ctl, const uint32_t* smask = nullptr,
-                     int sslots = 0);
+                     int sslots = 0, const double* dshift = nullptr);
 // CG step, first half: y[row] = S x on the surface rows and block partials of (x, S x) in
 // slots slot0..slot0 + surface_cg_blocks - 1; returns the number of slots used.
 int launch_surface_cg(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, double* partials,
@@ -111,8 +112,21 @@ void launch_add_correction(const LaunchCfg& c, long long N, double* T, const flo
 void launch_thickness(const LaunchCfg& c, int n0, int n1, int n2, const int* mat, const double* z, double* th);
 void launch_coef(const LaunchCfg& c, int n0, int n1, int n2, const double* T, const int* mat, const double* th,
                  const MatTable& tab, double* k64, float* k32, double* kz64, float* kz32, bool aniso);
+// Jacobi diagonal of the operator (plus `shift` per node when given) and its inverse
 void launch_diag(const LaunchCfg& c, const GridT<double>& g, const double* kxy, const double* kz, bool aniso,
-                 const SurfaceT<double>& s, const uint32_t* dmask, double* diag, double* minv64, float* minv32);
+                 const SurfaceT<double>& s, const uint32_t* dmask, double* diag, double* minv64, float* minv32,
+                 const double* shift = nullptr);
+// ---- time stepping (dyn3d_kernels.cu)
+// lumped heat capacity per node: sum over the node's active elements of
+// cp dens 0.125e-9 dx dy dz / timestep (FP64 and FP32 copies)
+void launch_lumped_mass(const LaunchCfg& c, const GridT<double>& g, const int* mat, const uint8_t* excl,
+                        const double* cp, const double* dens, double timestep, double* c64, float* c32);
+// v *= s for the four coefficient arrays (any may be nullptr)
+void launch_scale4(const LaunchCfg& c, long long N, double s, double* a64, float* a32, double* b64, float* b32);
+// X = cap T + w Y + F  (Y = -K T)
+void launch_dyn_rhs(const LaunchCfg& c, long long N, const double* cap, const double* T, const double* Y, double w,
+                    const double* F, double* X);
+
 void launch_heat_load(const LaunchCfg& c, const GridT<double>& g, const double* q, const int* mat, const MatTable& tab,
                       double* F);
 void launch_scatter_add(const LaunchCfg& c, int n, const int* idx, const double* val, double* F);

@@ -50,6 +50,9 @@ struct OpArgs {
     // written by k_surface, whose block partials of (x, S x) follow the operator's
     const uint32_t* smask;
     int sslots;
+    // diagonal added to the operator, y += dshift x (the lumped heat capacity of the
+    // time-stepping solver), or nullptr
+    const R* dshift;
 };
 
 __device__ __forceinline__ bool dir_bit(const uint32_t* __restrict__ m, long long n) {
@@ -212,6 +215,7 @@ __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
             for (int r = 1; r <= RR; ++r) {
                 if (out_lane && noff[r] >= 0) {
                     const long long n = pb + noff[r];
+                    if (a.dshift != nullptr) acc[r - 1] += a.dshift[n] * xlo[r];
                     R out;
                     if (MODE == MODE_CG) {
                         // Dirichlet rows: x is zero there and M^-1 = 0 keeps the CG residual zero
@@ -351,12 +355,12 @@ static void op_launch_rows(const LaunchCfg& c, dim3 grid, const OpArgs<R>& a, bo
 template <typename R>
 static void op_launch(const LaunchCfg& c, const GridT<R>& g, const R* zf, const R* zr, const R* x, R* y, const R* kxy,
                       const R* kz, bool aniso, const uint32_t* dmask, const R* rhs, double* partials, int mode,
-                      SolveCtl* ctl, const uint32_t* smask, int sslots) {
+                      SolveCtl* ctl, const uint32_t* smask, int sslots, const R* dshift) {
     constexpr bool fp64 = sizeof(R) == 8;
     dim3 grid;
     int zchunk;
     op_grid(c, g.n0, g.n1, g.n2, fp64, grid, zchunk);
-    OpArgs<R> a{g, x, y, kxy, kz, dmask, rhs, partials, ctl, zf, zr, zchunk, smask, sslots};
+    OpArgs<R> a{g, x, y, kxy, kz, dmask, rhs, partials, ctl, zf, zr, zchunk, smask, sslots, dshift};
     if constexpr (fp64) {
         op_launch_rows<R, 4>(c, grid, a, aniso, mode);
     } else {
@@ -370,14 +374,15 @@ static void op_launch(const LaunchCfg& c, const GridT<R>& g, const R* zf, const 
 
 void launch_operator(const LaunchCfg& c, const GridT<float>& g, const float* zf, const float* zr, const float* x,
                      float* y, const float* kxy, const float* kz, bool aniso, const uint32_t* dmask, const float* rhs,
-                     double* partials, int mode, SolveCtl* ctl, const uint32_t* smask, int sslots) {
-    op_launch<float>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, smask, sslots);
+                     double* partials, int mode, SolveCtl* ctl, const uint32_t* smask, int sslots,
+                     const float* dshift) {
+    op_launch<float>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, smask, sslots, dshift);
 }
 void launch_operator(const LaunchCfg& c, const GridT<double>& g, const double* zf, const double* zr, const double* x,
                      double* y, const double* kxy, const double* kz, bool aniso, const uint32_t* dmask,
                      const double* rhs, double* partials, int mode, SolveCtl* ctl, const uint32_t* smask,
-                     int sslots) {
-    op_launch<double>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, smask, sslots);
+                     int sslots, const double* dshift) {
+    op_launch<double>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, smask, sslots, dshift);
 }
 
 }  // namespace plgpu

@@ -37,6 +37,8 @@ class MaterialTable:
     kz_ratio: np.ndarray | None = None
     hexp: np.ndarray | None = None
     empty: np.ndarray | None = None
+    cp: np.ndarray | None = None     # heat capacity J/(kg K), for Dynamic3D
+    dens: np.ndarray | None = None   # density kg/m^3, for Dynamic3D
 
     def __post_init__(self):
         self.k300 = np.asarray(self.k300, np.float64)
@@ -467,6 +469,59 @@ class Static3D:
         th = self._fem.thickness()
         eidx = self._mesh.element_index_array().ravel()
         return th[eidx].reshape(self._mesh.element_shape)
+
+
+class Dynamic3D(Static3D):
+    """Finite element time-stepping thermal solver for 3D geometry, on the GPU.
+
+    A drop-in for PLaSK's ``thermal.dynamic.Dynamic3D`` (femT3d.cpp,
+    python/dynamic.cpp:34-45): ``compute(time)`` advances ``time`` ns with the theta
+    method; attributes ``inittemp`` (300 K), ``timestep`` (0.1 ns), ``methodparam``
+    (0.5: Crank-Nicolson), ``lumping`` (True; the consistent heat-capacity matrix is not
+    provided), ``rebuildfreq`` (0), ``logfreq`` (500), ``time`` / ``elapsed_time`` (read only,
+    python/dynamic.cpp:46-48),
+    ``algorithm`` ("iterative"), ``temperature_boundary``, ``inHeat`` and the providers
+    of Static3D.  The material table must carry ``cp`` and ``dens``.
+    """
+
+    def __init__(self, name=""):
+        super().__init__(name)
+        self.timestep = 0.1
+        self.methodparam = 0.5
+        self.lumping = True
+        self.rebuildfreq = 0
+        self.logfreq = 500
+        self._elapstime = 0.0
+        # the time-stepping solver has temperature conditions only (femT3d.hpp:54)
+        del self.heatflux_boundary, self.convection_boundary, self.radiation_boundary
+        self.heatflux_boundary = self.convection_boundary = self.radiation_boundary = ()
+
+    @property
+    def id(self):
+        return f"{self.name}:thermal.Dynamic3D" if self.name else "thermal.Dynamic3D"
+
+    @property
+    def time(self):
+        """Time of calculations performed so far since the last invalidation [ns]."""
+        return self._elapstime
+
+    elapsed_time = time
+
+    def compute(self, time):
+        """Run thermal calculations for ``time`` ns (femT3d.cpp:255-315)."""
+        self.initialize()
+        mt = self._geometry.materials
+        if mt.cp is None or mt.dens is None:
+            raise BadInput(-1, f"{self.id}: the material table has no cp / dens")
+        self._fem.set_dynamic(mt.cp, mt.dens, self.timestep, self.methodparam, self.lumping, self.rebuildfreq,
+                              self.logfreq)
+        self.loop_log = []
+        el, st = self._fem.compute_dynamic(time)
+        self._elapstime = el
+        self.stats = st
+        self.iterative.converged = bool(st["converged"])
+        self.iterative.iters = st["inner_iterations"]
+        return 0.0
 
 
 def _points(dst):

@@ -218,3 +218,21 @@ def test_heat_flux_of_slab_matches_power():
     total = np.sum(q[:, 0, 0] * np.diff(z) * 1e-6)
     assert np.allclose(flux[0, :, :, 2], -total, rtol=1e-9)
     assert np.allclose(flux[..., :2], 0.0, atol=1e-6 * total)
+
+
+def test_dynamic_oracle_reaches_the_static_state():
+    """Implicit Euler with a timestep far beyond the diffusion time, rebuilding k(T) every
+    step, is a Picard iteration of the static problem: it must land on the static
+    oracle's temperature (which itself stops at maxerr 0.05 K)."""
+    from oracle import dynamic3d as D
+    from plask_gb300 import structures as S
+
+    s = S.layered_c0(seed=21, n=(9, 8, 12))
+    p = O.from_structure(s, order="012", empty_elements="include")
+    Ts, _, _ = O.compute(p, loops=0)
+    cp = np.full(s.k300.size, 500.0)
+    dens = np.full(s.k300.size, 5000.0)
+    Td, elaps, steps = D.compute(p, 10e9, cp, dens, timestep=1e9, theta=1.0, rebuildfreq=1, method="cholesky")
+    node_id, _ = O.masked_numbering(p)
+    assert steps == 11 and abs(elaps - 10e9) < 1e-3
+    assert np.max(np.abs(O.to_full(p, node_id, Td) - Ts)) < 0.1
