@@ -1,4 +1,5 @@
-"""ctypes binding of the native library ``libplgpu_fem3d.so`` (include/plgpu_fem3d.h).
+"""ctypes binding of the native library ``libplgpu_fem3d.so`` (include/plgpu_fem3d.h,
+plgpu_fem2d.h, plgpu_elec3d.h, plgpu_unet.h).
 
 The library is the only compute path: importing this module fails loudly when
 it is missing or cannot be loaded, and every call checks the returned status
@@ -22,6 +23,8 @@ ALGORITHMS = {"cholesky": 0, "gauss": 1, "iterative": 2, "gpu-pcg": 3, "gpu-mixe
 NOCONV = {"error": 0, "warning": 1, "continue": 2}
 EMPTY = {"default": 0, "exclude": 1, "excluded": 1, "include": 2, "included": 2}
 NORMS = {"scaled": 0, "plain": 1}
+ORDERS2D = {"10": 0, "01": 1}
+GEOMETRY2D = {"cartesian": 1, "cylindrical": 2}
 
 
 class Stats(C.Structure):
@@ -127,6 +130,8 @@ SIGNATURES = {
     "plgpu_fem3d_batch_tune": (C.c_int, [C.POINTER(_h), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
                                          C.POINTER(C.c_int), _dp]),
     "plgpu_fem3d_get_element_temperature": (C.c_int, [_h, _dp]),
+    # include/plgpu_fem2d.h
+    "plgpu_fem2d_create": (C.c_int, [_dp, C.c_int, _dp, C.c_int, C.c_int, C.c_int, C.POINTER(_h)]),
 }
 
 _lib = None
@@ -355,6 +360,36 @@ class Fem3D:
     def set_grid_share(self, share):
         """Aim the stencil kernel's grid at 1/share of the GPU (batched solves)."""
         self._check(self._lib.plgpu_fem3d_set_grid_share(self._h, int(share)))
+
+
+class Fem2D(Fem3D):
+    """Owning wrapper of a planar ``plgpu_fem3d`` handle made by ``plgpu_fem2d_create``
+    (include/plgpu_fem2d.h): Static2D (geometry "cartesian") or StaticCyl ("cylindrical").
+
+    Arrays exchanged with it use the 2D mesh iteration order ("10": axis 0 fastest,
+    "01": axis 1 fastest); heat fluxes have 2 components per element."""
+
+    def __init__(self, axes, ordering="01", geometry="cartesian"):
+        lib = load()
+        self._lib = lib
+        ax = [_f64(a) for a in axes]
+        h = _h()
+        rc = lib.plgpu_fem2d_create(_ptr(ax[0], C.c_double), len(ax[0]), _ptr(ax[1], C.c_double), len(ax[1]),
+                                    ORDERS2D[ordering], GEOMETRY2D[geometry], C.byref(h))
+        if rc != OK:
+            msg = lib.plgpu_fem3d_last_error(None)
+            raise (BadInput if rc == ERR_ARG else NativeError)(rc, (msg or b"").decode())
+        self._h = h
+        self.shape = (len(ax[1]), len(ax[0]))
+        self.ordering = ordering
+        self.geometry = geometry
+        self._log_cb = None
+
+    def heat_flux(self):
+        _, ne = self.sizes()
+        out = np.empty((ne, 2))
+        self._check(self._lib.plgpu_fem3d_get_heat_flux(self._h, _ptr(out, C.c_double)))
+        return out
 
 
 class Elec3D:

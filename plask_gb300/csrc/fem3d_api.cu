@@ -24,9 +24,11 @@
 #include <vector>
 
 #include "../../include/plgpu_elec3d.h"
+#include "../../include/plgpu_fem2d.h"
 #include "../../include/plgpu_fem3d.h"
 #include "../../include/plgpu_unet.h"
 #include "elec3d_kernels.h"
+#include "fem2d_kernels.h"
 #include "fem3d_device.cuh"
 #include "fem3d_kernels.h"
 #include "unet.h"
@@ -105,6 +107,10 @@ struct plgpu_fem3d {
     long long ns[3] = {0, 0, 0};  // mesh-order node strides of axes 0/1/2
     long long es[3] = {0, 0, 0};  // mesh-order element strides
     std::vector<double> ax[3];
+    // 0: 3D; PLGPU_GEOMETRY_CARTESIAN / _CYLINDRICAL: a 2D mesh (axes 0 and 1) stored as
+    // one node plane, n[2] = 1, whose elements are the quads of axes 0 and 1
+    int planar = 0;
+    DevBuf rmid64, rmid32;  // cylindrical: midpoint radius of every element column
     cudaStream_t stream = nullptr;
     LaunchCfg cfg{};
     int sm_count = 0;
@@ -233,10 +239,20 @@ struct plgpu_fem3d {
     // ---------------------------------------------------------------------------------
     // mesh
 
-    void setup_mesh(const double* a0, int n0, const double* a1, int n1, const double* a2, int n2, int ord) {
+    // element extent along axis d (a planar mesh has one layer of quads along axis 2)
+    int me(int d) const { return (planar && d == 2) ? 1 : n[d] - 1; }
+
+    void setup_mesh(const double* a0, int n0, const double* a1, int n1, const double* a2, int n2, int ord,
+                    int plan = 0) {
         const double* a[3] = {a0, a1, a2};
         const int nn[3] = {n0, n1, n2};
+        planar = plan;
         for (int d = 0; d < 3; ++d) {
+            if (planar && d == 2) {
+                ax[2].assign(1, 0.0);
+                n[2] = 1;
+                continue;
+            }
             if (!a[d] || nn[d] < 2) throw ArgError("every axis needs at least 2 nodes");
             ax[d].assign(a[d], a[d] + nn[d]);
             for (int i = 1; i < nn[d]; ++i)
@@ -253,10 +269,10 @@ struct plgpu_fem3d {
         ns[medium] = n[minor];
         ns[major] = (long long)n[minor] * n[medium];
         es[minor] = 1;
-        es[medium] = n[minor] - 1;
-        es[major] = (long long)(n[minor] - 1) * (n[medium] - 1);
+        es[medium] = me(minor);
+        es[major] = (long long)me(minor) * me(medium);
         N = (long long)n[0] * n[1] * n[2];
-        NE = (long long)(n[0] - 1) * (n[1] - 1) * (n[2] - 1);
+        NE = (long long)me(0) * me(1) * me(2);
         if (N > (1LL << 31) - 1) throw ArgError("meshes above 2^31 nodes are not supported");
 
         ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -290,7 +306,18 @@ struct plgpu_fem3d {
             upload(h32[d], hf, stream);
             upload(r32[d], rf, stream);
         }
-        upload(z64, ax[2], stream);
+        upload(z64, ax[planar ? 1 : 2], stream);  // coordinates of the vertical axis
+        if (planar == PLGPU_GEOMETRY_CYLINDRICAL) {
+            if (ax[0][0] < 0.0) throw ArgError("the radial axis of a cylindrical mesh must start at r >= 0");
+            std::vector<double> rm((size_t)n[0], 0.0);
+            std::vector<float> rmf((size_t)n[0], 0.f);
+            for (int i = 0; i < n[0] - 1; ++i) {
+                rm[i] = 0.5 * (ax[0][i] + ax[0][i + 1]);  // elem.getMidpoint().rad_r(), therm2d.cpp:333
+                rmf[i] = (float)rm[i];
+            }
+            upload(rmid64, rm, stream);
+            upload(rmid32, rmf, stream);
+        }
         {
             std::vector<double> zf(n[2] - 1), zr(n[2] - 1);
             std::vector<float> zff(n[2] - 1), zrf(n[2] - 1);
@@ -401,13 +428,13 @@ struct plgpu_fem3d {
         DevBuf tmp;
         tmp.alloc((size_t)NE * 8);
         ck(cudaMemcpyAsync(tmp.p, mat, (size_t)NE * 4, cudaMemcpyHostToDevice, stream), "H2D mat");
-        launch_from_mesh_order_i32(cfg, n[0], n[1], n[2], n[0] - 1, n[1] - 1, n[2] - 1, es[0], es[1], es[2],
+        launch_from_mesh_order_i32(cfg, n[0], n[1], n[2], me(0), me(1), me(2), es[0], es[1], es[2],
                                    tmp.as<int>(), d_mat.as<int>(), 0);
         set_heat_impl(heat, tmp);
         if (leaf) {
             d_hleaf.alloc((size_t)N * 8);
             ck(cudaMemcpyAsync(tmp.p, leaf, (size_t)NE * 8, cudaMemcpyHostToDevice, stream), "H2D leaf");
-            launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], n[0] - 1, n[1] - 1, n[2] - 1, es[0], es[1], es[2],
+            launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], me(0), me(1), me(2), es[0], es[1], es[2],
                                        tmp.as<double>(), d_hleaf.as<double>(), 0.0);
             have_leaf = true;
         } else {
@@ -421,7 +448,7 @@ struct plgpu_fem3d {
     void set_heat_impl(const double* heat, DevBuf& tmp) {
         if (heat) {
             ck(cudaMemcpyAsync(tmp.p, heat, (size_t)NE * 8, cudaMemcpyHostToDevice, stream), "H2D heat");
-            launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], n[0] - 1, n[1] - 1, n[2] - 1, es[0], es[1], es[2],
+            launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], me(0), me(1), me(2), es[0], es[1], es[2],
                                        tmp.as<double>(), d_heat.as<double>(), 0.0);
         } else {
             ck(cudaMemsetAsync(d_heat.p, 0, (size_t)N * 8, stream), "memset");
@@ -473,12 +500,13 @@ struct plgpu_fem3d {
         std::vector<uint32_t> inact((size_t)(N + 31) / 32 + 1, 0u);
         if (any_ex) {
             std::vector<uint8_t> used((size_t)N, 0);
-            for (int k = 0; k < n[2] - 1; ++k)
+            const int corners = planar ? 4 : 8;
+            for (int k = 0; k < me(2); ++k)
                 for (int j = 0; j < n[1] - 1; ++j)
                     for (int i = 0; i < n[0] - 1; ++i) {
                         const long long em = i * es[0] + j * es[1] + (long long)k * es[2];
                         if (ex[host_mat[em]]) continue;
-                        for (int c = 0; c < 8; ++c) {
+                        for (int c = 0; c < corners; ++c) {
                             const long long cn = (i + (c & 1)) + (long long)n[0] * ((j + ((c >> 1) & 1)) +
                                                                                    (long long)n[1] * (k + (c >> 2)));
                             used[cn] = 1;
@@ -509,7 +537,10 @@ struct plgpu_fem3d {
         upload(inactive_mask, inact, stream);
 
         // thickness of layer runs
-        launch_thickness(cfg, n[0], n[1], n[2], d_mat.as<int>(), z64.as<double>(), d_th.as<double>());
+        if (planar)
+            launch_thickness2d(cfg, n[0], n[1], d_mat.as<int>(), z64.as<double>(), d_th.as<double>());
+        else
+            launch_thickness(cfg, n[0], n[1], n[2], d_mat.as<int>(), z64.as<double>(), d_th.as<double>());
         // temperatures = inittemp
         launch_fill(cfg, N, T.as<double>(), inittemp);
         ck(cudaStreamSynchronize(stream), "sync");
@@ -604,87 +635,176 @@ struct plgpu_fem3d {
         };
         std::vector<RadTerm> rad;
 
-        // global nodes 0..7 in the solver's numbering (radiation quirk, therm3d.cpp:265)
-        long long glob[8];
-        for (int w = 0; w < 8; ++w) {
-            long long cn = -1;
-            if (masked) {
-                if (w < (long long)h_active.size()) cn = h_active[w];
-            } else if (w < N) {
-                cn = canon_of_mesh(w);
-            }
-            glob[w] = cn;
-        }
-
-        std::vector<long long> cand;
-        {
-            std::vector<long long> nodes;
+        if (planar) {
+            // edge terms of the 2D solvers (setBoundaries, therm2d.cpp:139-172, and its uses
+            // at :230-266 Cartesian, :356-407 cylindrical)
+            std::vector<long long> cand;
             for (auto* m : {&mhf, &mcv, &mrd})
-                for (auto& kv : *m) nodes.push_back(kv.first);
-            std::vector<long long> els;
-            for (long long cn : nodes) {
-                const int i = (int)(cn % n[0]), j = (int)((cn / n[0]) % n[1]), k = (int)(cn / ((long long)n[0] * n[1]));
-                for (int c = 0; c < 8; ++c) {
-                    const int e0 = i - (c & 1), e1 = j - ((c >> 1) & 1), e2 = k - (c >> 2);
-                    if (e0 < 0 || e1 < 0 || e2 < 0 || e0 >= n[0] - 1 || e1 >= n[1] - 1 || e2 >= n[2] - 1) continue;
-                    els.push_back(e0 + (long long)n[0] * (e1 + (long long)n[1] * e2));
+                for (auto& kv : *m) {
+                    const int i = (int)(kv.first % n[0]), j = (int)(kv.first / n[0]);
+                    for (int c = 0; c < 4; ++c) {
+                        const int e0 = i - (c & 1), e1 = j - (c >> 1);
+                        if (e0 < 0 || e1 < 0 || e0 >= n[0] - 1 || e1 >= n[1] - 1) continue;
+                        cand.push_back(e0 + (long long)n[0] * e1);
+                    }
+                }
+            std::sort(cand.begin(), cand.end());
+            cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+            const bool cyl = planar == PLGPU_GEOMETRY_CYLINDRICAL;
+            // the stiffness scale of the edge terms: the reference omits the micrometre
+            // factor of len (its load terms carry 0.5e-6) and weights the cylindrical
+            // element matrix, edge terms included, by the midpoint radius
+            const double kscale = bc_compat ? 1.0 : 1e-6;
+            enum { BOTTOM, RIGHT, TOP, LEFT };
+            for (long long ec : cand) {
+                const int i = (int)(ec % n[0]), j = (int)(ec / n[0]);
+                const long long em = i * es[0] + j * es[1];
+                const int m = host_mat[em];
+                if (exclude_empty() && empty[m]) continue;
+                // i1 = lower left, i2 = lower right, i3 = upper right, i4 = upper left
+                const long long nd[4] = {ec, ec + 1, ec + 1 + n[0], ec + n[0]};
+                const double w = ax[0][i + 1] - ax[0][i], h = ax[1][j + 1] - ax[1][j];
+                const double rm = 0.5 * (ax[0][i] + ax[0][i + 1]);
+                const double rw = (cyl && bc_compat) ? rm : 1.0;  // the element's weight r K_e
+                // edges as (own node, other node, length, side): bottom 1-2, right 2-3, top 3-4, left 1-4
+                const int ea[4] = {0, 1, 2, 0}, eb[4] = {1, 2, 3, 3};
+                const int sides[4] = {BOTTOM, RIGHT, TOP, LEFT};
+                // radius factor of a node's share of an edge term (cylindrical form)
+                auto fac = [&](int side, int own, int other, double len) {
+                    if (!cyl) return 1.0;
+                    if (side == LEFT) return ax[0][i];
+                    if (side == RIGHT) return ax[0][i + 1];
+                    return rm + (nd[own] < nd[other] ? -len / 6.0 : len / 6.0);
+                };
+                auto facmn = [&](int side) {
+                    if (!cyl) return 1.0;
+                    if (side == LEFT) return ax[0][i];
+                    if (side == RIGHT) return ax[0][i + 1];
+                    return rm;
+                };
+                for (int kind = PLGPU_BC_HEATFLUX; kind <= PLGPU_BC_RADIATION; ++kind) {
+                    auto& mm = kind == PLGPU_BC_HEATFLUX ? mhf : kind == PLGPU_BC_CONVECTION ? mcv : mrd;
+                    if (mm.empty()) continue;
+                    int cond[4];
+                    bool has[4];
+                    for (int c = 0; c < 4; ++c) {
+                        auto it = mm.find(nd[c]);
+                        has[c] = it != mm.end();
+                        cond[c] = has[c] ? it->second : -1;
+                    }
+                    for (int q = 0; q < 4; ++q) {
+                        const int a = ea[q], b2 = eb[q];
+                        if (!(has[a] && has[b2])) continue;
+                        const int side = sides[q];
+                        const double len = (side == BOTTOM || side == TOP) ? w : h;
+                        const Cond& ca = bcs[kind][cond[a]];
+                        const Cond& cb = bcs[kind][cond[b2]];
+                        for (int t = 0; t < 2; ++t) {
+                            const int own = t ? b2 : a, oth = t ? a : b2;
+                            const Cond& co = t ? cb : ca;
+                            const double f = fac(side, own, oth, len);
+                            if (kind == PLGPU_BC_HEATFLUX) {
+                                fadd[nd[own]] += -0.5e-6 * len * co.v0 * f;
+                            } else if (kind == PLGPU_BC_CONVECTION) {
+                                fadd[nd[own]] += cyl ? 0.125e-6 * len * (ca.v0 + cb.v0) * (ca.v1 + cb.v1) * f
+                                                     : 0.5e-6 * len * co.v0 * co.v1;
+                                K[{nd[own], nd[own]}] += rw * kscale * (ca.v0 + cb.v0) * len / 6.0 * f;
+                            } else {
+                                rad.push_back({nd[own], nd[own], -0.5e-6 * len * co.v0 * kSB * f, co.v1});
+                            }
+                        }
+                        if (kind == PLGPU_BC_CONVECTION) {
+                            const double v = rw * kscale * (ca.v0 + cb.v0) * len / 12.0 * facmn(side);
+                            K[{nd[a], nd[b2]}] += v;
+                            K[{nd[b2], nd[a]}] += v;
+                        }
+                    }
                 }
             }
-            std::sort(els.begin(), els.end());
-            els.erase(std::unique(els.begin(), els.end()), els.end());
-            cand.swap(els);
-        }
-        static const int walls[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}};
-        for (long long ec : cand) {
-            const int i = (int)(ec % n[0]), j = (int)((ec / n[0]) % n[1]), k = (int)(ec / ((long long)n[0] * n[1]));
-            const long long em = i * es[0] + j * es[1] + (long long)k * es[2];
-            const int m = host_mat[em];
-            if (exclude_empty() && empty[m]) continue;
-            long long idx[8];
-            for (int c = 0; c < 8; ++c)
-                idx[c] = (i + (c & 1)) + (long long)n[0] * ((j + ((c >> 1) & 1)) + (long long)n[1] * (k + (c >> 2)));
-            const double dx = ax[0][i + 1] - ax[0][i], dy = ax[1][j + 1] - ax[1][j], dz = ax[2][k + 1] - ax[2][k];
-            const double areas[3] = {dx * dy, dy * dz, dz * dx};
-            for (int kind = PLGPU_BC_HEATFLUX; kind <= PLGPU_BC_RADIATION; ++kind) {
-                auto& mm = kind == PLGPU_BC_HEATFLUX ? mhf : kind == PLGPU_BC_CONVECTION ? mcv : mrd;
-                if (mm.empty()) continue;
-                int cond[8];
-                bool has[8];
-                for (int c = 0; c < 8; ++c) {
-                    auto it = mm.find(idx[c]);
-                    has[c] = it != mm.end();
-                    cond[c] = has[c] ? it->second : -1;
+        } else {
+            // global nodes 0..7 in the solver's numbering (radiation quirk, therm3d.cpp:265)
+            long long glob[8];
+            for (int w = 0; w < 8; ++w) {
+                long long cn = -1;
+                if (masked) {
+                    if (w < (long long)h_active.size()) cn = h_active[w];
+                } else if (w < N) {
+                    cn = canon_of_mesh(w);
                 }
-                for (int side = 0; side < 6; ++side) {
-                    const int* w = walls[side];
-                    if (!(has[w[0]] && has[w[1]] && has[w[2]] && has[w[3]])) continue;
-                    const double area = areas[side / 2];
-                    for (int a = 0; a < 4; ++a) {
-                        const Cond& ca = bcs[kind][cond[w[a]]];
-                        // where the term lands: element corner a (reference placement) or the face node
-                        const long long ta = bc_compat ? idx[a] : idx[w[a]];
-                        if (kind == PLGPU_BC_HEATFLUX) {
-                            fadd[ta] += -0.25e-12 * area * ca.v0;
-                        } else if (kind == PLGPU_BC_CONVECTION) {
-                            fadd[ta] += 0.25e-12 * area * ca.v0 * ca.v1;
-                            for (int bq = 0; bq <= a; ++bq) {
-                                const Cond& cb = bcs[kind][cond[w[bq]]];
-                                const int ij = a ^ bq;
-                                const bool edge = (ij == 1 || ij == 2 || ij == 4);
-                                const double v = 0.125e-12 * area * (ca.v0 + cb.v0) / (a == bq ? 9.0 : edge ? 18.0 : 36.0);
-                                const long long tb = bc_compat ? idx[bq] : idx[w[bq]];
-                                K[{ta, tb}] += v;
-                                if (ta != tb) K[{tb, ta}] += v;
+                glob[w] = cn;
+            }
+
+            std::vector<long long> cand;
+            {
+                std::vector<long long> nodes;
+                for (auto* m : {&mhf, &mcv, &mrd})
+                    for (auto& kv : *m) nodes.push_back(kv.first);
+                std::vector<long long> els;
+                for (long long cn : nodes) {
+                    const int i = (int)(cn % n[0]), j = (int)((cn / n[0]) % n[1]), k = (int)(cn / ((long long)n[0] * n[1]));
+                    for (int c = 0; c < 8; ++c) {
+                        const int e0 = i - (c & 1), e1 = j - ((c >> 1) & 1), e2 = k - (c >> 2);
+                        if (e0 < 0 || e1 < 0 || e2 < 0 || e0 >= n[0] - 1 || e1 >= n[1] - 1 || e2 >= n[2] - 1) continue;
+                        els.push_back(e0 + (long long)n[0] * (e1 + (long long)n[1] * e2));
+                    }
+                }
+                std::sort(els.begin(), els.end());
+                els.erase(std::unique(els.begin(), els.end()), els.end());
+                cand.swap(els);
+            }
+            static const int walls[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}};
+            for (long long ec : cand) {
+                const int i = (int)(ec % n[0]), j = (int)((ec / n[0]) % n[1]), k = (int)(ec / ((long long)n[0] * n[1]));
+                const long long em = i * es[0] + j * es[1] + (long long)k * es[2];
+                const int m = host_mat[em];
+                if (exclude_empty() && empty[m]) continue;
+                long long idx[8];
+                for (int c = 0; c < 8; ++c)
+                    idx[c] = (i + (c & 1)) + (long long)n[0] * ((j + ((c >> 1) & 1)) + (long long)n[1] * (k + (c >> 2)));
+                const double dx = ax[0][i + 1] - ax[0][i], dy = ax[1][j + 1] - ax[1][j], dz = ax[2][k + 1] - ax[2][k];
+                const double areas[3] = {dx * dy, dy * dz, dz * dx};
+                for (int kind = PLGPU_BC_HEATFLUX; kind <= PLGPU_BC_RADIATION; ++kind) {
+                    auto& mm = kind == PLGPU_BC_HEATFLUX ? mhf : kind == PLGPU_BC_CONVECTION ? mcv : mrd;
+                    if (mm.empty()) continue;
+                    int cond[8];
+                    bool has[8];
+                    for (int c = 0; c < 8; ++c) {
+                        auto it = mm.find(idx[c]);
+                        has[c] = it != mm.end();
+                        cond[c] = has[c] ? it->second : -1;
+                    }
+                    for (int side = 0; side < 6; ++side) {
+                        const int* w = walls[side];
+                        if (!(has[w[0]] && has[w[1]] && has[w[2]] && has[w[3]])) continue;
+                        const double area = areas[side / 2];
+                        for (int a = 0; a < 4; ++a) {
+                            const Cond& ca = bcs[kind][cond[w[a]]];
+                            // where the term lands: element corner a (reference placement) or the face node
+                            const long long ta = bc_compat ? idx[a] : idx[w[a]];
+                            if (kind == PLGPU_BC_HEATFLUX) {
+                                fadd[ta] += -0.25e-12 * area * ca.v0;
+                            } else if (kind == PLGPU_BC_CONVECTION) {
+                                fadd[ta] += 0.25e-12 * area * ca.v0 * ca.v1;
+                                for (int bq = 0; bq <= a; ++bq) {
+                                    const Cond& cb = bcs[kind][cond[w[bq]]];
+                                    const int ij = a ^ bq;
+                                    const bool edge = (ij == 1 || ij == 2 || ij == 4);
+                                    const double v = 0.125e-12 * area * (ca.v0 + cb.v0) / (a == bq ? 9.0 : edge ? 18.0 : 36.0);
+                                    const long long tb = bc_compat ? idx[bq] : idx[w[bq]];
+                                    K[{ta, tb}] += v;
+                                    if (ta != tb) K[{tb, ta}] += v;
+                                }
+                            } else {
+                                const long long src = bc_compat ? glob[w[a]] : idx[w[a]];
+                                if (src < 0) throw ArgError("radiation boundary on a mesh with fewer than 8 nodes");
+                                rad.push_back({ta, src, -0.25e-12 * area * ca.v0 * kSB, ca.v1});
                             }
-                        } else {
-                            const long long src = bc_compat ? glob[w[a]] : idx[w[a]];
-                            if (src < 0) throw ArgError("radiation boundary on a mesh with fewer than 8 nodes");
-                            rad.push_back({ta, src, -0.25e-12 * area * ca.v0 * kSB, ca.v1});
                         }
                     }
                 }
             }
         }
+
         // split the surface stiffness: free-free part on the device, free-Dirichlet part
         // eliminated into the static load (b_c -= A(c, r) v_first(r), matrix.hpp:137-144)
         std::vector<int> srow, sptr, scol;
@@ -763,7 +883,10 @@ struct plgpu_fem3d {
     }
 
     void build_static_load() {
-        launch_heat_load(cfg, g64, d_heat.as<double>(), d_mat.as<int>(), tab, F.as<double>());
+        if (planar)
+            launch_heat_load2d(cfg, g64, rmid_ptr64(), d_heat.as<double>(), d_mat.as<int>(), tab, F.as<double>());
+        else
+            launch_heat_load(cfg, g64, d_heat.as<double>(), d_mat.as<int>(), tab, F.as<double>());
         launch_scatter_add(cfg, n_fbc, fbc_idx.as<int>(), fbc_val.as<double>(), F.as<double>());
         heat_dirty = false;
     }
@@ -774,9 +897,45 @@ struct plgpu_fem3d {
     // y = A x (or a variant, see MODE_*) with the optimised operator and the current coefficients
     // MODE_CG: y = A p with the convective surface rows (k_surface_cg first, then the
     // operator), (p, A p) and the step length
+    const double* rmid_ptr64() const {
+        return planar == PLGPU_GEOMETRY_CYLINDRICAL ? rmid64.as<double>() : nullptr;
+    }
+    const float* rmid_ptr32() const { return planar == PLGPU_GEOMETRY_CYLINDRICAL ? rmid32.as<float>() : nullptr; }
+
+    // k(T) of every element at the current temperature (setMatrix's thermk calls)
+    void update_coef() {
+        if (planar)
+            launch_coef2d(cfg, n[0], n[1], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab, k64.as<double>(),
+                          k32.as<float>(), aniso ? kz64.as<double>() : nullptr, aniso ? kz32.as<float>() : nullptr,
+                          aniso);
+        else
+            launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab,
+                        k64.as<double>(), k32.as<float>(), aniso ? kz64.as<double>() : nullptr,
+                        aniso ? kz32.as<float>() : nullptr, aniso);
+    }
+    // Jacobi diagonal of the current operator and its inverse (FP64 and FP32)
+    void update_diag() {
+        if (planar) {
+            launch_diag2d(cfg, g64, rmid_ptr64(), k64.as<double>(), aniso ? kz64.as<double>() : nullptr,
+                          diag.as<double>());
+            launch_finish_diag(cfg, N, s64, dmask.as<uint32_t>(), diag.as<double>(), minv64.as<double>(),
+                               minv32.as<float>());
+        } else {
+            launch_diag(cfg, g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, s64,
+                        dmask.as<uint32_t>(), diag.as<double>(), minv64.as<double>(), minv32.as<float>());
+        }
+    }
+
     void op64(const double* x, double* y, const double* rhs, int mode, SolveCtl* ctl = nullptr) {
         SolveCtl* c = ctl ? ctl : d_ctl.as<SolveCtl>();
         int ss = 0;
+        if (planar) {
+            if (mode == MODE_CG) ss = launch_surface_cg(cfg, s64, x, y, partials.as<double>(), op2d_blocks(cfg, N), c);
+            launch_operator2d(cfg, g64, rmid_ptr64(), x, y, k64.as<double>(), aniso ? kz64.as<double>() : nullptr,
+                              dmask.as<uint32_t>(), rhs, partials.as<double>(), mode, c,
+                              ss > 0 ? smask.as<uint32_t>() : nullptr, ss);
+            return;
+        }
         if (mode == MODE_CG)
             ss = launch_surface_cg(cfg, s64, x, y, partials.as<double>(), op_blocks(cfg, n[0], n[1], n[2], true), c);
         launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), x, y, k64.as<double>(),
@@ -787,6 +946,13 @@ struct plgpu_fem3d {
     void op32(const float* x, float* y, int mode, SolveCtl* ctl = nullptr) {
         SolveCtl* c = ctl ? ctl : d_ctl.as<SolveCtl>();
         int ss = 0;
+        if (planar) {
+            if (mode == MODE_CG) ss = launch_surface_cg(cfg, s32, x, y, partials.as<double>(), op2d_blocks(cfg, N), c);
+            launch_operator2d(cfg, g32, rmid_ptr32(), x, y, k32.as<float>(), aniso ? kz32.as<float>() : nullptr,
+                              dmask.as<uint32_t>(), (const float*)nullptr, partials.as<double>(), mode, c,
+                              ss > 0 ? smask.as<uint32_t>() : nullptr, ss);
+            return;
+        }
         if (mode == MODE_CG)
             ss = launch_surface_cg(cfg, s32, x, y, partials.as<double>(), op_blocks(cfg, n[0], n[1], n[2], false), c);
         launch_operator(cfg, g32, zf32.as<float>(), zr32.as<float>(), x, y, k32.as<float>(),
@@ -1265,11 +1431,8 @@ struct plgpu_fem3d {
         do {
             ck(cudaMemcpyAsync(T0.p, T.p, (size_t)N * 8, cudaMemcpyDeviceToDevice, stream), "copy T0");
             // setMatrix: coefficients, Jacobi diagonal, right-hand side with Dirichlet elimination
-            launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab,
-                        k64.as<double>(), k32.as<float>(), aniso ? kz64.as<double>() : nullptr,
-                        aniso ? kz32.as<float>() : nullptr, aniso);
-            launch_diag(cfg, g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, s64,
-                        dmask.as<uint32_t>(), diag.as<double>(), minv64.as<double>(), minv32.as<float>());
+            update_coef();
+            update_diag();
             if (algorithm == PLGPU_ALGO_GPU_LEARNED && pre != nullptr) {
                 ensure_unet_buffers();
                 refresh_features();
@@ -1504,8 +1667,7 @@ struct plgpu_fem3d {
         if (bc_dirty) materialize_bc();
         if (reps <= 0) throw ArgError("reps must be positive");
         // coefficients of the current temperature, a deterministic input vector
-        launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab, k64.as<double>(),
-                    k32.as<float>(), aniso ? kz64.as<double>() : nullptr, aniso ? kz32.as<float>() : nullptr, aniso);
+        update_coef();
         launch_fill(cfg, N, p64.as<double>(), 1.0);
         launch_norm2(cfg, N, p64.as<double>(), p32.as<float>(), partials.as<double>(), d_ctl.as<SolveCtl>(), 4);
         // a scratch control block: the CG-mode operator sets a step length and may flag a
@@ -1522,7 +1684,15 @@ struct plgpu_fem3d {
             ck(cudaMemsetAsync(&ctl->status, 0, sizeof(int), stream), "memset");
             ck(cudaEventRecord(ev2, stream), "event");
             // the stencil kernel alone (no surface rows)
-            if (precision == 64)
+            if (planar && precision == 64)
+                launch_operator2d(cfg, g64, rmid_ptr64(), p64.as<double>(), q64.as<double>(), k64.as<double>(),
+                                  aniso ? kz64.as<double>() : nullptr, dmask.as<uint32_t>(), (const double*)nullptr,
+                                  partials.as<double>(), MODE_CG, ctl, nullptr, 0);
+            else if (planar)
+                launch_operator2d(cfg, g32, rmid_ptr32(), p32.as<float>(), q32.as<float>(), k32.as<float>(),
+                                  aniso ? kz32.as<float>() : nullptr, dmask.as<uint32_t>(), (const float*)nullptr,
+                                  partials.as<double>(), MODE_CG, ctl, nullptr, 0);
+            else if (precision == 64)
                 launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), p64.as<double>(), q64.as<double>(),
                                 k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(),
                                 nullptr, partials.as<double>(), MODE_CG, ctl);
@@ -1548,8 +1718,7 @@ struct plgpu_fem3d {
     void mult(int precision, const double* xin, double* yout) {
         if (!initialized) initialize();
         if (bc_dirty) materialize_bc();
-        launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab, k64.as<double>(),
-                    k32.as<float>(), aniso ? kz64.as<double>() : nullptr, aniso ? kz32.as<float>() : nullptr, aniso);
+        update_coef();
         DevBuf tmp;
         tmp.alloc((size_t)N * 8);
         ck(cudaMemcpyAsync(tmp.p, xin, (size_t)N * 8, cudaMemcpyHostToDevice, stream), "H2D x");
@@ -1611,14 +1780,25 @@ struct plgpu_fem3d {
         canon.alloc((size_t)NE * comps * 8);
         tmp.alloc((size_t)NE * comps * 8);
         fill(this, canon.as<double>());
-        launch_to_mesh_order_f64(cfg, n[0] - 1, n[1] - 1, n[2] - 1, n[0] - 1, (long long)(n[0] - 1) * (n[1] - 1), es[0],
-                                 es[1], es[2], comps, canon.as<double>(), tmp.as<double>());
+        launch_to_mesh_order_f64(cfg, me(0), me(1), me(2), me(0), (long long)me(0) * me(1), es[0], es[1], es[2], comps,
+                                 canon.as<double>(), tmp.as<double>());
         ck(cudaMemcpyAsync(out, tmp.p, (size_t)NE * comps * 8, cudaMemcpyDeviceToHost, stream), "D2H");
         ck(cudaStreamSynchronize(stream), "sync");
     }
 
+    // 3 values per element (2 on a planar handle)
     void get_flux(double* out3) {
         if (!initialized) initialize();
+        if (planar) {
+            element_output(2,
+                           [](plgpu_fem3d* h, double* dst) {
+                               launch_flux2d(h->cfg, h->g64, h->T.as<double>(), h->d_mat.as<int>(),
+                                             h->have_leaf ? h->d_hleaf.as<double>() : h->d_th.as<double>(), h->tab,
+                                             dst);
+                           },
+                           out3);
+            return;
+        }
         element_output(3,
                        [](plgpu_fem3d* h, double* dst) {
                            launch_flux(h->cfg, h->g64, h->T.as<double>(), h->d_mat.as<int>(),
@@ -1630,8 +1810,12 @@ struct plgpu_fem3d {
         if (!initialized) initialize();
         element_output(2,
                        [](plgpu_fem3d* h, double* dst) {
-                           launch_conductivity(h->cfg, h->n[0], h->n[1], h->n[2], h->T.as<double>(),
-                                               h->d_mat.as<int>(), h->d_th.as<double>(), h->tab, dst);
+                           if (h->planar)
+                               launch_conductivity2d(h->cfg, h->n[0], h->n[1], h->T.as<double>(), h->d_mat.as<int>(),
+                                                     h->d_th.as<double>(), h->tab, dst);
+                           else
+                               launch_conductivity(h->cfg, h->n[0], h->n[1], h->n[2], h->T.as<double>(),
+                                                   h->d_mat.as<int>(), h->d_th.as<double>(), h->tab, dst);
                        },
                        out2);
     }
@@ -1639,7 +1823,7 @@ struct plgpu_fem3d {
         if (!initialized) initialize();
         DevBuf tmp;
         tmp.alloc((size_t)NE * 8);
-        launch_to_mesh_order_f64(cfg, n[0] - 1, n[1] - 1, n[2] - 1, n[0], (long long)n[0] * n[1], es[0], es[1], es[2], 1,
+        launch_to_mesh_order_f64(cfg, me(0), me(1), me(2), n[0], (long long)n[0] * n[1], es[0], es[1], es[2], 1,
                                  d_th.as<double>(), tmp.as<double>());
         ck(cudaMemcpyAsync(out, tmp.p, (size_t)NE * 8, cudaMemcpyDeviceToHost, stream), "D2H");
         ck(cudaStreamSynchronize(stream), "sync");
@@ -1694,8 +1878,7 @@ void plgpu_fem3d::mult_noalloc(int precision, const double* xin, double* yout) {
         throw StateError("plgpu_fem3d_mult_noalloc needs a handle whose mesh, materials and boundary conditions "
                          "are already set up on the device: call plgpu_fem3d_compute or plgpu_fem3d_mult once first");
     double* stage = noalloc_stage();
-    launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab, k64.as<double>(),
-                k32.as<float>(), aniso ? kz64.as<double>() : nullptr, aniso ? kz32.as<float>() : nullptr, aniso);
+    update_coef();
     ck(cudaMemcpyAsync(stage, xin, (size_t)N * 8, cudaMemcpyHostToDevice, stream), "H2D x");
     launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], n[1], n[2], ns[0], ns[1], ns[2], stage, p64.as<double>(),
                                0.0);
@@ -2179,6 +2362,36 @@ int plgpu_fem3d_create(const double* ax0, int n0, const double* ax1, int n1, con
     return PLGPU_OK;
 }
 
+int plgpu_fem2d_create(const double* ax0, int n0, const double* ax1, int n1, int ordering, int geometry,
+                       plgpu_fem3d** out) {
+    if (!out) return PLGPU_ERR_ARG;
+    *out = nullptr;
+    if (ordering != PLGPU_ORDER2D_10 && ordering != PLGPU_ORDER2D_01) {
+        g_create_error = "unknown 2D iteration order";
+        return PLGPU_ERR_ARG;
+    }
+    if (geometry != PLGPU_GEOMETRY_CARTESIAN && geometry != PLGPU_GEOMETRY_CYLINDRICAL) {
+        g_create_error = "unknown 2D geometry";
+        return PLGPU_ERR_ARG;
+    }
+    std::unique_ptr<plgpu_fem3d> h(new plgpu_fem3d());
+    try {
+        // the node plane is the major (outermost) axis 2 of size 1: ORDER_10 (axis 0
+        // fastest) is the 3D order 210, ORDER_01 (axis 1 fastest) the order 201
+        const double z0 = 0.0;
+        h->setup_mesh(ax0, n0, ax1, n1, &z0, 1, ordering == PLGPU_ORDER2D_10 ? PLGPU_ORDER_210 : PLGPU_ORDER_201,
+                      geometry);
+    } catch (const ArgError& e) {
+        g_create_error = e.what();
+        return PLGPU_ERR_ARG;
+    } catch (const std::exception& e) {
+        g_create_error = e.what();
+        return PLGPU_ERR_CUDA;
+    }
+    *out = h.release();
+    return PLGPU_OK;
+}
+
 int plgpu_fem3d_destroy(plgpu_fem3d* h) {
     if (!h) return PLGPU_ERR_ARG;
     if (h->stream) cudaStreamSynchronize(h->stream);
@@ -2437,7 +2650,10 @@ int plgpu_unet_load(plgpu_unet* net, const char* path) {
 int plgpu_unet_train(plgpu_unet* net, plgpu_fem3d* fem, int steps, float lr, unsigned long long seed, int smooth_min,
                      int smooth_max, int pair_kind, float* losses) {
     if (!net) return PLGPU_ERR_ARG;
-    return guarded(fem, [&] { fem->train(net, steps, lr, seed, smooth_min, smooth_max, pair_kind, losses); });
+    return guarded(fem, [&] {
+        if (fem->planar) throw ArgError("the learned preconditioner is 3D only");
+        fem->train(net, steps, lr, seed, smooth_min, smooth_max, pair_kind, losses);
+    });
 }
 
 int plgpu_unet_loss_grad(plgpu_unet* net, plgpu_fem3d* fem, const double* e, double* loss, float* grad, double* r_out,
@@ -2445,6 +2661,7 @@ int plgpu_unet_loss_grad(plgpu_unet* net, plgpu_fem3d* fem, const double* e, dou
     if (!net) return PLGPU_ERR_ARG;
     return guarded(fem, [&] {
         if (!e || !loss || !grad) throw ArgError("null argument");
+        if (fem->planar) throw ArgError("the learned preconditioner is 3D only");
         fem->loss_grad(net, e, loss, grad, r_out, z_out);
     });
 }
@@ -2453,12 +2670,14 @@ int plgpu_unet_apply(plgpu_unet* net, plgpu_fem3d* fem, const double* r, double*
     if (!net) return PLGPU_ERR_ARG;
     return guarded(fem, [&] {
         if (!r || !z) throw ArgError("null argument");
+        if (fem->planar) throw ArgError("the learned preconditioner is 3D only");
         fem->apply_net(net, r, z);
     });
 }
 
 int plgpu_fem3d_set_preconditioner(plgpu_fem3d* fem, plgpu_unet* net) {
     return guarded(fem, [&] {
+        if (fem->planar && net) throw ArgError("the learned preconditioner is 3D only");
         fem->pre = net;
         fem->invalidate_graphs();
     });
@@ -2646,6 +2865,7 @@ int plgpu_fem3d_heat_from(plgpu_fem3d* thermal, plgpu_elec3d* electrical) {
     if (!electrical) return PLGPU_ERR_ARG;
     return guarded(thermal, [&] {
         if (thermal == electrical) throw ArgError("the thermal and electrical handles must differ");
+        if (thermal->planar) throw ArgError("a 2D thermal handle cannot take 3D heat");
         for (int d = 0; d < 3; ++d)
             if (thermal->ax[d] != electrical->ax[d])
                 throw ArgError("thermal and electrical meshes differ (interpolate on the host instead)");
@@ -2659,6 +2879,7 @@ int plgpu_fem3d_heat_from(plgpu_fem3d* thermal, plgpu_elec3d* electrical) {
 int plgpu_fem3d_get_element_temperature(plgpu_fem3d* h, double* out) {
     return guarded(h, [&] {
         if (!out) throw ArgError("null output");
+        if (h->planar) throw ArgError("element temperatures are provided for 3D handles");
         if (!h->initialized) {
             for (long long e = 0; e < h->NE; ++e) out[e] = h->inittemp;
             return;
@@ -2775,6 +2996,7 @@ int plgpu_fem3d_batch_tune(plgpu_fem3d* const* handles, int count, int loops, in
 int plgpu_fem3d_set_dynamic(plgpu_fem3d* h, const double* cp, const double* dens, double timestep,
                             double methodparam, int lumping, int rebuildfreq, int logfreq) {
     return guarded(h, [&] {
+        if (h->planar) throw ArgError("time stepping is provided for 3D handles (Dynamic3D)");
         if (h->n_mat == 0) throw StateError("set the material table first");
         if (!cp || !dens) throw ArgError("cp and dens are required");
         if (!(timestep > 0.0) || !std::isfinite(timestep)) throw ArgError("timestep must be positive");
@@ -2797,6 +3019,7 @@ int plgpu_fem3d_set_dynamic(plgpu_fem3d* h, const double* cp, const double* dens
 int plgpu_fem3d_compute_dynamic(plgpu_fem3d* h, double time, double* elapsed, plgpu_stats* stats) {
     return guarded(h, [&] {
         if (!std::isfinite(time) || time < 0.0) throw ArgError("time must be finite and >= 0");
+        if (h->planar) throw ArgError("time stepping is provided for 3D handles (Dynamic3D)");
         h->compute_dynamic(time, stats);
         if (elapsed) *elapsed = h->elapstime;
     });

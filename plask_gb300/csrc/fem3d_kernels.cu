@@ -979,6 +979,11 @@ void launch_diag(const LaunchCfg& c, const GridT<double>& g, const double* kxy, 
     if (shift) launch(k_add_vec, vec_blocks(c, g.N), 256, c.stream, g.N, diag, shift);
     launch(k_invert_diag, vec_blocks(c, g.N), 256, c.stream, g.N, diag, dmask, minv64, minv32);
 }
+void launch_finish_diag(const LaunchCfg& c, long long N, const SurfaceT<double>& s, const uint32_t* dmask,
+                        double* diag, double* minv64, float* minv32) {
+    if (s.nrows > 0) launch(k_surface_diag, grid_for(s.nrows, 256, 1024), 256, c.stream, s, diag);
+    launch(k_invert_diag, vec_blocks(c, N), 256, c.stream, N, diag, dmask, minv64, minv32);
+}
 void launch_heat_load(const LaunchCfg& c, const GridT<double>& g, const double* q, const int* mat, const MatTable& tab,
                       double* F) {
     launch(k_heat_load, vec_blocks(c, g.N), 256, c.stream, g, q, mat, tab, F);

@@ -116,6 +116,9 @@ void launch_coef(const LaunchCfg& c, int n0, int n1, int n2, const double* T, co
 void launch_diag(const LaunchCfg& c, const GridT<double>& g, const double* kxy, const double* kz, bool aniso,
                  const SurfaceT<double>& s, const uint32_t* dmask, double* diag, double* minv64, float* minv32,
                  const double* shift = nullptr);
+// add the surface rows' diagonal to `diag` and invert it (Dirichlet and empty rows: 0)
+void launch_finish_diag(const LaunchCfg& c, long long N, const SurfaceT<double>& s, const uint32_t* dmask,
+                        double* diag, double* minv64, float* minv32);
 // ---- time stepping (dyn3d_kernels.cu)
 // lumped heat capacity per node: sum over the node's active elements of
 // cp dens 0.125e-9 dx dy dz / timestep (FP64 and FP32 copies)

@@ -1,4 +1,4 @@
-"""Rectilinear 3D mesh with PLaSK's iteration orders and named boundaries.
+"""Rectilinear 3D and 2D meshes with PLaSK's iteration orders and named boundaries.
 
 Mirrors the parts of ``plask.mesh.Rectangular3D`` that the Static3D path uses
 (plask/mesh/rectilinear3d.hpp, rectilinear3d.cpp:20-190):
@@ -11,7 +11,9 @@ Mirrors the parts of ``plask.mesh.Rectangular3D`` that the Static3D path uses
 * ``setOptimalIterationOrder`` (largest axis major, smallest minor).
 
 Arrays called "canonical" here have shape (n2, n1, n0) -- axis 0 fastest --
-which is also the device layout of the GPU solver.
+which is also the device layout of the GPU solver.  The 2D mesh
+(``RectangularMesh2D``, plask/mesh/rectangular2d.hpp/.cpp) has orders ORDER_10
+(axis 0 fastest) and ORDER_01 (axis 1 fastest) and canonical shape (n1, n0).
 """
 from __future__ import annotations
 
@@ -207,3 +209,128 @@ class RectangularMesh3D:
         return {"back": RectangularMesh3D.Back, "front": RectangularMesh3D.Front, "left": RectangularMesh3D.Left,
                 "right": RectangularMesh3D.Right, "bottom": RectangularMesh3D.Bottom,
                 "top": RectangularMesh3D.Top}[name]()
+
+
+# ----------------------------------------------------------------------------------------
+# 2D
+
+
+ORDERS2D = ("10", "01")
+
+
+def optimal_order2d(n0, n1):
+    """RectangularMesh2D::setOptimalIterationOrder (rectangular2d.hpp:296-298): the longer axis major."""
+    return "01" if n0 > n1 else "10"
+
+
+def mesh_index2d(sizes, order):
+    """Canonical-shaped (n1, n0) array of mesh-order indices (rectangular2d.cpp:20-38):
+    ORDER_10 index = i0 + n0 i1, ORDER_01 index = i1 + n1 i0."""
+    n0, n1 = sizes
+    i0 = np.arange(n0)[None, :]
+    i1 = np.arange(n1)[:, None]
+    if order == "10":
+        return (i0 + n0 * i1).astype(np.int64)
+    if order == "01":
+        return (i1 + n1 * i0).astype(np.int64)
+    raise ValueError(f"unknown 2D iteration order {order!r}")
+
+
+def to_mesh_order2d(canon, order, comps=None):
+    """Flatten a canonical (n1, n0[, c]) array into mesh order."""
+    canon = np.asarray(canon)
+    sizes = (canon.shape[1], canon.shape[0])
+    idx = mesh_index2d(sizes, order).ravel()
+    tail = canon.shape[2:]
+    out = np.empty((idx.size,) + tail, dtype=canon.dtype)
+    out[idx] = canon.reshape((idx.size,) + tail)
+    return out
+
+
+class RectangularMesh2D:
+    """Rectilinear 2D mesh (plask.mesh.Rectangular2D): axis 0 horizontal (the radius of a
+    cylindrical geometry), axis 1 vertical, micrometres, with an iteration order
+    "01" (default, axis 1 fastest), "10" or "best"."""
+
+    def __init__(self, axis0, axis1, ordering=None):
+        self.axis0 = np.ascontiguousarray(axis0, dtype=np.float64)
+        self.axis1 = np.ascontiguousarray(axis1, dtype=np.float64)
+        for a in self.axes:
+            if a.ndim != 1 or a.size < 2 or np.any(np.diff(a) <= 0):
+                raise ValueError("mesh axes must be strictly increasing with at least 2 points")
+        if ordering is None:
+            ordering = "01"
+        if ordering == "best":
+            ordering = optimal_order2d(*self.sizes)
+        if ordering not in ORDERS2D:
+            raise ValueError(f"unknown iteration order {ordering!r}")
+        self.ordering = ordering
+
+    @property
+    def axes(self):
+        return (self.axis0, self.axis1)
+
+    @property
+    def sizes(self):
+        return (self.axis0.size, self.axis1.size)
+
+    @property
+    def shape(self):
+        """Canonical node shape (n1, n0)."""
+        return (self.axis1.size, self.axis0.size)
+
+    @property
+    def element_shape(self):
+        return (self.axis1.size - 1, self.axis0.size - 1)
+
+    def __len__(self):
+        return self.axis0.size * self.axis1.size
+
+    @property
+    def elements_count(self):
+        return (self.axis0.size - 1) * (self.axis1.size - 1)
+
+    def index_array(self):
+        return mesh_index2d(self.sizes, self.ordering)
+
+    def element_index_array(self):
+        return mesh_index2d((self.axis0.size - 1, self.axis1.size - 1), self.ordering)
+
+    def element_midpoints(self):
+        """Canonical (ne1, ne0, 2) array of element midpoints."""
+        m0 = 0.5 * (self.axis0[1:] + self.axis0[:-1])
+        m1 = 0.5 * (self.axis1[1:] + self.axis1[:-1])
+        Y, X = np.meshgrid(m1, m0, indexing="ij")
+        return np.stack([X, Y], axis=-1)
+
+    # named boundaries (rectangular2d.hpp: left/right along axis 0, bottom/top along axis 1)
+    @staticmethod
+    def Left():
+        return _side((slice(None), 0), "left")
+
+    @staticmethod
+    def Right():
+        return _side((slice(None), -1), "right")
+
+    @staticmethod
+    def Bottom():
+        return _side((0,), "bottom")
+
+    @staticmethod
+    def Top():
+        return _side((-1,), "top")
+
+    @staticmethod
+    def IndexBox(i0, i1, j0, j1):
+        """Nodes with index ranges [i0, i1] x [j0, j1] (inclusive)."""
+        return _side((slice(j0, j1 + 1), slice(i0, i1 + 1)), "box")
+
+    @staticmethod
+    def Nodes(mask):
+        mask = np.asarray(mask, bool)
+        return Boundary(lambda mesh: mask.reshape(mesh.shape), "nodes")
+
+    @staticmethod
+    def side(name):
+        return {"left": RectangularMesh2D.Left, "right": RectangularMesh2D.Right,
+                "bottom": RectangularMesh2D.Bottom, "top": RectangularMesh2D.Top}[name]()

@@ -339,3 +339,42 @@ def shockley_c4(seed=4000, n=(200, 200, 120), voltage=None, n_layers=12, contact
                          empty=np.zeros(n_mat, bool), noheat=np.zeros(n_mat, bool), junction=junction, beta=[18.0],
                          js=[1.0], voltage=[(top, volts), (bottom, 0.0)], symmetric=(True, True), maxerr=0.1,
                          thermal=thermal, name=f"shockley-{n[0]}x{n[1]}x{n[2]}-s{seed}")
+
+
+def layered_2d(seed=0, n=(60, 80), power=1e15, n_layers=10, etch=False, anisotropic=False):
+    """2D layered structure for Static2D / StaticCyl: the 3D generator's vertical stack on
+    a 0..50 um horizontal axis refined toward 0 (the axis or the symmetry plane), a
+    source within 4 um of it in a 0.1 um layer, bottom at 300 K.  The default power is a
+    tenth of the 3D generator's: a 2D strip source (infinite along the depth) heats far
+    more than a disc, and at 1e16 W/m^3 the k(T) layers run away thermally.
+
+    ``etch``: the layers above the active one are removed beyond x = 15 um (an EMPTY
+    material there, a mesa), which exercises the masked mesh.  ``anisotropic``: k_1/k_0
+    ~ U[0.5, 1] per material.  Axes are (axis0, axis1), ``mat``/``heat`` of shape
+    (n1-1, n0-1), boundary sides "left", "right", "bottom", "top"."""
+    rng = np.random.default_rng(seed)
+    n_layers = max(1, min(n_layers, (n[1] - 1) - max(1, int(round(0.25 * (n[1] - 1))))))
+    thick = np.exp(rng.uniform(math.log(0.05), math.log(3.0), n_layers))
+    active = int(rng.integers(n_layers // 3, max(n_layers // 3 + 1, 2 * n_layers // 3)))
+    thick[active] = 0.1
+    x0 = graded_axis(n[0])
+    y, layer_of = vertical_axis(thick, n[1])
+    n_mat = n_layers + 1
+    k300 = np.exp(rng.uniform(math.log(1.0), math.log(150.0), n_mat))
+    p = rng.uniform(0.5, 1.5, n_mat)
+    kz = rng.uniform(0.5, 1.0, n_mat) if anisotropic else np.ones(n_mat)
+    mat = np.broadcast_to(layer_of[:, None], (n[1] - 1, n[0] - 1)).astype(np.int32).copy()
+    xm = 0.5 * (x0[1:] + x0[:-1])
+    empty = np.zeros(n_mat, bool)
+    if etch:
+        k300 = np.append(k300, 0.026)
+        p = np.append(p, 0.0)
+        kz = np.append(kz, 1.0)
+        empty = np.append(empty, True)
+        mat[(layer_of > active + 1)[:, None] & (xm > 15.0)[None, :]] = n_mat
+        n_mat += 1
+    heat = np.zeros(mat.shape)
+    heat[layer_of == active + 1] = np.where(np.abs(xm) <= 4.0, power, 0.0)[None]
+    return Structure(axes=(x0, y), mat=np.ascontiguousarray(mat), k300=k300, p=p, kz_ratio=kz,
+                     hexp=np.zeros(n_mat), empty=empty, heat=heat, temperature=[("bottom", 300.0)],
+                     name=f"layered2d-{n[0]}x{n[1]}-s{seed}")
