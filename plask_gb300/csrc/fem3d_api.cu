@@ -1042,7 +1042,10 @@ struct plgpu_fem3d {
     //                                   than rtol ||b|| would notice),
     // unless that asks for less than the rounding floor of computing b - A T in FP64,
     // estimated as kFloorUlps eps sqrt(sum A_ii T_i^2) (a row sums about 27 products of
-    // size A_ii |T|).  A solve whose FP64 residual stops falling has reached the floor:
+    // size A_ii |T|); static solves stop at twice the estimate (one more refinement below
+    // it costs 14 % more CG iterations at 128x128x200 and moves max T by < 1e-9 K), time
+    // steps, whose right-hand sides carry the capacity terms, at the estimate itself.
+    // A solve whose FP64 residual stops falling has reached the floor:
     // it counts as converged when ||r|| <= kStagnationAccept ||b||, as failed above that.
     static constexpr double kChangeRtol = 1e-6;
     static constexpr double kFloorUlps = 8.0;
@@ -1063,7 +1066,7 @@ struct plgpu_fem3d {
                           d_ctl.as<SolveCtl>(), 4);
         const SolveCtl c = read_ctl();
         const double floor_rel = bn > 0 ? kFloorUlps * 1.1102230246251565e-16 * std::sqrt(c.red[4]) / bn : 0.0;
-        return std::max(std::min(rtol, kChangeRtol * relres0), floor_rel);
+        return std::max(std::min(rtol, kChangeRtol * relres0), (dyn_active ? 1.0 : 2.0) * floor_rel);
     }
 
     // FP64 Jacobi-PCG on A T = b starting from the current T.  When the recursive

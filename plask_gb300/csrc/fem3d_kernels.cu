@@ -233,6 +233,7 @@ __global__ void __launch_bounds__(256) k_cg_update(long long N, R* __restrict__ 
 // FP32 forms of k_cg_update and k_cg_direction with 16-byte accesses: thread t
 // handles the float4 groups t, t + stride, ...; the last N % 4 entries by the first
 // threads.  Same arithmetic per entry as the scalar kernels.
+constexpr int kVecUnroll = 4;
 __device__ __forceinline__ void cg_update_one(float& x, float& r, float p, float q, float m, float alpha, float& rz,
                                               float& rr) {
     x += alpha * p;
@@ -256,15 +257,34 @@ __global__ void __launch_bounds__(256) k_cg_update_v4(long long N, float* __rest
     const float4* p4 = reinterpret_cast<const float4*>(p);
     const float4* q4 = reinterpret_cast<const float4*>(q);
     const float4* m4 = reinterpret_cast<const float4*>(minv);
-    for (long long v = t0; v < N4; v += stride) {
-        const float4 pn = p4[v], qn = q4[v], mn = m4[v];
-        float4 xn = x4[v], rn = r4[v];
-        cg_update_one(xn.x, rn.x, pn.x, qn.x, mn.x, alpha, rz, rr);
-        cg_update_one(xn.y, rn.y, pn.y, qn.y, mn.y, alpha, rz, rr);
-        cg_update_one(xn.z, rn.z, pn.z, qn.z, mn.z, alpha, rz, rr);
-        cg_update_one(xn.w, rn.w, pn.w, qn.w, mn.w, alpha, rz, rr);
-        x4[v] = xn;
-        r4[v] = rn;
+    // kVecUnroll groups per trip, all loads issued before the arithmetic (the vectors are
+    // mostly L2-resident: latency, not bandwidth, limits one group at a time); each
+    // thread still visits its groups in increasing order
+    for (long long v0 = t0; v0 < N4; v0 += kVecUnroll * stride) {
+        float4 pn[kVecUnroll], qn[kVecUnroll], mn[kVecUnroll], xn[kVecUnroll], rn[kVecUnroll];
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) {
+            const long long v = v0 + u * stride;
+            if (v < N4) {
+                pn[u] = p4[v];
+                qn[u] = q4[v];
+                mn[u] = m4[v];
+                xn[u] = x4[v];
+                rn[u] = r4[v];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) {
+            const long long v = v0 + u * stride;
+            if (v < N4) {
+                cg_update_one(xn[u].x, rn[u].x, pn[u].x, qn[u].x, mn[u].x, alpha, rz, rr);
+                cg_update_one(xn[u].y, rn[u].y, pn[u].y, qn[u].y, mn[u].y, alpha, rz, rr);
+                cg_update_one(xn[u].z, rn[u].z, pn[u].z, qn[u].z, mn[u].z, alpha, rz, rr);
+                cg_update_one(xn[u].w, rn[u].w, pn[u].w, qn[u].w, mn[u].w, alpha, rz, rr);
+                x4[v] = xn[u];
+                r4[v] = rn[u];
+            }
+        }
     }
     for (long long n = (N4 << 2) + t0; n < N; n += stride) {
         float xn = x[n], rn = r[n];
@@ -312,14 +332,28 @@ __global__ void __launch_bounds__(256) k_cg_direction_v4(long long N, float* __r
     float4* p4 = reinterpret_cast<float4*>(p);
     const float4* r4 = reinterpret_cast<const float4*>(r);
     const float4* m4 = reinterpret_cast<const float4*>(minv);
-    for (long long v = t0; v < N4; v += stride) {
-        const float4 rn = r4[v], mn = m4[v];
-        float4 pn = p4[v];
-        pn.x = mn.x * rn.x + beta * pn.x;
-        pn.y = mn.y * rn.y + beta * pn.y;
-        pn.z = mn.z * rn.z + beta * pn.z;
-        pn.w = mn.w * rn.w + beta * pn.w;
-        p4[v] = pn;
+    for (long long v0 = t0; v0 < N4; v0 += kVecUnroll * stride) {
+        float4 rn[kVecUnroll], mn[kVecUnroll], pn[kVecUnroll];
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) {
+            const long long v = v0 + u * stride;
+            if (v < N4) {
+                rn[u] = r4[v];
+                mn[u] = m4[v];
+                pn[u] = p4[v];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) {
+            const long long v = v0 + u * stride;
+            if (v < N4) {
+                pn[u].x = mn[u].x * rn[u].x + beta * pn[u].x;
+                pn[u].y = mn[u].y * rn[u].y + beta * pn[u].y;
+                pn[u].z = mn[u].z * rn[u].z + beta * pn[u].z;
+                pn[u].w = mn[u].w * rn[u].w + beta * pn[u].w;
+                p4[v] = pn[u];
+            }
+        }
     }
     for (long long n = (N4 << 2) + t0; n < N; n += stride) p[n] = minv[n] * r[n] + beta * p[n];
 }
