@@ -66,7 +66,9 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 // MINB: blocks per SM the register budget is sized for; UNR: unrolling of the z-march
-template <typename R, int RR, bool ANISO, int MODE, int MINB = (sizeof(R) == 4 ? 4 : 2), int UNR = 1>
+// SHIFT: add the diagonal a.dshift (time steps); static solves compile it out.
+template <typename R, int RR, bool ANISO, int MODE, bool SHIFT = false, int MINB = (sizeof(R) == 4 ? 4 : 2),
+          int UNR = 1>
 __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
     if (MODE == MODE_CG && a.ctl != nullptr && a.ctl->status != SOLVE_RUNNING) return;
     const int n0 = a.g.n0, n1 = a.g.n1, n2 = a.g.n2;
@@ -215,7 +217,7 @@ __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
             for (int r = 1; r <= RR; ++r) {
                 if (out_lane && noff[r] >= 0) {
                     const long long n = pb + noff[r];
-                    if (a.dshift != nullptr) acc[r - 1] += a.dshift[n] * xlo[r];
+                    if (SHIFT) acc[r - 1] += a.dshift[n] * xlo[r];
                     R out;
                     if (MODE == MODE_CG) {
                         // Dirichlet rows: x is zero there and M^-1 = 0 keeps the CG residual zero
@@ -254,6 +256,216 @@ __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
         const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
         // (x, A x): block partial, then the last block to finish adds the surface kernel's
         // partials and sets the step length
+        double v[1] = {(double)dot};
+        write_partial<1, OpSum>(v, a.partials, bid);
+        const int nblocks = gridDim.x * gridDim.y * gridDim.z;
+        if (arrive_last(&a.ctl->arrive[0], nblocks)) {
+            reduce_partials<1, OpSum>(v, a.partials, nblocks + a.sslots);
+            if (threadIdx.x == 0) {
+                const double pq = v[0];
+                a.ctl->pq = pq;
+                if (!isfinite(pq))
+                    a.ctl->status = SOLVE_NONFINITE;
+                else if (!(pq > 0.0))
+                    a.ctl->status = SOLVE_BREAKDOWN;
+                else
+                    a.ctl->alpha = a.ctl->rz / pq;
+            }
+        }
+    }
+}
+
+// The same operator with the butterfly stages shared between neighbouring elements.
+// The x-stage (sum and difference of a node and its +x neighbour) of every node row is
+// computed once per plane and used by the two element rows and two element layers that
+// contain that x-edge; the contributions of all elements to a node row are accumulated as
+// (sum, difference) pairs and unfolded into the two node columns once per plane, so one
+// lane shuffle per output row replaces four per element.  Per output node this issues
+// 11 % fewer FMA-pipe and 23 % fewer load/store-pipe instructions than k_apply_haar
+// (ncu, 128x128x200, 4 rows per thread).
+template <typename R, int RR, bool ANISO, int MODE, bool SHIFT = false, int MINB = (sizeof(R) == 4 ? 4 : 2)>
+__global__ void __launch_bounds__(128, MINB) k_apply_shared(const OpArgs<R> a) {
+    if (MODE == MODE_CG && a.ctl != nullptr && a.ctl->status != SOLVE_RUNNING) return;
+    const int n0 = a.g.n0, n1 = a.g.n1, n2 = a.g.n2;
+    const int s2 = n0 * n1;  // N < 2^31 (checked on the host)
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int i = blockIdx.x * 30 - 1 + lane;
+    const int jb = (blockIdx.y * (blockDim.x >> 5) + warp) * RR;
+    const int k0 = blockIdx.z * a.zchunk;
+    const int k1 = min(k0 + a.zchunk, n2);
+    const bool out_lane = lane >= 1 && lane <= 30 && i < n0;
+    const bool have_i = i >= 0 && i < n0;
+    const bool elem_i = i >= 0 && i < n0 - 1;
+
+    int noff[RR + 2], eoff[RR + 1];
+#pragma unroll
+    for (int r = 0; r < RR + 2; ++r) {
+        const int j = jb - 1 + r;
+        noff[r] = (have_i && j >= 0 && j < n1) ? i + n0 * j : -1;
+    }
+    R gx[RR + 1], gy[RR + 1], gz[RR + 1];
+    {
+        const R dx = elem_i ? a.g.h0[i] : R(0);
+        const R rdx = elem_i ? a.g.r0[i] : R(0);
+#pragma unroll
+        for (int e = 0; e <= RR; ++e) {
+            const int j = jb - 1 + e;
+            const bool ok = elem_i && j >= 0 && j < n1 - 1;
+            eoff[e] = ok ? i + n0 * j : -1;
+            const R dy = ok ? a.g.h1[j] : R(0);
+            const R rdy = ok ? a.g.r1[j] : R(0);
+            gx[e] = dy * rdx;
+            gy[e] = dx * rdy;
+            gz[e] = dx * dy;
+        }
+    }
+    auto load_x = [&](int k, R(&xv)[RR + 2]) {
+        const bool kin = k >= 0 && k < n2;
+        const R* base = a.x + (long long)s2 * (kin ? k : 0);
+#pragma unroll
+        for (int r = 0; r < RR + 2; ++r) {
+            R v = R(0);
+            if (kin && noff[r] >= 0) {
+                v = base[noff[r]];
+                if ((MODE == MODE_RESID || MODE == MODE_MULT) && dir_bit(a.dmask, (long long)s2 * k + noff[r])) v = R(0);
+            }
+            xv[r] = v;
+        }
+    };
+    auto load_k = [&](int k, R(&kk)[RR + 1], R(&kv)[RR + 1]) {
+        const bool kin = k >= 0 && k < n2 - 1;
+        const long long b = (long long)s2 * (kin ? k : 0);
+#pragma unroll
+        for (int e = 0; e <= RR; ++e) {
+            R v = R(0), w = R(0);
+            if (kin && eoff[e] >= 0) {
+                v = a.kxy[b + eoff[e]];
+                if (ANISO) w = a.kz[b + eoff[e]];
+            }
+            kk[e] = v;
+            kv[e] = ANISO ? w : v;
+        }
+    };
+    // x-stage of a plane: s = x + x(i+1), d = x(i+1) - x per node row
+    auto xstage = [&](const R(&xv)[RR + 2], R(&sx)[RR + 2], R(&dx)[RR + 2]) {
+#pragma unroll
+        for (int r = 0; r < RR + 2; ++r) {
+            const R xp = __shfl_down_sync(0xffffffffu, xv[r], 1);
+            sx[r] = xv[r] + xp;
+            dx[r] = xp - xv[r];
+        }
+    };
+
+    // (sum, difference) accumulators of the output rows 1..RR: plane k and plane k + 1
+    R accS[RR], accD[RR], nxtS[RR], nxtD[RR];
+#pragma unroll
+    for (int r = 0; r < RR; ++r) accS[r] = accD[r] = nxtS[r] = nxtD[r] = R(0);
+
+    R dot = R(0);
+    const int kstart = max(k0 - 1, 0);
+    R xlo[RR], xhi[RR + 2], xnx[RR + 2];  // xlo: raw x of the output rows of plane k
+    R sxl[RR + 2], dxl[RR + 2];
+    R kk[RR + 1], kv[RR + 1], kkn[RR + 1], kvn[RR + 1];
+    {
+        R x0[RR + 2];
+        load_x(kstart, x0);
+        xstage(x0, sxl, dxl);
+#pragma unroll
+        for (int r = 0; r < RR; ++r) xlo[r] = x0[r + 1];
+    }
+    load_x(kstart + 1, xhi);
+    load_k(kstart, kk, kv);
+
+    for (int k = kstart; k < k1; ++k) {
+        load_x(k + 2, xnx);
+        load_k(k + 1, kkn, kvn);
+        R sxh[RR + 2], dxh[RR + 2];
+        xstage(xhi, sxh, dxh);
+        const int kl = min(k, n2 - 2);
+        const R zf = a.zf[kl], zr = a.zr[kl];
+#pragma unroll
+        for (int e = 0; e <= RR; ++e) {
+            const R X = kk[e] * gx[e] * zf;
+            const R Y = kk[e] * gy[e] * zf;
+            const R Z = kv[e] * gz[e] * zr;
+            const R l100 = R(3) * X, l010 = R(3) * Y, l001 = R(3) * Z;
+            const R l110 = X + Y, l101 = X + Z, l011 = Y + Z;
+            const R l111 = (X + Y + Z) * R(1.0 / 3.0);
+            // y-stage of the rows e, e + 1 on both planes
+            const R ss0 = sxl[e] + sxl[e + 1], sd0 = sxl[e + 1] - sxl[e];
+            const R ds0 = dxl[e] + dxl[e + 1], dd0 = dxl[e + 1] - dxl[e];
+            const R ss1 = sxh[e] + sxh[e + 1], sd1 = sxh[e + 1] - sxh[e];
+            const R ds1 = dxh[e] + dxh[e + 1], dd1 = dxh[e + 1] - dxh[e];
+            // z-stage and the weights
+            const R m001 = (ss1 - ss0) * l001;
+            const R m010 = (sd0 + sd1) * l010, m011 = (sd1 - sd0) * l011;
+            const R m100 = (ds0 + ds1) * l100, m101 = (ds1 - ds0) * l101;
+            const R m110 = (dd0 + dd1) * l110, m111 = (dd1 - dd0) * l111;
+            // transposed z- and y-stages: (sum, difference) pairs of the four node rows
+            const R tsd0 = m010 - m011, tsd1 = m010 + m011;
+            const R tds0 = m100 - m101, tds1 = m100 + m101;
+            const R tdd0 = m110 - m111, tdd1 = m110 + m111;
+            if (e >= 1) {  // row e (cj = 0)
+                accS[e - 1] += -m001 - tsd0;
+                accD[e - 1] += tds0 - tdd0;
+                nxtS[e - 1] += m001 - tsd1;
+                nxtD[e - 1] += tds1 - tdd1;
+            }
+            if (e + 1 <= RR) {  // row e + 1 (cj = 1)
+                accS[e] += tsd0 - m001;
+                accD[e] += tds0 + tdd0;
+                nxtS[e] += m001 + tsd1;
+                nxtD[e] += tds1 + tdd1;
+            }
+        }
+        // plane k is complete: own column s - d, column i + 1 (the next lane) s + d
+        if (k >= k0) {
+            const long long pb = (long long)s2 * k;
+#pragma unroll
+            for (int r = 1; r <= RR; ++r) {
+                const R recv = __shfl_up_sync(0xffffffffu, accS[r - 1] + accD[r - 1], 1);
+                R res = (accS[r - 1] - accD[r - 1]) + recv;
+                if (out_lane && noff[r] >= 0) {
+                    const long long n = pb + noff[r];
+                    if (SHIFT) res += a.dshift[n] * xlo[r - 1];
+                    R out;
+                    if (MODE == MODE_CG) {
+                        out = res;
+                        dot += xlo[r - 1] * out;
+                        if (a.smask != nullptr && dir_bit(a.smask, n)) out += a.y[n];
+                    } else if (MODE == MODE_RESID) {
+                        out = dir_bit(a.dmask, n) ? R(a.rhs[n] - a.x[n]) : R(a.rhs[n] - res);
+                    } else if (MODE == MODE_MULT) {
+                        out = dir_bit(a.dmask, n) ? a.x[n] : res;
+                    } else {
+                        out = a.rhs[n] - res;
+                    }
+                    a.y[n] = out;
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < RR; ++r) {
+            accS[r] = nxtS[r];
+            accD[r] = nxtD[r];
+            nxtS[r] = nxtD[r] = R(0);
+            xlo[r] = xhi[r + 1];
+        }
+#pragma unroll
+        for (int r = 0; r < RR + 2; ++r) {
+            sxl[r] = sxh[r];
+            dxl[r] = dxh[r];
+            xhi[r] = xnx[r];
+        }
+#pragma unroll
+        for (int e = 0; e <= RR; ++e) {
+            kk[e] = kkn[e];
+            kv[e] = kvn[e];
+        }
+    }
+    if (MODE == MODE_CG) {
+        const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
         double v[1] = {(double)dot};
         write_partial<1, OpSum>(v, a.partials, bid);
         const int nblocks = gridDim.x * gridDim.y * gridDim.z;
@@ -312,7 +524,7 @@ static void op_grid(const LaunchCfg& c, int n0, int n1, int n2, bool fp64, dim3&
 // (rows covered / n1) x (r + 1) / r.  Pick the smallest (then the fewest rows on a tie).
 // The choice is a fixed function of the mesh, so results do not depend on timing
 // (the tile changes the order in which (p, A p) is summed).  Measured at 128x128x200:
-// r = 4, 5, 6 take 34.2, 34.4, 37.3 us per launch; the model picks 4.
+// r = 4, 5, 6 take 32.4, 34.3, 35.9 us per launch; the model picks 4.
 int choose_op_rows(int n1) {
     int best = 6;
     double best_cost = 1e300;
@@ -335,15 +547,31 @@ int op_blocks(const LaunchCfg& c, int n0, int n1, int n2, bool fp64) {
     return (int)(g.x * g.y * g.z);
 }
 
+// FP32 tiles of 4 and 5 rows run the shared-stage kernel (measured at 128x128x200:
+// 32.4 and 34.3 us against 34.5 and 35.6 us for k_apply_haar); 6 rows and FP64 keep
+// k_apply_haar (the shared form spills at 6 rows in 128 registers).
+template <typename R, int RR, bool ANISO, int MODEV, bool SHIFT>
+static void op_launch_one(const LaunchCfg& c, dim3 grid, const OpArgs<R>& a) {
+    if constexpr (sizeof(R) == 4 && RR <= 5)
+        launch_kernel(k_apply_shared<R, RR, ANISO, MODEV, SHIFT>, grid, dim3(32 * kWarps), c.stream, a);
+    else
+        launch_kernel(k_apply_haar<R, RR, ANISO, MODEV, SHIFT>, grid, dim3(32 * kWarps), c.stream, a);
+}
+
 template <typename R, int RR>
 static void op_launch_rows(const LaunchCfg& c, dim3 grid, const OpArgs<R>& a, bool aniso, int mode) {
-#define PLGPU_OP(MODEV)                                                                                   \
-    if (mode == MODEV) {                                                                                  \
-        if (aniso)                                                                                        \
-            launch_kernel(k_apply_haar<R, RR, true, MODEV>, grid, dim3(32 * kWarps), c.stream, a);        \
-        else                                                                                              \
-            launch_kernel(k_apply_haar<R, RR, false, MODEV>, grid, dim3(32 * kWarps), c.stream, a);       \
-        return;                                                                                           \
+    const bool shift = a.dshift != nullptr;
+#define PLGPU_OP(MODEV)                                             \
+    if (mode == MODEV) {                                            \
+        if (aniso && shift)                                         \
+            op_launch_one<R, RR, true, MODEV, true>(c, grid, a);    \
+        else if (aniso)                                             \
+            op_launch_one<R, RR, true, MODEV, false>(c, grid, a);   \
+        else if (shift)                                             \
+            op_launch_one<R, RR, false, MODEV, true>(c, grid, a);   \
+        else                                                        \
+            op_launch_one<R, RR, false, MODEV, false>(c, grid, a);  \
+        return;                                                     \
     }
     PLGPU_OP(MODE_CG)
     PLGPU_OP(MODE_RESID)
