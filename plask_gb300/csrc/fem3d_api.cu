@@ -1682,7 +1682,8 @@ struct plgpu_fem3d {
         DevBuf flush;
         if (flush_l2) flush.alloc((size_t)512 << 20);  // well above the 126 MiB L2
         float total = 0.f;
-        for (int r = 0; r < reps; ++r) {
+        // two untimed launches first: the first launch of a kernel in a process also loads it
+        for (int r = -2; r < reps; ++r) {
             if (flush_l2) ck(cudaMemsetAsync(flush.p, r & 0xff, flush.bytes, stream), "flush");
             ck(cudaMemsetAsync(&ctl->status, 0, sizeof(int), stream), "memset");
             ck(cudaEventRecord(ev2, stream), "event");
@@ -1707,7 +1708,7 @@ struct plgpu_fem3d {
             ck(cudaEventSynchronize(ev3), "sync");
             float ms = 0.f;
             ck(cudaEventElapsedTime(&ms, ev2, ev3), "elapsed");
-            total += ms;
+            if (r >= 0) total += ms;
         }
         ck(cudaGetLastError(), "launch");
         *avg_ms = total / reps;
