@@ -246,10 +246,10 @@ int plgpu_fem3d_set_log_callback(plgpu_fem3d* h, void (*cb)(void* user, int leve
    on the same handle, mesh, materials, heat and temperature conditions. */
 
 /* Heat capacity cp [J/(kg K)] and density dens [kg/m^3] per material, timestep [ns],
-   methodparam theta (0.5 Crank-Nicolson, 0 explicit, 1 implicit), lumping (only the
-   lumped heat-capacity matrix, the reference's default, is provided: 0 is rejected),
-   rebuildfreq (rebuild A and B with k(T) every that many steps, 0 never) and logfreq
-   (femT3d.cpp:26-34, 54-66). */
+   methodparam theta (0.5 Crank-Nicolson, 0 explicit, 1 implicit), lumping (nonzero:
+   the lumped heat-capacity matrix, the reference's default; 0: the consistent matrix
+   c (8, 4, 2, 1) / 27 per element, femT3d.cpp:203-226), rebuildfreq (rebuild A and B
+   with k(T) every that many steps, 0 never) and logfreq (femT3d.cpp:26-34, 54-66). */
 int plgpu_fem3d_set_dynamic(plgpu_fem3d* h, const double* cp, const double* dens, double timestep,
                             double methodparam, int lumping, int rebuildfreq, int logfreq);
 

@@ -1,10 +1,12 @@
 // Kernels of the time-stepping thermal solver (PLaSK solvers/thermal/dynamic/femT3d.cpp):
-// the system matrix is theta K + C with the lumped heat capacity C, applied by the
-// stencil kernel with a diagonal shift, so only the capacity, the coefficient scaling
-// and the right-hand side X = B T + F = C T - (1 - theta) K T + F live here.
+// the system matrix is theta K + C with the heat capacity C, applied by the stencil
+// kernel (the lumped C as a diagonal shift, the consistent C through per-element corner
+// capacities), so only the capacity, the coefficient scaling and the right-hand side
+// X = B T + F = C T - (1 - theta) K T + F live here.
 //
 //   k_lumped_mass   c = cp dens 0.125e-9 dx dy dz / timestep per element corner,
-//                   summed onto the nodes                     femT3d.cpp:183, 203-210
+//                   summed onto the nodes (times a weight)    femT3d.cpp:183, 203-210
+//   k_elem_capacity c per element for the consistent matrix    femT3d.cpp:183, 211-226
 //   k_dyn_rhs       X = B T + F                                femT3d.cpp:292-293
 #include <cstdint>
 
@@ -22,7 +24,7 @@ inline int grid_for(const LaunchCfg& c, long long n) {
 
 __global__ void __launch_bounds__(256) k_lumped_mass(const GridT<double> g, const int* __restrict__ mat,
                                                      const uint8_t* __restrict__ excl, const double* __restrict__ cp,
-                                                     const double* __restrict__ dens, double timestep,
+                                                     const double* __restrict__ dens, double timestep, double weight,
                                                      double* __restrict__ c64, float* __restrict__ c32) {
     const int n0 = g.n0, n1 = g.n1, n2 = g.n2;
     const long long s1 = n0, s2 = (long long)n0 * n1;
@@ -37,8 +39,32 @@ __global__ void __launch_bounds__(256) k_lumped_mass(const GridT<double> g, cons
             if (excl[m]) continue;
             c += cp[m] * dens[m] * 0.125e-9 * g.h0[ei] * g.h1[ej] * g.h2[ek] / timestep;
         }
-        c64[n] = c;
-        c32[n] = (float)c;
+        c64[n] = weight * c;
+        if (c32) c32[n] = (float)(weight * c);
+    }
+}
+
+// Corner capacity c of every element (padded layout, 0 for padding and excluded
+// elements): the consistent matrix of an element is c (8, 4, 2, 1) / 27 by corner
+// distance, c (M (x) M (x) M) with M = [[2,1],[1,2]] / 3.  cneg = -c for the right-hand
+// side product.
+__global__ void __launch_bounds__(256) k_elem_capacity(const GridT<double> g, const int* __restrict__ mat,
+                                                       const uint8_t* __restrict__ excl, const double* __restrict__ cp,
+                                                       const double* __restrict__ dens, double timestep,
+                                                       double* __restrict__ c64, float* __restrict__ c32,
+                                                       double* __restrict__ cneg) {
+    const int n0 = g.n0, n1 = g.n1, n2 = g.n2;
+    const long long s2 = (long long)n0 * n1;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < g.N; e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n0), j = (int)((e / n0) % n1), k = (int)(e / s2);
+        double c = 0.0;
+        if (i < n0 - 1 && j < n1 - 1 && k < n2 - 1) {
+            const int m = mat[e];
+            if (!excl[m]) c = cp[m] * dens[m] * 0.125e-9 * g.h0[i] * g.h1[j] * g.h2[k] / timestep;
+        }
+        c64[e] = c;
+        c32[e] = (float)c;
+        cneg[e] = -c;
     }
 }
 
@@ -60,8 +86,14 @@ __global__ void __launch_bounds__(256) k_dyn_rhs(long long N, const double* __re
 }
 
 void launch_lumped_mass(const LaunchCfg& c, const GridT<double>& g, const int* mat, const uint8_t* excl,
-                        const double* cp, const double* dens, double timestep, double* c64, float* c32) {
-    launch_kernel(k_lumped_mass, grid_for(c, g.N), 256, c.stream, g, mat, excl, cp, dens, timestep, c64, c32);
+                        const double* cp, const double* dens, double timestep, double* c64, float* c32,
+                        double weight) {
+    launch_kernel(k_lumped_mass, grid_for(c, g.N), 256, c.stream, g, mat, excl, cp, dens, timestep, weight, c64, c32);
+}
+void launch_elem_capacity(const LaunchCfg& c, const GridT<double>& g, const int* mat, const uint8_t* excl,
+                          const double* cp, const double* dens, double timestep, double* c64, float* c32,
+                          double* cneg) {
+    launch_kernel(k_elem_capacity, grid_for(c, g.N), 256, c.stream, g, mat, excl, cp, dens, timestep, c64, c32, cneg);
 }
 void launch_scale4(const LaunchCfg& c, long long N, double s, double* a64, float* a32, double* b64, float* b32) {
     launch_kernel(k_scale4, grid_for(c, N), 256, c.stream, N, s, a64, a32, b64, b32);

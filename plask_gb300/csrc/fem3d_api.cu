@@ -187,6 +187,7 @@ struct plgpu_fem3d {
     int dyn_rebuild = 0, dyn_logfreq = 500;
     double elapstime = 0.0;
     DevBuf d_cp, d_dens, cap64, cap32, kB64, kzB64, Fel, Yb, Zb, Tscratch;
+    DevBuf cel64, cel32, celneg64;  // consistent capacity: corner capacity per element, and negated
 
     // learned preconditioner
     plgpu_unet* pre = nullptr;
@@ -941,7 +942,8 @@ struct plgpu_fem3d {
         launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), x, y, k64.as<double>(),
                         aniso ? kz64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(), rhs, partials.as<double>(),
                         mode, c, ss > 0 ? smask.as<uint32_t>() : nullptr, ss,
-                        dyn_active ? cap64.as<double>() : nullptr);
+                        dyn_active && dyn_lumping ? cap64.as<double>() : nullptr,
+                        dyn_active && !dyn_lumping ? cel64.as<double>() : nullptr);
     }
     void op32(const float* x, float* y, int mode, SolveCtl* ctl = nullptr) {
         SolveCtl* c = ctl ? ctl : d_ctl.as<SolveCtl>();
@@ -958,7 +960,8 @@ struct plgpu_fem3d {
         launch_operator(cfg, g32, zf32.as<float>(), zr32.as<float>(), x, y, k32.as<float>(),
                         aniso ? kz32.as<float>() : nullptr, aniso, dmask.as<uint32_t>(), (const float*)nullptr,
                         partials.as<double>(), mode, c, ss > 0 ? smask.as<uint32_t>() : nullptr, ss,
-                        dyn_active ? cap32.as<float>() : nullptr);
+                        dyn_active && dyn_lumping ? cap32.as<float>() : nullptr,
+                        dyn_active && !dyn_lumping ? cel32.as<float>() : nullptr);
     }
     void opR(const double* x, double* y, int mode) { op64(x, y, nullptr, mode); }
     void opR(const float* x, float* y, int mode) { op32(x, y, mode); }
@@ -1523,8 +1526,21 @@ struct plgpu_fem3d {
         if (aniso) ck(cudaMemcpyAsync(kzB64.p, kz64.p, N8, cudaMemcpyDeviceToDevice, stream), "copy kz");
         launch_scale4(cfg, N, dyn_theta, k64.as<double>(), k32.as<float>(), aniso ? kz64.as<double>() : nullptr,
                       aniso ? kz32.as<float>() : nullptr);
-        launch_lumped_mass(cfg, g64, d_mat.as<int>(), d_excl.as<uint8_t>(), d_cp.as<double>(), d_dens.as<double>(),
-                           dyn_dt, cap64.as<double>(), cap32.as<float>());
+        if (dyn_lumping) {
+            launch_lumped_mass(cfg, g64, d_mat.as<int>(), d_excl.as<uint8_t>(), d_cp.as<double>(),
+                               d_dens.as<double>(), dyn_dt, cap64.as<double>(), cap32.as<float>());
+        } else {
+            // consistent C: corner capacities for the operator, its diagonal (8/27 c per
+            // element corner) for the Jacobi preconditioner, and B's stiffness part
+            // (1 - theta) K kept in kB for the right-hand side product
+            launch_elem_capacity(cfg, g64, d_mat.as<int>(), d_excl.as<uint8_t>(), d_cp.as<double>(),
+                                 d_dens.as<double>(), dyn_dt, cel64.as<double>(), cel32.as<float>(),
+                                 celneg64.as<double>());
+            launch_lumped_mass(cfg, g64, d_mat.as<int>(), d_excl.as<uint8_t>(), d_cp.as<double>(),
+                               d_dens.as<double>(), dyn_dt, cap64.as<double>(), nullptr, 8.0 / 27.0);
+            launch_scale4(cfg, N, 1.0 - dyn_theta, kB64.as<double>(), nullptr, aniso ? kzB64.as<double>() : nullptr,
+                          nullptr);
+        }
         launch_diag(cfg, g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, s64, dmask.as<uint32_t>(),
                     diag.as<double>(), minv64.as<double>(), minv32.as<float>(), cap64.as<double>());
         // F with the elimination of A's Dirichlet columns, the row values at the Dirichlet rows
@@ -1548,6 +1564,11 @@ struct plgpu_fem3d {
         if (aniso) kzB64.alloc(N8);
         cap64.alloc(N8);
         cap32.alloc((size_t)N * 4);
+        if (!dyn_lumping) {
+            cel64.alloc(N8);
+            cel32.alloc((size_t)N * 4);
+            celneg64.alloc(N8);
+        }
         Fel.alloc(N8);
         Yb.alloc(N8);
         Tscratch.alloc(N8);
@@ -1591,11 +1612,19 @@ struct plgpu_fem3d {
                 r = dyn_rebuild;
             }
             // X = B T + F = C T - (1 - theta) K T + F, then Dirichlet rows of T take X
-            launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), T.as<double>(), Yb.as<double>(),
-                            kB64.as<double>(), aniso ? kzB64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(),
-                            Zb.as<double>(), partials.as<double>(), MODE_RHS, d_ctl.as<SolveCtl>());
-            launch_dyn_rhs(cfg, N, cap64.as<double>(), T.as<double>(), Yb.as<double>(), 1.0 - dyn_theta,
-                           Fel.as<double>(), b.as<double>());
+            if (dyn_lumping) {
+                launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), T.as<double>(), Yb.as<double>(),
+                                kB64.as<double>(), aniso ? kzB64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(),
+                                Zb.as<double>(), partials.as<double>(), MODE_RHS, d_ctl.as<SolveCtl>());
+                launch_dyn_rhs(cfg, N, cap64.as<double>(), T.as<double>(), Yb.as<double>(), 1.0 - dyn_theta,
+                               Fel.as<double>(), b.as<double>());
+            } else {
+                // one operator pass: F - ((1 - theta) K - C) T with kB = (1 - theta) K and -c
+                launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), T.as<double>(), b.as<double>(),
+                                kB64.as<double>(), aniso ? kzB64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(),
+                                Fel.as<double>(), partials.as<double>(), MODE_RHS, d_ctl.as<SolveCtl>(), nullptr, 0,
+                                nullptr, celneg64.as<double>());
+            }
             launch_set_dirichlet(cfg, nrows, d_didx.as<int>(), d_dval.as<double>(), b.as<double>(), T.as<double>());
             ck(cudaEventRecord(ev2, stream), "event");
             int status = 0, iters = 0, refs = 0;
@@ -3005,7 +3034,6 @@ int plgpu_fem3d_set_dynamic(plgpu_fem3d* h, const double* cp, const double* dens
         if (!cp || !dens) throw ArgError("cp and dens are required");
         if (!(timestep > 0.0) || !std::isfinite(timestep)) throw ArgError("timestep must be positive");
         if (!(methodparam >= 0.0 && methodparam <= 1.0)) throw ArgError("methodparam must be in [0, 1]");
-        if (!lumping) throw ArgError("only the lumped heat-capacity matrix is provided (lumping = true)");
         if (rebuildfreq < 0 || logfreq < 0) throw ArgError("frequencies must be >= 0");
         for (int m = 0; m < h->n_mat; ++m)
             if (!std::isfinite(cp[m]) || !std::isfinite(dens[m]) || cp[m] < 0 || dens[m] < 0)

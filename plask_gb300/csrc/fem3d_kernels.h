@@ -67,11 +67,13 @@ int choose_op_rows(int n1);
 void launch_operator(const LaunchCfg& c, const GridT<float>& g, const float* zf, const float* zr, const float* x,
                      float* y, const float* kxy, const float* kz, bool aniso, const uint32_t* dmask, const float* rhs,
                      double* partials, int mode, SolveCtl* ctl, const uint32_t* smask = nullptr, int sslots = 0,
-                     const float* dshift = nullptr);
+                     const float* dshift = nullptr, const float* cmass = nullptr);
 void launch_operator(const LaunchCfg& c, const GridT<double>& g, const double* zf, const double* zr, const double* x,
                      double* y, const double* kxy, const double* kz, bool aniso, const uint32_t* dmask,
                      const double* rhs, double* partials, int mode, SolveCtl* ctl, const uint32_t* smask = nullptr,
-                     int sslots = 0, const double* dshift = nullptr);
+                     int sslots = 0, const double* dshift = nullptr, const double* cmass = nullptr);
+// dshift: a diagonal added to the operator (lumped capacity); cmass: per-element corner
+// capacities c of a consistent capacity matrix c (M (x) M (x) M), M = [[2,1],[1,2]] / 3
 // CG step, first half: y[row] = S x on the surface rows and block partials of (x, S x) in
 // slots slot0..slot0 + surface_cg_blocks - 1; returns the number of slots used.
 int launch_surface_cg(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, double* partials,
@@ -121,9 +123,14 @@ void launch_finish_diag(const LaunchCfg& c, long long N, const SurfaceT<double>&
                         double* diag, double* minv64, float* minv32);
 // ---- time stepping (dyn3d_kernels.cu)
 // lumped heat capacity per node: sum over the node's active elements of
-// cp dens 0.125e-9 dx dy dz / timestep (FP64 and FP32 copies)
+// cp dens 0.125e-9 dx dy dz / timestep, times `weight` (FP64 and, when c32 is given, FP32)
 void launch_lumped_mass(const LaunchCfg& c, const GridT<double>& g, const int* mat, const uint8_t* excl,
-                        const double* cp, const double* dens, double timestep, double* c64, float* c32);
+                        const double* cp, const double* dens, double timestep, double* c64, float* c32,
+                        double weight = 1.0);
+// corner capacity per element (consistent matrix), FP64, FP32 and negated FP64
+void launch_elem_capacity(const LaunchCfg& c, const GridT<double>& g, const int* mat, const uint8_t* excl,
+                          const double* cp, const double* dens, double timestep, double* c64, float* c32,
+                          double* cneg);
 // v *= s for the four coefficient arrays (any may be nullptr)
 void launch_scale4(const LaunchCfg& c, long long N, double s, double* a64, float* a32, double* b64, float* b32);
 // X = cap T + w Y + F  (Y = -K T)

@@ -53,7 +53,27 @@ struct OpArgs {
     // diagonal added to the operator, y += dshift x (the lumped heat capacity of the
     // time-stepping solver), or nullptr
     const R* dshift;
+    // consistent heat capacity: per element (padded like the conductivities) the corner
+    // capacity c, adding c (M (x) M (x) M), M = [[2,1],[1,2]] / 3, to the element matrix,
+    // or nullptr
+    const R* cmass;
 };
+
+// Weights of the consistent capacity in the butterfly basis: per axis M = (1/2) e e^T +
+// (1/6) d d^T, so moment m gets c (1/2)^(#sums) (1/6)^(#differences).
+template <typename R>
+__device__ __forceinline__ void add_mass_weights(R c, R& l000, R& l100, R& l010, R& l001, R& l110, R& l101, R& l011,
+                                                 R& l111) {
+    const R c24 = c * R(1.0 / 24.0), c72 = c * R(1.0 / 72.0);
+    l000 = c * R(0.125);
+    l100 += c24;
+    l010 += c24;
+    l001 += c24;
+    l110 += c72;
+    l101 += c72;
+    l011 += c72;
+    l111 += c * R(1.0 / 216.0);
+}
 
 __device__ __forceinline__ bool dir_bit(const uint32_t* __restrict__ m, long long n) {
     return (__ldg(m + (n >> 5)) >> (n & 31)) & 1u;
@@ -66,9 +86,10 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 // MINB: blocks per SM the register budget is sized for; UNR: unrolling of the z-march
-// SHIFT: add the diagonal a.dshift (time steps); static solves compile it out.
-template <typename R, int RR, bool ANISO, int MODE, bool SHIFT = false, int MINB = (sizeof(R) == 4 ? 4 : 2),
-          int UNR = 1>
+// SHIFT: add the diagonal a.dshift (lumped capacity of time steps); MASS: add the
+// consistent capacity a.cmass; static solves compile both out.
+template <typename R, int RR, bool ANISO, int MODE, bool SHIFT = false, bool MASS = false,
+          int MINB = (sizeof(R) == 4 ? 4 : 2), int UNR = 1>
 __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
     if (MODE == MODE_CG && a.ctl != nullptr && a.ctl->status != SOLVE_RUNNING) return;
     const int n0 = a.g.n0, n1 = a.g.n1, n2 = a.g.n2;
@@ -121,18 +142,20 @@ __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
             xv[r] = v;
         }
     };
-    auto load_k = [&](int k, R(&kk)[RR + 1], R(&kv)[RR + 1]) {
+    auto load_k = [&](int k, R(&kk)[RR + 1], R(&kv)[RR + 1], R(&cm)[MASS ? RR + 1 : 1]) {
         const bool kin = k >= 0 && k < n2 - 1;
         const long long b = (long long)s2 * (kin ? k : 0);
 #pragma unroll
         for (int e = 0; e <= RR; ++e) {
-            R v = R(0), w = R(0);
+            R v = R(0), w = R(0), c = R(0);
             if (kin && eoff[e] >= 0) {
                 v = a.kxy[b + eoff[e]];
                 if (ANISO) w = a.kz[b + eoff[e]];
+                if constexpr (MASS) c = a.cmass[b + eoff[e]];
             }
             kk[e] = v;
             kv[e] = ANISO ? w : v;
+            if constexpr (MASS) cm[e] = c;
         }
     };
 
@@ -144,9 +167,10 @@ __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
     const int kstart = max(k0 - 1, 0);
     R xlo[RR + 2], xlo_p[RR + 2], xhi[RR + 2], xnx[RR + 2];
     R kk[RR + 1], kv[RR + 1], kkn[RR + 1], kvn[RR + 1];
+    R cm[MASS ? RR + 1 : 1], cmn[MASS ? RR + 1 : 1];
     load_x(kstart, xlo);
     load_x(kstart + 1, xhi);
-    load_k(kstart, kk, kv);
+    load_k(kstart, kk, kv, cm);
 #pragma unroll
     for (int r = 0; r < RR + 2; ++r) xlo_p[r] = __shfl_down_sync(0xffffffffu, xlo[r], 1);
 
@@ -154,7 +178,7 @@ __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
     for (int k = kstart; k < k1; ++k) {
         // prefetch the next plane and the next element layer while this layer is computed
         load_x(k + 2, xnx);
-        load_k(k + 1, kkn, kvn);
+        load_k(k + 1, kkn, kvn, cmn);
         R xhi_p[RR + 2];
 #pragma unroll
         for (int r = 0; r < RR + 2; ++r) xhi_p[r] = __shfl_down_sync(0xffffffffu, xhi[r], 1);
@@ -166,9 +190,11 @@ __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
             const R X = kk[e] * gx[e] * zf;
             const R Y = kk[e] * gy[e] * zf;
             const R Z = kv[e] * gz[e] * zr;
-            const R l100 = R(3) * X, l010 = R(3) * Y, l001 = R(3) * Z;
-            const R l110 = X + Y, l101 = X + Z, l011 = Y + Z;
-            const R l111 = (X + Y + Z) * R(1.0 / 3.0);
+            R l100 = R(3) * X, l010 = R(3) * Y, l001 = R(3) * Z;
+            R l110 = X + Y, l101 = X + Z, l011 = Y + Z;
+            R l111 = (X + Y + Z) * R(1.0 / 3.0);
+            R l000 = R(0);
+            if constexpr (MASS) add_mass_weights(cm[e], l000, l100, l010, l001, l110, l101, l011, l111);
             // corners c = ci + 2 cj + 4 ck
             const R c0 = xlo[e], c1 = xlo_p[e], c2 = xlo[e + 1], c3 = xlo_p[e + 1];
             const R c4 = xhi[e], c5 = xhi_p[e], c6 = xhi[e + 1], c7 = xhi_p[e + 1];
@@ -185,7 +211,15 @@ __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
             const R tsd0 = m010 - m011, tsd1 = m010 + m011;
             const R tds0 = m100 - m101, tds1 = m100 + m101;
             const R tdd0 = m110 - m111, tdd1 = m110 + m111;
-            const R ys0 = -m001 - tsd0, ys1 = tsd0 - m001, ys2 = m001 - tsd1, ys3 = m001 + tsd1;
+            R ys0 = -m001 - tsd0, ys1 = tsd0 - m001, ys2 = m001 - tsd1, ys3 = m001 + tsd1;
+            if constexpr (MASS) {  // the all-sum moment m000 of the capacity
+                const R m000 = (ss0 + ss1) * l000;
+                const R tss0 = m000 - m001, tss1 = m000 + m001;
+                ys0 = tss0 - tsd0;
+                ys1 = tss0 + tsd0;
+                ys2 = tss1 - tsd1;
+                ys3 = tss1 + tsd1;
+            }
             const R yd0 = tds0 - tdd0, yd1 = tds0 + tdd0, yd2 = tds1 - tdd1, yd3 = tds1 + tdd1;
             // own column (ci = 0): node rows e (cj = 0) and e + 1 (cj = 1); output rows are 1..RR
             if (e >= 1) {
@@ -250,6 +284,7 @@ __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
         for (int e = 0; e <= RR; ++e) {
             kk[e] = kkn[e];
             kv[e] = kvn[e];
+            if constexpr (MASS) cm[e] = cmn[e];
         }
     }
     if (MODE == MODE_CG) {
@@ -283,7 +318,8 @@ __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
 // lane shuffle per output row replaces four per element.  Per output node this issues
 // 11 % fewer FMA-pipe and 23 % fewer load/store-pipe instructions than k_apply_haar
 // (ncu, 128x128x200, 4 rows per thread).
-template <typename R, int RR, bool ANISO, int MODE, bool SHIFT = false, int MINB = (sizeof(R) == 4 ? 4 : 2)>
+template <typename R, int RR, bool ANISO, int MODE, bool SHIFT = false, bool MASS = false,
+          int MINB = (sizeof(R) == 4 ? 4 : 2)>
 __global__ void __launch_bounds__(128, MINB) k_apply_shared(const OpArgs<R> a) {
     if (MODE == MODE_CG && a.ctl != nullptr && a.ctl->status != SOLVE_RUNNING) return;
     const int n0 = a.g.n0, n1 = a.g.n1, n2 = a.g.n2;
@@ -333,18 +369,20 @@ __global__ void __launch_bounds__(128, MINB) k_apply_shared(const OpArgs<R> a) {
             xv[r] = v;
         }
     };
-    auto load_k = [&](int k, R(&kk)[RR + 1], R(&kv)[RR + 1]) {
+    auto load_k = [&](int k, R(&kk)[RR + 1], R(&kv)[RR + 1], R(&cm)[MASS ? RR + 1 : 1]) {
         const bool kin = k >= 0 && k < n2 - 1;
         const long long b = (long long)s2 * (kin ? k : 0);
 #pragma unroll
         for (int e = 0; e <= RR; ++e) {
-            R v = R(0), w = R(0);
+            R v = R(0), w = R(0), c = R(0);
             if (kin && eoff[e] >= 0) {
                 v = a.kxy[b + eoff[e]];
                 if (ANISO) w = a.kz[b + eoff[e]];
+                if constexpr (MASS) c = a.cmass[b + eoff[e]];
             }
             kk[e] = v;
             kv[e] = ANISO ? w : v;
+            if constexpr (MASS) cm[e] = c;
         }
     };
     // x-stage of a plane: s = x + x(i+1), d = x(i+1) - x per node row
@@ -367,6 +405,7 @@ __global__ void __launch_bounds__(128, MINB) k_apply_shared(const OpArgs<R> a) {
     R xlo[RR], xhi[RR + 2], xnx[RR + 2];  // xlo: raw x of the output rows of plane k
     R sxl[RR + 2], dxl[RR + 2];
     R kk[RR + 1], kv[RR + 1], kkn[RR + 1], kvn[RR + 1];
+    R cm[MASS ? RR + 1 : 1], cmn[MASS ? RR + 1 : 1];
     {
         R x0[RR + 2];
         load_x(kstart, x0);
@@ -375,11 +414,11 @@ __global__ void __launch_bounds__(128, MINB) k_apply_shared(const OpArgs<R> a) {
         for (int r = 0; r < RR; ++r) xlo[r] = x0[r + 1];
     }
     load_x(kstart + 1, xhi);
-    load_k(kstart, kk, kv);
+    load_k(kstart, kk, kv, cm);
 
     for (int k = kstart; k < k1; ++k) {
         load_x(k + 2, xnx);
-        load_k(k + 1, kkn, kvn);
+        load_k(k + 1, kkn, kvn, cmn);
         R sxh[RR + 2], dxh[RR + 2];
         xstage(xhi, sxh, dxh);
         const int kl = min(k, n2 - 2);
@@ -389,9 +428,11 @@ __global__ void __launch_bounds__(128, MINB) k_apply_shared(const OpArgs<R> a) {
             const R X = kk[e] * gx[e] * zf;
             const R Y = kk[e] * gy[e] * zf;
             const R Z = kv[e] * gz[e] * zr;
-            const R l100 = R(3) * X, l010 = R(3) * Y, l001 = R(3) * Z;
-            const R l110 = X + Y, l101 = X + Z, l011 = Y + Z;
-            const R l111 = (X + Y + Z) * R(1.0 / 3.0);
+            R l100 = R(3) * X, l010 = R(3) * Y, l001 = R(3) * Z;
+            R l110 = X + Y, l101 = X + Z, l011 = Y + Z;
+            R l111 = (X + Y + Z) * R(1.0 / 3.0);
+            R l000 = R(0);
+            if constexpr (MASS) add_mass_weights(cm[e], l000, l100, l010, l001, l110, l101, l011, l111);
             // y-stage of the rows e, e + 1 on both planes
             const R ss0 = sxl[e] + sxl[e + 1], sd0 = sxl[e + 1] - sxl[e];
             const R ds0 = dxl[e] + dxl[e + 1], dd0 = dxl[e + 1] - dxl[e];
@@ -406,16 +447,25 @@ __global__ void __launch_bounds__(128, MINB) k_apply_shared(const OpArgs<R> a) {
             const R tsd0 = m010 - m011, tsd1 = m010 + m011;
             const R tds0 = m100 - m101, tds1 = m100 + m101;
             const R tdd0 = m110 - m111, tdd1 = m110 + m111;
+            R s0 = -m001 - tsd0, s1 = tsd0 - m001, s2n = m001 - tsd1, s3 = m001 + tsd1;
+            if constexpr (MASS) {  // the all-sum moment m000 of the capacity
+                const R m000 = (ss0 + ss1) * l000;
+                const R tss0 = m000 - m001, tss1 = m000 + m001;
+                s0 = tss0 - tsd0;
+                s1 = tss0 + tsd0;
+                s2n = tss1 - tsd1;
+                s3 = tss1 + tsd1;
+            }
             if (e >= 1) {  // row e (cj = 0)
-                accS[e - 1] += -m001 - tsd0;
+                accS[e - 1] += s0;
                 accD[e - 1] += tds0 - tdd0;
-                nxtS[e - 1] += m001 - tsd1;
+                nxtS[e - 1] += s2n;
                 nxtD[e - 1] += tds1 - tdd1;
             }
             if (e + 1 <= RR) {  // row e + 1 (cj = 1)
-                accS[e] += tsd0 - m001;
+                accS[e] += s1;
                 accD[e] += tds0 + tdd0;
-                nxtS[e] += m001 + tsd1;
+                nxtS[e] += s3;
                 nxtD[e] += tds1 + tdd1;
             }
         }
@@ -462,6 +512,7 @@ __global__ void __launch_bounds__(128, MINB) k_apply_shared(const OpArgs<R> a) {
         for (int e = 0; e <= RR; ++e) {
             kk[e] = kkn[e];
             kv[e] = kvn[e];
+            if constexpr (MASS) cm[e] = cmn[e];
         }
     }
     if (MODE == MODE_CG) {
@@ -550,45 +601,51 @@ int op_blocks(const LaunchCfg& c, int n0, int n1, int n2, bool fp64) {
 // FP32 tiles of 4 and 5 rows run the shared-stage kernel (measured at 128x128x200:
 // 32.4 and 34.3 us against 34.5 and 35.6 us for k_apply_haar); 6 rows and FP64 keep
 // k_apply_haar (the shared form spills at 6 rows in 128 registers).
-template <typename R, int RR, bool ANISO, int MODEV, bool SHIFT>
+template <typename R, int RR, bool ANISO, int MODEV, bool SHIFT, bool MASS>
 static void op_launch_one(const LaunchCfg& c, dim3 grid, const OpArgs<R>& a) {
     if constexpr (sizeof(R) == 4 && RR <= 5)
-        launch_kernel(k_apply_shared<R, RR, ANISO, MODEV, SHIFT>, grid, dim3(32 * kWarps), c.stream, a);
+        launch_kernel(k_apply_shared<R, RR, ANISO, MODEV, SHIFT, MASS>, grid, dim3(32 * kWarps), c.stream, a);
     else
-        launch_kernel(k_apply_haar<R, RR, ANISO, MODEV, SHIFT>, grid, dim3(32 * kWarps), c.stream, a);
+        launch_kernel(k_apply_haar<R, RR, ANISO, MODEV, SHIFT, MASS>, grid, dim3(32 * kWarps), c.stream, a);
 }
 
 template <typename R, int RR>
 static void op_launch_rows(const LaunchCfg& c, dim3 grid, const OpArgs<R>& a, bool aniso, int mode) {
-    const bool shift = a.dshift != nullptr;
-#define PLGPU_OP(MODEV)                                             \
-    if (mode == MODEV) {                                            \
-        if (aniso && shift)                                         \
-            op_launch_one<R, RR, true, MODEV, true>(c, grid, a);    \
-        else if (aniso)                                             \
-            op_launch_one<R, RR, true, MODEV, false>(c, grid, a);   \
-        else if (shift)                                             \
-            op_launch_one<R, RR, false, MODEV, true>(c, grid, a);   \
-        else                                                        \
-            op_launch_one<R, RR, false, MODEV, false>(c, grid, a);  \
-        return;                                                     \
+    // at most one capacity form: a lumped diagonal or the consistent element matrices
+    const int cap = a.cmass != nullptr ? 2 : a.dshift != nullptr ? 1 : 0;
+#define PLGPU_OP_A(MODEV, ANISOV)                                           \
+    if (cap == 2)                                                           \
+        op_launch_one<R, RR, ANISOV, MODEV, false, true>(c, grid, a);       \
+    else if (cap == 1)                                                      \
+        op_launch_one<R, RR, ANISOV, MODEV, true, false>(c, grid, a);       \
+    else                                                                    \
+        op_launch_one<R, RR, ANISOV, MODEV, false, false>(c, grid, a);
+#define PLGPU_OP(MODEV)              \
+    if (mode == MODEV) {             \
+        if (aniso) {                 \
+            PLGPU_OP_A(MODEV, true)  \
+        } else {                     \
+            PLGPU_OP_A(MODEV, false) \
+        }                            \
+        return;                      \
     }
     PLGPU_OP(MODE_CG)
     PLGPU_OP(MODE_RESID)
     PLGPU_OP(MODE_RHS)
     PLGPU_OP(MODE_MULT)
 #undef PLGPU_OP
+#undef PLGPU_OP_A
 }
 
 template <typename R>
 static void op_launch(const LaunchCfg& c, const GridT<R>& g, const R* zf, const R* zr, const R* x, R* y, const R* kxy,
                       const R* kz, bool aniso, const uint32_t* dmask, const R* rhs, double* partials, int mode,
-                      SolveCtl* ctl, const uint32_t* smask, int sslots, const R* dshift) {
+                      SolveCtl* ctl, const uint32_t* smask, int sslots, const R* dshift, const R* cmass) {
     constexpr bool fp64 = sizeof(R) == 8;
     dim3 grid;
     int zchunk;
     op_grid(c, g.n0, g.n1, g.n2, fp64, grid, zchunk);
-    OpArgs<R> a{g, x, y, kxy, kz, dmask, rhs, partials, ctl, zf, zr, zchunk, smask, sslots, dshift};
+    OpArgs<R> a{g, x, y, kxy, kz, dmask, rhs, partials, ctl, zf, zr, zchunk, smask, sslots, dshift, cmass};
     if constexpr (fp64) {
         op_launch_rows<R, 4>(c, grid, a, aniso, mode);
     } else {
@@ -603,14 +660,16 @@ static void op_launch(const LaunchCfg& c, const GridT<R>& g, const R* zf, const 
 void launch_operator(const LaunchCfg& c, const GridT<float>& g, const float* zf, const float* zr, const float* x,
                      float* y, const float* kxy, const float* kz, bool aniso, const uint32_t* dmask, const float* rhs,
                      double* partials, int mode, SolveCtl* ctl, const uint32_t* smask, int sslots,
-                     const float* dshift) {
-    op_launch<float>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, smask, sslots, dshift);
+                     const float* dshift, const float* cmass) {
+    op_launch<float>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, smask, sslots, dshift,
+                     cmass);
 }
 void launch_operator(const LaunchCfg& c, const GridT<double>& g, const double* zf, const double* zr, const double* x,
                      double* y, const double* kxy, const double* kz, bool aniso, const uint32_t* dmask,
                      const double* rhs, double* partials, int mode, SolveCtl* ctl, const uint32_t* smask,
-                     int sslots, const double* dshift) {
-    op_launch<double>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, smask, sslots, dshift);
+                     int sslots, const double* dshift, const double* cmass) {
+    op_launch<double>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, smask, sslots, dshift,
+                      cmass);
 }
 
 }  // namespace plgpu

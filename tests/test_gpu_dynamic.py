@@ -1,8 +1,8 @@
-"""Dynamic3D (theta-method time stepping, lumped heat capacity) on the GPU against the
-CPU oracle (oracle/dynamic3d.py, a restatement of solvers/thermal/dynamic/femT3d.cpp):
-temperatures within 1e-6 K after the same number of steps, the same elapsed time, for
-Crank-Nicolson, implicit Euler, periodic k(T) rebuilds and a second compute() that
-continues from the first.  Dirichlet nodes hold their values (the scheme the
+"""Dynamic3D (theta-method time stepping, lumped or consistent heat capacity) on the GPU
+against the CPU oracle (oracle/dynamic3d.py, a restatement of
+solvers/thermal/dynamic/femT3d.cpp): temperatures within 1e-6 K after the same number of
+steps, the same elapsed time, for Crank-Nicolson, implicit Euler, theta = 0.75, periodic
+k(T) rebuilds and a second compute() that continues from the first.  Dirichlet nodes hold their values (the scheme the
 reference's setMatrix prepares; its step loop lets them drift, see oracle/dynamic3d.py)."""
 import numpy as np
 import pytest
@@ -40,14 +40,17 @@ def _solver(s, cp, dens, order, **kw):
     return sv
 
 
-@pytest.mark.parametrize("theta,rebuild,algorithm", [(0.5, 0, "gpu-mixed"), (1.0, 0, "gpu-pcg"), (0.5, 3, "gpu-mixed")])
-def test_time_steps_match_oracle(theta, rebuild, algorithm):
+@pytest.mark.parametrize("theta,rebuild,algorithm,lumping", [
+    (0.5, 0, "gpu-mixed", True), (1.0, 0, "gpu-pcg", True), (0.5, 3, "gpu-mixed", True),
+    (0.5, 0, "gpu-mixed", False), (1.0, 2, "gpu-pcg", False), (0.75, 0, "gpu-mixed", False)])
+def test_time_steps_match_oracle(theta, rebuild, algorithm, lumping):
     s, cp, dens = _case()
     order = "201"
-    sv = _solver(s, cp, dens, order, timestep=0.2, methodparam=theta, rebuildfreq=rebuild, algorithm=algorithm)
+    sv = _solver(s, cp, dens, order, timestep=0.2, methodparam=theta, rebuildfreq=rebuild, algorithm=algorithm,
+                 lumping=lumping)
     sv.compute(2.0)
     p = O.from_structure(s, order=order, empty_elements="include")
-    To, elaps, steps = D.compute(p, 2.0, cp, dens, timestep=0.2, theta=theta, rebuildfreq=rebuild)
+    To, elaps, steps = D.compute(p, 2.0, cp, dens, timestep=0.2, theta=theta, lumping=lumping, rebuildfreq=rebuild)
     node_id, _ = O.masked_numbering(p)
     To_full = O.to_full(p, node_id, To)
     Tg = sv._full_temperature()

@@ -220,10 +220,12 @@ def test_heat_flux_of_slab_matches_power():
     assert np.allclose(flux[..., :2], 0.0, atol=1e-6 * total)
 
 
-def test_dynamic_oracle_reaches_the_static_state():
+@pytest.mark.parametrize("lumping", [True, False])
+def test_dynamic_oracle_reaches_the_static_state(lumping):
     """Implicit Euler with a timestep far beyond the diffusion time, rebuilding k(T) every
     step, is a Picard iteration of the static problem: it must land on the static
-    oracle's temperature (which itself stops at maxerr 0.05 K)."""
+    oracle's temperature (which itself stops at maxerr 0.05 K), with the lumped or the
+    consistent heat capacity."""
     from oracle import dynamic3d as D
     from plask_gb300 import structures as S
 
@@ -232,7 +234,25 @@ def test_dynamic_oracle_reaches_the_static_state():
     Ts, _, _ = O.compute(p, loops=0)
     cp = np.full(s.k300.size, 500.0)
     dens = np.full(s.k300.size, 5000.0)
-    Td, elaps, steps = D.compute(p, 10e9, cp, dens, timestep=1e9, theta=1.0, rebuildfreq=1, method="cholesky")
+    Td, elaps, steps = D.compute(p, 10e9, cp, dens, timestep=1e9, theta=1.0, lumping=lumping, rebuildfreq=1,
+                                 method="cholesky")
     node_id, _ = O.masked_numbering(p)
     assert steps == 11 and abs(elaps - 10e9) < 1e-3
     assert np.max(np.abs(O.to_full(p, node_id, Td) - Ts)) < 0.1
+
+
+def test_consistent_capacity_rows_sum_to_the_lumped_capacity():
+    """The consistent matrix c (8, 4, 2, 1)/27 per element (femT3d.cpp:203-226) has the
+    lumped capacity as its row sums."""
+    from oracle import dynamic3d as D
+    from plask_gb300 import structures as S
+
+    s = S.layered_c0(seed=22, n=(7, 6, 9))
+    p = O.from_structure(s, order="012", empty_elements="include")
+    numbering = O.masked_numbering(p)
+    cp = np.linspace(300.0, 900.0, s.k300.size)
+    dens = np.linspace(2000.0, 6000.0, s.k300.size)
+    Cl = D._mass(p, cp, dens, 0.1, True, numbering)
+    Cc = D._mass(p, cp, dens, 0.1, False, numbering)
+    np.testing.assert_allclose(np.asarray(Cc.sum(axis=1)).ravel(), Cl.diagonal(), rtol=1e-13)
+    assert abs(Cc - Cc.T).max() <= 1e-12 * abs(Cc).max()
