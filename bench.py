@@ -22,7 +22,7 @@ cpu_baseline  the reference's default iterative algorithm (IC + CG) restated
     python bench.py --workload sweep [--sweep-count 256]   # batched sweep line (not the default)
 
 The sweep line solves the uneven-size sweep (layered generator, 32..96 nodes per
-axis, source power 1e15..1e17 W/m^3): every structure one at a time, then all of
+axis, source power 1e15..1e16 W/m^3): every structure one at a time, then all of
 them batched (concurrent solves on separate streams) with the thread count and
 stencil grid policy the autotuner picks on a sample of 32 structures.
 """
