@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--workload", default="layered", choices=["layered", "sweep"])
     ap.add_argument("--sweep-count", type=int, default=256)
     ap.add_argument("--sweep-loops", type=int, default=30, help="outer-loop cap of every sweep solve")
+    ap.add_argument("--clocks-dir", default=None, help="directory that keeps the raw nvidia-smi clock samples")
     ap.add_argument("--operator-only", action="store_true",
                     help="only set up the case and time the operator kernel (for kernel profiling)")
     return ap.parse_args()
@@ -114,10 +115,16 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, directory=None):
         self.gpu = gpu_index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_rank{gpu_index}.csv"
+        # the raw samples go to `directory` when given (kept), else to a temporary file
+        if directory:
+            self.path = pathlib.Path(directory) / f"clocks_rank{gpu_index}.csv"
+        else:
+            import tempfile
+
+            self.path = pathlib.Path(tempfile.mkdtemp(prefix="plgpu_clocks_")) / f"clocks_rank{gpu_index}.csv"
 
     def start(self):
         try:
@@ -356,7 +363,7 @@ def main():
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    sampler = ClockSampler(dist.local)
+    sampler = ClockSampler(dist.local, args.clocks_dir)
     sampler.start()
     dist.barrier()
     torch.cuda.synchronize()
