@@ -288,10 +288,6 @@ struct plgpu_fem3d {
         cfg.op_rows = choose_op_rows(n[1]);
         cfg.vec_blocks = sm_count * 4;
         if (cfg.vec_blocks > kMaxPartialBlocks) cfg.vec_blocks = kMaxPartialBlocks;
-        // choose z-planes per operator block so that the block count stays within the partial slots
-        cfg.apply_planes = 1;
-        while (apply_blocks(cfg, n[0], n[1], n[2]) > kMaxPartialBlocks - 256) cfg.apply_planes *= 2;
-        while (apply_blocks(cfg, n[0], n[1], n[2]) > sm_count * 16 && cfg.apply_planes < 16) cfg.apply_planes *= 2;
 
         for (int d = 0; d < 3; ++d) {
             std::vector<double> h(n[d] - 1), r(n[d] - 1);

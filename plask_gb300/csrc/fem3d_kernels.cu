@@ -4,9 +4,8 @@
 //   k_thickness      ThermalFem3DSolver::onInitialize layer-run thickness  solvers/thermal/static/therm3d.cpp:81-113
 //   k_coef           per-element k(T) of setMatrix                          therm3d.cpp:208-220
 //   k_heat_load      element load vector f = 0.125e-18 V q                  therm3d.cpp:222-223, 239-240, 274
-//   k_apply_*        the assembled stiffness matrix times a vector, matrix-free
-//                    (K_e of therm3d.cpp:226-237 summed over elements, Dirichlet rows
-//                    as after BandMatrix::setBC, plask/common/fem/matrix.hpp:132-145)
+//   (the stiffness operator itself, K_e of therm3d.cpp:226-237 applied matrix-free,
+//   is in fem3d_operator.cu)
 //   k_surface        convective face terms of setBoundaries                  therm3d.cpp:141-168, 250-259
 //   k_cg_*           the linear solve that replaces dpbtrf/dpbtrs or NSPCG  cholesky_matrix.hpp:90-111,
 //                                                                            iterative_matrix.hpp:141-339
@@ -41,104 +40,6 @@ __device__ __forceinline__ void element_xyz(const GridT<R>& g, int e0, int e1, i
     X = kxy * g.r0[e0] * dy * dz;
     Y = kxy * dx * g.r1[e1] * dz;
     Z = kz * dx * dy * g.r2[e2];
-}
-
-// Entries of the trilinear-hex stiffness K_e: K[a][b] depends only on a ^ b (therm3d.cpp:227-237).
-template <typename R>
-__device__ __forceinline__ void element_g(R X, R Y, R Z, R (&gg)[8]) {
-    const R s = X + Y + Z;
-    const R c9 = R(1.0 / 9.0), c18 = R(1.0 / 18.0), c36 = R(1.0 / 36.0);
-    gg[0] = s * c9;
-    gg[1] = (Y + Z - R(2) * X) * c18;
-    gg[2] = (X + Z - R(2) * Y) * c18;
-    gg[4] = (X + Y - R(2) * Z) * c18;
-    gg[3] = (Z - R(2) * X - R(2) * Y) * c36;
-    gg[5] = (Y - R(2) * X - R(2) * Z) * c36;
-    gg[6] = (X - R(2) * Y - R(2) * Z) * c36;
-    gg[7] = -s * c36;
-}
-
-// ----------------------------------------------------------------------------------------
-// operator application (node-gather form)
-//
-// MODE_CG:    y = A x, Dirichlet rows y = x; per-block partial of (x, y)
-// MODE_RESID: y = rhs - A x with Dirichlet neighbours of x masked to zero,
-//             Dirichlet rows y = rhs - x
-// MODE_RHS:   y = rhs - A x with the full (unmasked) operator; Dirichlet rows
-//             are overwritten afterwards by k_set_dirichlet
-
-template <typename R, bool ANISO, int MODE>
-__global__ void __launch_bounds__(256) k_apply_gather(const GridT<R> g, const R* __restrict__ x, R* __restrict__ y,
-                                                      const R* __restrict__ kxy, const R* __restrict__ kzp,
-                                                      const uint32_t* __restrict__ dmask,
-                                                      const R* __restrict__ rhs, double* __restrict__ partials,
-                                                      int planes, const SolveCtl* __restrict__ ctl) {
-    if (MODE == MODE_CG && ctl != nullptr && ctl->status != SOLVE_RUNNING) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k0 = blockIdx.z * planes;
-    const int n0 = g.n0, n1 = g.n1, n2 = g.n2;
-    const int k1 = min(k0 + planes, n2);
-    const long long s1 = n0, s2 = (long long)n0 * n1;
-    double dot = 0.0;
-    if (i < n0 && j < n1) {
-        for (int k = k0; k < k1; ++k) {
-            const long long n = i + s1 * j + s2 * k;
-            const bool isd = is_dir(dmask, n);
-            R out;
-            if (MODE == MODE_CG && isd) {
-                out = x[n];
-            } else if (MODE == MODE_RESID && isd) {
-                out = rhs[n] - x[n];
-            } else {
-                R xv[27];
-#pragma unroll
-                for (int dk = 0; dk < 3; ++dk)
-#pragma unroll
-                    for (int dj = 0; dj < 3; ++dj)
-#pragma unroll
-                        for (int di = 0; di < 3; ++di) {
-                            const int ii = i + di - 1, jj = j + dj - 1, kk = k + dk - 1;
-                            R v = R(0);
-                            if (ii >= 0 && ii < n0 && jj >= 0 && jj < n1 && kk >= 0 && kk < n2) {
-                                const long long m = ii + s1 * jj + s2 * kk;
-                                v = x[m];
-                                if (MODE == MODE_RESID && is_dir(dmask, m)) v = R(0);
-                            }
-                            xv[di + 3 * (dj + 3 * dk)] = v;
-                        }
-                R acc = R(0);
-#pragma unroll
-                for (int ek = 0; ek < 2; ++ek)
-#pragma unroll
-                    for (int ej = 0; ej < 2; ++ej)
-#pragma unroll
-                        for (int ei = 0; ei < 2; ++ei) {
-                            const int e0 = i - 1 + ei, e1 = j - 1 + ej, e2 = k - 1 + ek;
-                            if (e0 < 0 || e0 >= n0 - 1 || e1 < 0 || e1 >= n1 - 1 || e2 < 0 || e2 >= n2 - 1) continue;
-                            const long long e = e0 + s1 * e1 + s2 * e2;
-                            const R kk = kxy[e];
-                            const R kv = ANISO ? kzp[e] : kk;
-                            R X, Y, Z, gg[8];
-                            element_xyz(g, e0, e1, e2, kk, kv, X, Y, Z);
-                            element_g(X, Y, Z, gg);
-                            const int a = (1 - ei) | ((1 - ej) << 1) | ((1 - ek) << 2);
-#pragma unroll
-                            for (int b = 0; b < 8; ++b) {
-                                const int bi = b & 1, bj = (b >> 1) & 1, bk = b >> 2;
-                                acc += gg[a ^ b] * xv[(ei + bi) + 3 * ((ej + bj) + 3 * (ek + bk))];
-                            }
-                        }
-                out = (MODE == MODE_CG) ? acc : R(rhs[n] - acc);
-            }
-            y[n] = out;
-            if (MODE == MODE_CG) dot += (double)x[n] * (double)out;
-        }
-    }
-    if (MODE == MODE_CG) {
-        double v[1] = {dot};
-        write_partial<1, OpSum>(v, partials, linear_bid());
-    }
 }
 
 // Convective face terms: a sparse symmetric operator on free nodes.
@@ -819,46 +720,6 @@ static inline int grid_for(long long n, int threads, int cap) {
     long long b = (n + threads - 1) / threads;
     if (b < 1) b = 1;
     return (int)(b < cap ? b : cap);
-}
-
-template <typename R>
-static void launch_apply_any(const LaunchCfg& c, const GridT<R>& g, const R* x, R* y, const R* kxy, const R* kz,
-                             bool aniso, const uint32_t* dmask, const R* rhs, double* partials, int mode,
-                             const SolveCtl* ctl, int* nblocks_out) {
-    dim3 block(32, 8, 1);
-    const int planes = c.apply_planes;
-    dim3 grid((g.n0 + 31) / 32, (g.n1 + 7) / 8, (g.n2 + planes - 1) / planes);
-    if (nblocks_out) *nblocks_out = (int)(grid.x * grid.y * grid.z);
-#define PLGPU_APPLY_CASE(MODEV)                                                                                          \
-    if (mode == MODEV) {                                                                                                 \
-        if (aniso)                                                                                                       \
-            launch(k_apply_gather<R, true, MODEV>, grid, block, c.stream, g, x, y, kxy, kz, dmask, rhs, partials, planes,  \
-                                                                         ctl);                                           \
-        else                                                                                                             \
-            launch(k_apply_gather<R, false, MODEV>, grid, block, c.stream, g, x, y, kxy, kz, dmask, rhs, partials, planes, \
-                                                                          ctl);                                          \
-        return;                                                                                                          \
-    }
-    PLGPU_APPLY_CASE(MODE_CG)
-    PLGPU_APPLY_CASE(MODE_RESID)
-    PLGPU_APPLY_CASE(MODE_RHS)
-#undef PLGPU_APPLY_CASE
-}
-
-int apply_blocks(const LaunchCfg& c, int n0, int n1, int n2) {
-    const int planes = c.apply_planes;
-    return ((n0 + 31) / 32) * ((n1 + 7) / 8) * ((n2 + planes - 1) / planes);
-}
-
-void launch_apply(const LaunchCfg& c, const GridT<double>& g, const double* x, double* y, const double* kxy,
-                  const double* kz, bool aniso, const uint32_t* dmask, const double* rhs, double* partials, int mode,
-                  const SolveCtl* ctl) {
-    launch_apply_any<double>(c, g, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, nullptr);
-}
-void launch_apply(const LaunchCfg& c, const GridT<float>& g, const float* x, float* y, const float* kxy,
-                  const float* kz, bool aniso, const uint32_t* dmask, const float* rhs, double* partials, int mode,
-                  const SolveCtl* ctl) {
-    launch_apply_any<float>(c, g, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, nullptr);
 }
 
 template <typename R>

@@ -37,7 +37,6 @@ struct LaunchCfg {
     cudaStream_t stream;
     int sm_count;      // streaming multiprocessors of the device
     int vec_blocks;    // grid size cap of streaming kernels (a multiple of the SM count)
-    int apply_planes;  // z-planes per block of the operator kernels
     int op_share;      // the stencil kernel's grid aims at 1/op_share of the GPU's resident
                        // blocks (1: the whole GPU; >1 when several solves run concurrently)
     int op_rows;       // FP32 stencil kernel: output rows per thread (4, 5 or 6), chosen per mesh
@@ -46,15 +45,8 @@ struct LaunchCfg {
 long long launch_count();         // kernels launched by this library so far (all handles)
 long long thread_launch_count();  // kernels launched so far from the calling host thread
 void prime_launch_shapes();  // occupancy-derived grid sizes, queried before any graph capture
-int apply_blocks(const LaunchCfg& c, int n0, int n1, int n2);
 int vec_blocks(const LaunchCfg& c, long long N);
 
-void launch_apply(const LaunchCfg& c, const GridT<double>& g, const double* x, double* y, const double* kxy,
-                  const double* kz, bool aniso, const uint32_t* dmask, const double* rhs, double* partials, int mode,
-                  const SolveCtl* ctl);
-void launch_apply(const LaunchCfg& c, const GridT<float>& g, const float* x, float* y, const float* kxy,
-                  const float* kz, bool aniso, const uint32_t* dmask, const float* rhs, double* partials, int mode,
-                  const SolveCtl* ctl);
 // Optimised operator (fem3d_operator.cu).  zf[k] = dz_k / 48, zr[k] = 1 / (48 dz_k).
 // number of blocks (= partial-sum slots written in MODE_CG) of one operator launch
 int op_blocks(const LaunchCfg& c, int n0, int n1, int n2, bool fp64);
