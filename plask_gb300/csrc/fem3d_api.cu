@@ -1082,7 +1082,8 @@ struct plgpu_fem3d {
         const double bn = std::sqrt(c0.red[2]);
         relres = bn > 0 ? std::sqrt(c0.red[3]) / bn : 0.0;
         iters = 0;
-        if (!std::isfinite(relres)) {
+        // a NaN or Inf in b or A T fails every comparison: test the norms themselves
+        if (!std::isfinite(c0.red[2]) || !std::isfinite(c0.red[3]) || !std::isfinite(relres)) {
             status = SOLVE_NONFINITE;
             return;
         }
@@ -1106,6 +1107,10 @@ struct plgpu_fem3d {
             launch_norm2(cfg, N, r64v.as<double>(), nullptr, part, ctl, 3, w);
             const SolveCtl c = read_ctl();
             relres = bn > 0 ? std::sqrt(c.red[3]) / bn : 0.0;
+            if (!std::isfinite(c.red[3])) {
+                status = SOLVE_NONFINITE;
+                return;
+            }
             if (relres <= 2.0 * target) {
                 status = SOLVE_CONVERGED;
                 return;
@@ -1147,7 +1152,7 @@ struct plgpu_fem3d {
             SolveCtl c = read_ctl();
             ++refinements;
             relres = c.red[2] > 0 ? std::sqrt(c.red[3] / c.red[2]) : 0.0;
-            if (!std::isfinite(relres)) {
+            if (!std::isfinite(c.red[2]) || !std::isfinite(c.red[3]) || !std::isfinite(relres)) {
                 status = SOLVE_NONFINITE;
                 return;
             }
