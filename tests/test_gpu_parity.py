@@ -73,3 +73,46 @@ def test_heat_flux_conductivity_thickness_match_oracle():
     # k = k300 (300/T)^p: |dk|/k <= p |dT| / T <= 1.5 * 1e-6 K / 300 K = 5e-9 at the temperature tolerance
     assert np.allclose(k[..., 0].ravel(), kxy, rtol=1e-8)
     assert np.allclose(k[..., 1].ravel(), kz, rtol=1e-8)
+
+
+def _mesa_with_faces(seed, n):
+    """A layered structure whose top layers are etched into a mesa (an EMPTY material
+    around it: masked mesh), with heat flux, convection and radiation on several faces."""
+    s = S.layered_c0(seed=seed, n=n, power=1e15)
+    n_mat = s.k300.size
+    s.k300 = np.append(s.k300, 0.026)
+    s.p = np.append(s.p, 0.0)
+    s.kz_ratio = np.append(s.kz_ratio, 1.0)
+    s.hexp = np.append(s.hexp, 0.0)
+    s.empty = np.append(s.empty, True)
+    ne2 = s.mat.shape[0]
+    xm = 0.5 * (s.axes[0][1:] + s.axes[0][:-1])
+    ym = 0.5 * (s.axes[1][1:] + s.axes[1][:-1])
+    outside = (xm[None, :] > 20.0) | (ym[:, None] > 20.0)
+    mat = s.mat.copy()
+    for k in range(ne2 - 4, ne2):
+        mat[k][outside] = n_mat
+    s.mat = mat
+    s.heatflux = [("left", -2e3)]
+    s.convection = [("top", 80.0, 295.0), ("right", 40.0, 300.0)]
+    s.radiation = [("front", 0.7, 310.0), ("top", 0.5, 280.0)]
+    return s
+
+
+@pytest.mark.parametrize("algorithm", ["gpu-mixed", "gpu-pcg"])
+@pytest.mark.parametrize("order", ["201", "012"])
+def test_masked_mesh_with_face_conditions_matches_oracle(order, algorithm):
+    """Full compute() with a masked mesh and heat-flux, convective and radiative faces in
+    the reference's placement (face terms on element corners 0-3, radiation reading the
+    temperatures of global nodes 0-7), against the oracle."""
+    s = _mesa_with_faces(seed=12, n=(12, 11, 16))
+    p = O.from_structure(s, order=order)
+    To, tot_o, rec = O.compute(p)
+    sv, T, tot = _gpu(s, order, algorithm)
+    node_id, n_act = O.masked_numbering(p)
+    act = node_id >= 0
+    assert n_act < act.size  # the etched corner drops nodes
+    assert sv.stats["loops"] == len(rec)
+    assert np.all(np.isnan(T[~act]))
+    assert np.max(np.abs(T[act] - To[act])) <= TOL_T
+    assert abs(tot - tot_o) <= TOL_T
