@@ -175,6 +175,27 @@ class Provider:
         return self._fn(mesh, interpolation)
 
 
+def _nearest_axis(axis, x):
+    """Index of the nearest node, the lower one on a tie (find_nearest_binary,
+    plask/utils/stl.hpp:59-80)."""
+    lb = np.searchsorted(axis, x, side="left")
+    hi = np.minimum(lb, axis.size - 1)
+    lo = np.maximum(lb - 1, 0)
+    take_lo = (lb == axis.size) | ((lb > 0) & (x - axis[lo] <= axis[hi] - x))
+    return np.where(take_lo, lo, hi)
+
+
+def _element_axis(axis, x):
+    """Index of the element holding x, clamped to the mesh (findUpIndex - 1)."""
+    return np.clip(np.searchsorted(axis, x, side="right") - 1, 0, axis.size - 2)
+
+
+def _check_interpolation(method):
+    if method not in ("linear", "nearest", "default", None):
+        raise BadInput(-1, f"unsupported interpolation {method!r} (linear or nearest)")
+    return "linear" if method in ("default", None) else method
+
+
 def _interp_axis(axis, x):
     """Bracketing indices and weights of points x on an increasing axis (clamped)."""
     i = np.clip(np.searchsorted(axis, x, side="right") - 1, 0, axis.size - 2)
@@ -421,6 +442,11 @@ class Static3D:
         if dst_mesh is None:
             return T
         pts = _points(dst_mesh)
+        if _check_interpolation(interpolation) == "nearest":
+            # the nearest node (rectilinear3d.hpp:853-860); masked-out nodes read 300 K
+            i0, i1, i2 = (_nearest_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
+            out = T[i2, i1, i0]
+            return np.where(np.isnan(out), 300.0, out)
         return _trilinear(self._mesh.axes, T, pts, fill=300.0)
 
     def heat_fluxes(self):
@@ -440,6 +466,15 @@ class Static3D:
             return q
         mids = [0.5 * (a[1:] + a[:-1]) for a in self._mesh.axes]
         pts = _points(dst_mesh)
+        if _check_interpolation(interpolation) == "nearest":
+            # the element holding the point (the reference's element-mesh lookup,
+            # rectilinear3d.hpp:282-297, searches axis 0 for the second coordinate as well;
+            # that slip is not reproduced)
+            i0, i1, i2 = (_element_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
+            out = q[i2, i1, i0].copy()
+            inside = np.all([(pts[:, d] >= a[0]) & (pts[:, d] <= a[-1]) for d, a in enumerate(self._mesh.axes)], axis=0)
+            out[~inside] = 0.0
+            return out
         out = np.stack([_trilinear(mids, q[..., c], pts, fill=0.0, clamp=True, box=self._mesh.axes)
                         for c in range(3)], axis=-1)
         return out

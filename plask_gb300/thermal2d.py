@@ -19,7 +19,8 @@ import numpy as np
 
 from . import _native
 from .mesh import RectangularMesh2D, mesh_index2d, to_mesh_order2d
-from .thermal import BadInput, BoundaryConditions, IterativeParams, MaterialTable, Provider
+from .thermal import (BadInput, BoundaryConditions, IterativeParams, MaterialTable, Provider, _check_interpolation,
+                      _element_axis, _nearest_axis)
 
 log = logging.getLogger("plask_gb300.thermal2d")
 
@@ -311,7 +312,12 @@ class Static2D:
         T = self._full_temperature()
         if dst_mesh is None:
             return T
-        return _bilinear(self._mesh.axes, T, _points2d(dst_mesh), fill=300.0)
+        pts = _points2d(dst_mesh)
+        if _check_interpolation(interpolation) == "nearest":
+            i0, i1 = (_nearest_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
+            out = T[i1, i0]
+            return np.where(np.isnan(out), 300.0, out)
+        return _bilinear(self._mesh.axes, T, pts, fill=300.0)
 
     def heat_fluxes(self):
         """Per-element heat flux [W/m^2], canonical (ne1, ne0, 2) (saveHeatFluxes)."""
@@ -330,6 +336,12 @@ class Static2D:
             return q
         mids = [0.5 * (a[1:] + a[:-1]) for a in self._mesh.axes]
         pts = _points2d(dst_mesh)
+        if _check_interpolation(interpolation) == "nearest":
+            i0, i1 = (_element_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
+            out = q[i1, i0].copy()
+            inside = np.all([(pts[:, d] >= a[0]) & (pts[:, d] <= a[-1]) for d, a in enumerate(self._mesh.axes)], axis=0)
+            out[~inside] = 0.0
+            return out
         return np.stack([_bilinear(mids, q[..., c], pts, fill=0.0, box=self._mesh.axes) for c in range(2)], axis=-1)
 
     def _get_conductivity(self, dst_mesh, interpolation="linear"):

@@ -148,3 +148,21 @@ def test_time_stepping_is_3d_only():
     sv.initialize()
     with pytest.raises(_native.BadInput):
         sv._fem.set_dynamic(np.ones(s.k300.size), np.ones(s.k300.size))
+
+
+@pytest.mark.parametrize("cls", [T2.Static2D, T2.StaticCyl])
+def test_nearest_interpolation_of_providers(cls):
+    s = S.layered_2d(seed=61, n=(20, 26))
+    sv = T2.solver_for_structure2d(s, cls=cls, ordering="10")
+    sv.compute()
+    T = sv._full_temperature()
+    x0, x1 = sv.mesh.axes
+    # at the nodes, nearest and linear give the nodal temperature
+    pts = np.array([[x0[3], x1[5]], [x0[-1], x1[0]]])
+    np.testing.assert_allclose(sv.outTemperature(pts, "nearest"), [T[5, 3], T[0, -1]], rtol=0, atol=0)
+    # just right of a node the nearest node is that node
+    p = np.array([[x0[3] + 0.25 * (x0[4] - x0[3]), x1[5]]])
+    assert sv.outTemperature(p, "nearest")[0] == T[5, 3]
+    q = sv.heat_fluxes()
+    mid = np.array([[0.5 * (x0[2] + x0[3]), 0.5 * (x1[7] + x1[8])]])
+    np.testing.assert_allclose(sv.outHeatFlux(mid, "nearest")[0], q[7, 2])

@@ -1,0 +1,26 @@
+"""Provider helpers on the CPU: the nearest-node rule of PLaSK's rectilinear meshes
+(find_nearest_binary, plask/utils/stl.hpp:59-80: the lower node on a tie, clamped to the
+axis) and the element lookup (findUpIndex - 1, clamped)."""
+import numpy as np
+import pytest
+
+from plask_gb300.thermal import BadInput, _check_interpolation, _element_axis, _nearest_axis
+
+
+def test_nearest_node_rule():
+    a = np.array([0.0, 1.0, 3.0, 4.0])
+    x = np.array([-1.0, 0.0, 0.5, 0.6, 2.0, 2.1, 3.5, 5.0])
+    assert list(_nearest_axis(a, x)) == [0, 0, 0, 1, 1, 2, 2, 3]
+
+
+def test_element_lookup():
+    a = np.array([0.0, 1.0, 3.0, 4.0])
+    x = np.array([-1.0, 0.0, 0.5, 1.0, 3.9, 4.0, 5.0])
+    assert list(_element_axis(a, x)) == [0, 0, 0, 1, 2, 2, 2]
+
+
+def test_interpolation_names():
+    assert _check_interpolation("default") == "linear"
+    assert _check_interpolation("nearest") == "nearest"
+    with pytest.raises(BadInput):
+        _check_interpolation("spline")
