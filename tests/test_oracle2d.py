@@ -154,3 +154,40 @@ def test_convective_edge_terms_follow_the_reference_scaling():
         assert dA[t0, t1] == pytest.approx(scale * 14.0 * 2.0 / 12.0)
         assert dA[t1, t2] == pytest.approx(scale * 14.0 * 3.0 / 12.0)
         assert F[t1] - F0[t1] == pytest.approx(0.5e-6 * (2.0 + 3.0) * 7.0 * 290.0)
+
+
+@pytest.mark.parametrize("geometry", ["cartesian", "cylindrical"])
+@pytest.mark.parametrize("lumping", [True, False])
+def test_dynamic2d_oracle_reaches_the_static_state(geometry, lumping):
+    """Implicit Euler with a timestep far beyond the diffusion time, rebuilding k(T) every
+    step, lands on the static 2D oracle's answer (solvers/thermal/dynamic/femT2d.cpp)."""
+    from oracle import dynamic2d as D2
+
+    s = S.layered_2d(seed=7, n=(14, 18))
+    mats = O3.Materials(s.k300, s.p, s.kz_ratio, s.hexp, s.empty)
+    bottom = np.zeros((len(s.axes[1]), len(s.axes[0])), bool)
+    bottom[0] = True
+    p = O2.Problem2D(axes=s.axes, mat=s.mat, materials=mats, heat=s.heat, geometry=geometry,
+                     temperature=[(bottom, 300.0)], order="01")
+    Ts, _, _ = O2.compute(p)
+    cp = np.full(s.k300.size, 500.0)
+    dens = np.full(s.k300.size, 5000.0)
+    Td, elaps, steps = D2.compute(p, 10e9, cp, dens, timestep=1e9, theta=1.0, lumping=lumping, rebuildfreq=1)
+    node_id, _ = O2.masked_numbering(p)
+    assert steps == 11
+    assert np.max(np.abs(O2.to_full(p, node_id, Td) - Ts)) < 0.1
+
+
+def test_dynamic2d_consistent_capacity_rows_sum_to_lumped():
+    from oracle import dynamic2d as D2
+
+    s = S.layered_2d(seed=8, n=(9, 11))
+    mats = O3.Materials(s.k300, s.p, s.kz_ratio, s.hexp, s.empty)
+    for geometry in ("cartesian", "cylindrical"):
+        p = O2.Problem2D(axes=s.axes, mat=s.mat, materials=mats, heat=s.heat, geometry=geometry)
+        num = O2.masked_numbering(p)
+        cp = np.linspace(300.0, 900.0, s.k300.size)
+        dens = np.linspace(2000.0, 6000.0, s.k300.size)
+        Cl = D2._mass(p, cp, dens, 0.1, True, num)
+        Cc = D2._mass(p, cp, dens, 0.1, False, num)
+        np.testing.assert_allclose(np.asarray(Cc.sum(axis=1)).ravel(), Cl.diagonal(), rtol=1e-13)
