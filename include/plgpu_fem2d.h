@@ -22,8 +22,13 @@
  *     its load term carries (therm2d.cpp:242-255, 367-392), and in the cylindrical
  *     form it is weighted by the element's midpoint radius once more
  *     (therm2d.cpp:410-420); bc_compat = 0 applies 1e-6 len and a single radius weight.
- *   - Time stepping (plgpu_fem3d_set_dynamic) and the learned preconditioner are 3D only
- *     and return PLGPU_ERR_ARG on a 2D handle.
+ *   - Time stepping (plgpu_fem3d_set_dynamic, plgpu_fem3d_compute_dynamic) is PLaSK's
+ *     thermal.dynamic.Dynamic2D / DynamicCyl (solvers/thermal/dynamic/femT2d.cpp): the
+ *     capacity per element corner is c = cp dens 0.25e-3 w h / timestep (times the
+ *     midpoint radius in the cylindrical form, femT2d.cpp:167, 298), lumped onto the
+ *     diagonal or, with lumping 0, the consistent matrix c (4, 2, 1) / 9 by corner
+ *     distance (femT2d.cpp:199-233).
+ *   - The learned preconditioner is 3D only and returns PLGPU_ERR_ARG on a 2D handle.
  * Units as in plgpu_fem3d.h; the 2D system is per metre of depth (Cartesian) or per
  * radian with r in micrometres (cylindrical), as in the reference.
  */

@@ -243,7 +243,8 @@ int plgpu_fem3d_set_log_callback(plgpu_fem3d* h, void (*cb)(void* user, int leve
 
 /* ---------------------------------------------------------------------------------
    Time stepping: PLaSK's thermal.dynamic.Dynamic3D (solvers/thermal/dynamic/femT3d.cpp)
-   on the same handle, mesh, materials, heat and temperature conditions. */
+   on the same handle, mesh, materials, heat and temperature conditions (on a 2D handle
+   Dynamic2D / DynamicCyl, femT2d.cpp: plgpu_fem2d.h). */
 
 /* Heat capacity cp [J/(kg K)] and density dens [kg/m^3] per material, timestep [ns],
    methodparam theta (0.5 Crank-Nicolson, 0 explicit, 1 implicit), lumping (nonzero:

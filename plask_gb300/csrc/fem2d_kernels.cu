@@ -48,6 +48,8 @@ struct Op2dArgs {
     SolveCtl* ctl;
     const uint32_t* smask;
     int sslots;
+    const R* dshift;  // lumped heat capacity per node (time steps), or nullptr
+    const R* cmass;   // consistent heat capacity: corner capacity c per element, or nullptr
 };
 
 // X and Y of element (ie, je); zero outside the mesh (padding slots hold zero k)
@@ -68,7 +70,9 @@ __device__ __forceinline__ void element_xy(const Op2dArgs<R>& a, int ie, int je,
     }
 }
 
-template <typename R, int MODE>
+// CAP: 0 none, 1 the lumped capacity a.dshift on the diagonal, 2 the consistent capacity
+// c (M (x) M), M = [[2,1],[1,2]] / 3, of every element (corner weights 4/9, 2/9, 1/9)
+template <typename R, int MODE, int CAP>
 __global__ void __launch_bounds__(256) k_apply2d(const Op2dArgs<R> a) {
     if (MODE == MODE_CG && a.ctl->status != SOLVE_RUNNING) return;
     const int n0 = a.g.n0, n1 = a.g.n1;
@@ -106,7 +110,15 @@ __global__ void __launch_bounds__(256) k_apply2d(const Op2dArgs<R> a) {
                 const R xn = xv[1][1 + sx], yn = xv[1 + sy][1], dn = xv[1 + sy][1 + sx];
                 // X/6 (2 (x0 - xn) + (yn - dn)) + Y/6 (2 (x0 - yn) + (xn - dn))
                 acc += (X * (R(2) * (x0 - xn) + (yn - dn)) + Y * (R(2) * (x0 - yn) + (xn - dn))) * R(1.0 / 6.0);
+                if constexpr (CAP == 2) {
+                    const int ie = i - ca, je = j - cb;
+                    if (ie >= 0 && je >= 0 && ie < n0 - 1 && je < n1 - 1) {
+                        const R c = a.cmass[ie + (long long)n0 * je];
+                        acc += c * (R(4.0 / 9.0) * x0 + R(2.0 / 9.0) * (xn + yn) + R(1.0 / 9.0) * dn);
+                    }
+                }
             }
+        if constexpr (CAP == 1) acc += a.dshift[n] * x0;
         R out;
         if (MODE == MODE_CG) {
             out = acc;
@@ -192,7 +204,7 @@ __global__ void __launch_bounds__(256) k_coef2d(int n0, int n1, const double* __
 
 __global__ void __launch_bounds__(256) k_diag2d(const GridT<double> g, const double* __restrict__ rmid,
                                                 const double* __restrict__ kx, const double* __restrict__ ky,
-                                                double* __restrict__ diag) {
+                                                const double* __restrict__ shift, double* __restrict__ diag) {
     const int n0 = g.n0, n1 = g.n1;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < g.N; n += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(n % n0), j = (int)(n / n0);
@@ -209,7 +221,7 @@ __global__ void __launch_bounds__(256) k_diag2d(const GridT<double> g, const dou
             }
             d += (X + Y) * (1.0 / 3.0);
         }
-        diag[n] = d;
+        diag[n] = shift ? d + shift[n] : d;
     }
 }
 
@@ -230,6 +242,59 @@ __global__ void __launch_bounds__(256) k_heat_load2d(const GridT<double> g, cons
             f += v;
         }
         F[n] = f;
+    }
+}
+
+// Heat capacity of the time-stepping solvers (femT2d.cpp:167, 298): per element corner
+// c = cp dens 0.25e-3 w h / timestep (times the midpoint radius in the cylindrical form).
+__device__ __forceinline__ double corner_capacity(const GridT<double>& g, const double* rmid, int ie, int je, int m,
+                                                  const double* cp, const double* dens, double timestep) {
+    if (rmid)
+        return cp[m] * dens[m] * 0.25 * 1e-12 * rmid[ie] * g.h1[je] * g.h0[ie] / timestep / 1e-9;
+    return cp[m] * dens[m] * 0.25 * 1e-12 * g.h1[je] * g.h0[ie] / timestep / 1e-9;
+}
+
+// lumped capacity per node: weight times the sum of c over the node's active elements
+__global__ void __launch_bounds__(256) k_lumped_mass2d(const GridT<double> g, const double* __restrict__ rmid,
+                                                       const int* __restrict__ mat, const uint8_t* __restrict__ excl,
+                                                       const double* __restrict__ cp, const double* __restrict__ dens,
+                                                       double timestep, double weight, double* __restrict__ c64,
+                                                       float* __restrict__ c32) {
+    const int n0 = g.n0, n1 = g.n1;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < g.N; n += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(n % n0), j = (int)(n / n0);
+        double c = 0.0;
+        for (int k = 0; k < 4; ++k) {  // the (up to 4) elements around the node, fixed order
+            const int ie = i - 1 + (k & 1), je = j - 1 + (k >> 1);
+            if (ie < 0 || je < 0 || ie >= n0 - 1 || je >= n1 - 1) continue;
+            const int m = mat[ie + (long long)n0 * je];
+            if (excl[m]) continue;
+            c += corner_capacity(g, rmid, ie, je, m, cp, dens, timestep);
+        }
+        c64[n] = weight * c;
+        if (c32) c32[n] = (float)(weight * c);
+    }
+}
+
+// corner capacity per element (padded layout; 0 for padding and excluded elements), and -c
+__global__ void __launch_bounds__(256) k_elem_capacity2d(const GridT<double> g, const double* __restrict__ rmid,
+                                                         const int* __restrict__ mat,
+                                                         const uint8_t* __restrict__ excl,
+                                                         const double* __restrict__ cp,
+                                                         const double* __restrict__ dens, double timestep,
+                                                         double* __restrict__ c64, float* __restrict__ c32,
+                                                         double* __restrict__ cneg) {
+    const int n0 = g.n0, n1 = g.n1;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < g.N; e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n0), j = (int)(e / n0);
+        double c = 0.0;
+        if (i < n0 - 1 && j < n1 - 1) {
+            const int m = mat[e];
+            if (!excl[m]) c = corner_capacity(g, rmid, i, j, m, cp, dens, timestep);
+        }
+        c64[e] = c;
+        c32[e] = (float)c;
+        cneg[e] = -c;
     }
 }
 
@@ -282,18 +347,28 @@ int grid_cap(long long n, int threads, int cap) {
     return (int)(b < cap ? b : cap);
 }
 
+template <typename R, int CAP>
+void operator2d_cap(const LaunchCfg& c, const Op2dArgs<R>& a, int mode) {
+    const int blocks = op2d_blocks(c, a.g.N);
+    switch (mode) {
+        case MODE_CG: launch_kernel(k_apply2d<R, MODE_CG, CAP>, blocks, 256, c.stream, a); break;
+        case MODE_RESID: launch_kernel(k_apply2d<R, MODE_RESID, CAP>, blocks, 256, c.stream, a); break;
+        case MODE_RHS: launch_kernel(k_apply2d<R, MODE_RHS, CAP>, blocks, 256, c.stream, a); break;
+        default: launch_kernel(k_apply2d<R, MODE_MULT, CAP>, blocks, 256, c.stream, a); break;
+    }
+}
+
 template <typename R>
 void operator2d_any(const LaunchCfg& c, const GridT<R>& g, const R* rmid, const R* x, R* y, const R* kx, const R* ky,
                     const uint32_t* dmask, const R* rhs, double* partials, int mode, SolveCtl* ctl,
-                    const uint32_t* smask, int sslots) {
-    const Op2dArgs<R> a{g, rmid, x, y, kx, ky, dmask, rhs, partials, ctl, smask, sslots};
-    const int blocks = op2d_blocks(c, g.N);
-    switch (mode) {
-        case MODE_CG: launch_kernel(k_apply2d<R, MODE_CG>, blocks, 256, c.stream, a); break;
-        case MODE_RESID: launch_kernel(k_apply2d<R, MODE_RESID>, blocks, 256, c.stream, a); break;
-        case MODE_RHS: launch_kernel(k_apply2d<R, MODE_RHS>, blocks, 256, c.stream, a); break;
-        default: launch_kernel(k_apply2d<R, MODE_MULT>, blocks, 256, c.stream, a); break;
-    }
+                    const uint32_t* smask, int sslots, const R* dshift, const R* cmass) {
+    const Op2dArgs<R> a{g, rmid, x, y, kx, ky, dmask, rhs, partials, ctl, smask, sslots, dshift, cmass};
+    if (cmass)
+        operator2d_cap<R, 2>(c, a, mode);
+    else if (dshift)
+        operator2d_cap<R, 1>(c, a, mode);
+    else
+        operator2d_cap<R, 0>(c, a, mode);
 }
 
 }  // namespace
@@ -305,13 +380,15 @@ int op2d_blocks(const LaunchCfg& c, long long N) {
 
 void launch_operator2d(const LaunchCfg& c, const GridT<double>& g, const double* rmid, const double* x, double* y,
                        const double* kx, const double* ky, const uint32_t* dmask, const double* rhs,
-                       double* partials, int mode, SolveCtl* ctl, const uint32_t* smask, int sslots) {
-    operator2d_any<double>(c, g, rmid, x, y, kx, ky, dmask, rhs, partials, mode, ctl, smask, sslots);
+                       double* partials, int mode, SolveCtl* ctl, const uint32_t* smask, int sslots,
+                       const double* dshift, const double* cmass) {
+    operator2d_any<double>(c, g, rmid, x, y, kx, ky, dmask, rhs, partials, mode, ctl, smask, sslots, dshift, cmass);
 }
 void launch_operator2d(const LaunchCfg& c, const GridT<float>& g, const float* rmid, const float* x, float* y,
                        const float* kx, const float* ky, const uint32_t* dmask, const float* rhs, double* partials,
-                       int mode, SolveCtl* ctl, const uint32_t* smask, int sslots) {
-    operator2d_any<float>(c, g, rmid, x, y, kx, ky, dmask, rhs, partials, mode, ctl, smask, sslots);
+                       int mode, SolveCtl* ctl, const uint32_t* smask, int sslots, const float* dshift,
+                       const float* cmass) {
+    operator2d_any<float>(c, g, rmid, x, y, kx, ky, dmask, rhs, partials, mode, ctl, smask, sslots, dshift, cmass);
 }
 
 void launch_thickness2d(const LaunchCfg& c, int n0, int n1, const int* mat, const double* y, double* th) {
@@ -328,8 +405,20 @@ void launch_coef2d(const LaunchCfg& c, int n0, int n1, const double* T, const in
 }
 
 void launch_diag2d(const LaunchCfg& c, const GridT<double>& g, const double* rmid, const double* kx,
-                   const double* ky, double* diag) {
-    launch_kernel(k_diag2d, vec_blocks(c, g.N), 256, c.stream, g, rmid, kx, ky, diag);
+                   const double* ky, double* diag, const double* shift) {
+    launch_kernel(k_diag2d, vec_blocks(c, g.N), 256, c.stream, g, rmid, kx, ky, shift, diag);
+}
+void launch_lumped_mass2d(const LaunchCfg& c, const GridT<double>& g, const double* rmid, const int* mat,
+                          const uint8_t* excl, const double* cp, const double* dens, double timestep, double* c64,
+                          float* c32, double weight) {
+    launch_kernel(k_lumped_mass2d, vec_blocks(c, g.N), 256, c.stream, g, rmid, mat, excl, cp, dens, timestep, weight,
+                  c64, c32);
+}
+void launch_elem_capacity2d(const LaunchCfg& c, const GridT<double>& g, const double* rmid, const int* mat,
+                            const uint8_t* excl, const double* cp, const double* dens, double timestep, double* c64,
+                            float* c32, double* cneg) {
+    launch_kernel(k_elem_capacity2d, vec_blocks(c, g.N), 256, c.stream, g, rmid, mat, excl, cp, dens, timestep, c64,
+                  c32, cneg);
 }
 
 void launch_heat_load2d(const LaunchCfg& c, const GridT<double>& g, const double* rmid, const double* q,

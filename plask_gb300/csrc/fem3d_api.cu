@@ -910,16 +910,17 @@ struct plgpu_fem3d {
                         k64.as<double>(), k32.as<float>(), aniso ? kz64.as<double>() : nullptr,
                         aniso ? kz32.as<float>() : nullptr, aniso);
     }
-    // Jacobi diagonal of the current operator and its inverse (FP64 and FP32)
-    void update_diag() {
+    // Jacobi diagonal of the current operator and its inverse (FP64 and FP32); `shift` adds
+    // the capacity's diagonal of a time step
+    void update_diag(const double* shift = nullptr) {
         if (planar) {
             launch_diag2d(cfg, g64, rmid_ptr64(), k64.as<double>(), aniso ? kz64.as<double>() : nullptr,
-                          diag.as<double>());
+                          diag.as<double>(), shift);
             launch_finish_diag(cfg, N, s64, dmask.as<uint32_t>(), diag.as<double>(), minv64.as<double>(),
                                minv32.as<float>());
         } else {
             launch_diag(cfg, g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, s64,
-                        dmask.as<uint32_t>(), diag.as<double>(), minv64.as<double>(), minv32.as<float>());
+                        dmask.as<uint32_t>(), diag.as<double>(), minv64.as<double>(), minv32.as<float>(), shift);
         }
     }
 
@@ -930,7 +931,9 @@ struct plgpu_fem3d {
             if (mode == MODE_CG) ss = launch_surface_cg(cfg, s64, x, y, partials.as<double>(), op2d_blocks(cfg, N), c);
             launch_operator2d(cfg, g64, rmid_ptr64(), x, y, k64.as<double>(), aniso ? kz64.as<double>() : nullptr,
                               dmask.as<uint32_t>(), rhs, partials.as<double>(), mode, c,
-                              ss > 0 ? smask.as<uint32_t>() : nullptr, ss);
+                              ss > 0 ? smask.as<uint32_t>() : nullptr, ss,
+                              dyn_active && dyn_lumping ? cap64.as<double>() : nullptr,
+                              dyn_active && !dyn_lumping ? cel64.as<double>() : nullptr);
             return;
         }
         if (mode == MODE_CG)
@@ -948,7 +951,9 @@ struct plgpu_fem3d {
             if (mode == MODE_CG) ss = launch_surface_cg(cfg, s32, x, y, partials.as<double>(), op2d_blocks(cfg, N), c);
             launch_operator2d(cfg, g32, rmid_ptr32(), x, y, k32.as<float>(), aniso ? kz32.as<float>() : nullptr,
                               dmask.as<uint32_t>(), (const float*)nullptr, partials.as<double>(), mode, c,
-                              ss > 0 ? smask.as<uint32_t>() : nullptr, ss);
+                              ss > 0 ? smask.as<uint32_t>() : nullptr, ss,
+                              dyn_active && dyn_lumping ? cap32.as<float>() : nullptr,
+                              dyn_active && !dyn_lumping ? cel32.as<float>() : nullptr);
             return;
         }
         if (mode == MODE_CG)
@@ -1519,31 +1524,57 @@ struct plgpu_fem3d {
     // conditions, and passes the vectors through buffers that alias after the first
     // step; on meshes whose capacity per node exceeds 1 that grows without bound.)
 
+    // lumped capacity per node (weight x the corner capacities around it) and the
+    // consistent matrix's corner capacity per element; 3D hexes or planar quads
+    void lumped_capacity(double* c64, float* c32, double weight) {
+        if (planar)
+            launch_lumped_mass2d(cfg, g64, rmid_ptr64(), d_mat.as<int>(), d_excl.as<uint8_t>(), d_cp.as<double>(),
+                                 d_dens.as<double>(), dyn_dt, c64, c32, weight);
+        else
+            launch_lumped_mass(cfg, g64, d_mat.as<int>(), d_excl.as<uint8_t>(), d_cp.as<double>(),
+                               d_dens.as<double>(), dyn_dt, c64, c32, weight);
+    }
+    void element_capacity() {
+        if (planar)
+            launch_elem_capacity2d(cfg, g64, rmid_ptr64(), d_mat.as<int>(), d_excl.as<uint8_t>(), d_cp.as<double>(),
+                                   d_dens.as<double>(), dyn_dt, cel64.as<double>(), cel32.as<float>(),
+                                   celneg64.as<double>());
+        else
+            launch_elem_capacity(cfg, g64, d_mat.as<int>(), d_excl.as<uint8_t>(), d_cp.as<double>(),
+                                 d_dens.as<double>(), dyn_dt, cel64.as<double>(), cel32.as<float>(),
+                                 celneg64.as<double>());
+    }
+    // y = rhs - (kB x + cneg-capacity x), the right-hand side product of a time step
+    void op_step_rhs(const double* x, double* y, const double* rhs, const double* cneg) {
+        if (planar)
+            launch_operator2d(cfg, g64, rmid_ptr64(), x, y, kB64.as<double>(), aniso ? kzB64.as<double>() : nullptr,
+                              dmask.as<uint32_t>(), rhs, partials.as<double>(), MODE_RHS, d_ctl.as<SolveCtl>(),
+                              nullptr, 0, nullptr, cneg);
+        else
+            launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), x, y, kB64.as<double>(),
+                            aniso ? kzB64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(), rhs,
+                            partials.as<double>(), MODE_RHS, d_ctl.as<SolveCtl>(), nullptr, 0, nullptr, cneg);
+    }
+
     void dyn_set_matrix() {
         const size_t N8 = (size_t)N * 8;
-        launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab, k64.as<double>(),
-                    k32.as<float>(), aniso ? kz64.as<double>() : nullptr, aniso ? kz32.as<float>() : nullptr, aniso);
+        update_coef();
         ck(cudaMemcpyAsync(kB64.p, k64.p, N8, cudaMemcpyDeviceToDevice, stream), "copy k");
         if (aniso) ck(cudaMemcpyAsync(kzB64.p, kz64.p, N8, cudaMemcpyDeviceToDevice, stream), "copy kz");
         launch_scale4(cfg, N, dyn_theta, k64.as<double>(), k32.as<float>(), aniso ? kz64.as<double>() : nullptr,
                       aniso ? kz32.as<float>() : nullptr);
         if (dyn_lumping) {
-            launch_lumped_mass(cfg, g64, d_mat.as<int>(), d_excl.as<uint8_t>(), d_cp.as<double>(),
-                               d_dens.as<double>(), dyn_dt, cap64.as<double>(), cap32.as<float>());
+            lumped_capacity(cap64.as<double>(), cap32.as<float>(), 1.0);
         } else {
-            // consistent C: corner capacities for the operator, its diagonal (8/27 c per
-            // element corner) for the Jacobi preconditioner, and B's stiffness part
-            // (1 - theta) K kept in kB for the right-hand side product
-            launch_elem_capacity(cfg, g64, d_mat.as<int>(), d_excl.as<uint8_t>(), d_cp.as<double>(),
-                                 d_dens.as<double>(), dyn_dt, cel64.as<double>(), cel32.as<float>(),
-                                 celneg64.as<double>());
-            launch_lumped_mass(cfg, g64, d_mat.as<int>(), d_excl.as<uint8_t>(), d_cp.as<double>(),
-                               d_dens.as<double>(), dyn_dt, cap64.as<double>(), nullptr, 8.0 / 27.0);
+            // consistent C: corner capacities for the operator, its diagonal ((2/3)^3 = 8/27 c
+            // per hex corner, (2/3)^2 = 4/9 c per quad corner) for the Jacobi preconditioner,
+            // and B's stiffness part (1 - theta) K kept in kB for the right-hand side product
+            element_capacity();
+            lumped_capacity(cap64.as<double>(), nullptr, planar ? 4.0 / 9.0 : 8.0 / 27.0);
             launch_scale4(cfg, N, 1.0 - dyn_theta, kB64.as<double>(), nullptr, aniso ? kzB64.as<double>() : nullptr,
                           nullptr);
         }
-        launch_diag(cfg, g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, s64, dmask.as<uint32_t>(),
-                    diag.as<double>(), minv64.as<double>(), minv32.as<float>(), cap64.as<double>());
+        update_diag(cap64.as<double>());
         // F with the elimination of A's Dirichlet columns, the row values at the Dirichlet rows
         op64(vD.as<double>(), Fel.as<double>(), F.as<double>(), MODE_RHS);
         launch_set_dirichlet(cfg, (int)(d_didx.bytes / sizeof(int)), d_didx.as<int>(), d_dval.as<double>(),
@@ -1614,17 +1645,12 @@ struct plgpu_fem3d {
             }
             // X = B T + F = C T - (1 - theta) K T + F, then Dirichlet rows of T take X
             if (dyn_lumping) {
-                launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), T.as<double>(), Yb.as<double>(),
-                                kB64.as<double>(), aniso ? kzB64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(),
-                                Zb.as<double>(), partials.as<double>(), MODE_RHS, d_ctl.as<SolveCtl>());
+                op_step_rhs(T.as<double>(), Yb.as<double>(), Zb.as<double>(), nullptr);
                 launch_dyn_rhs(cfg, N, cap64.as<double>(), T.as<double>(), Yb.as<double>(), 1.0 - dyn_theta,
                                Fel.as<double>(), b.as<double>());
             } else {
                 // one operator pass: F - ((1 - theta) K - C) T with kB = (1 - theta) K and -c
-                launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), T.as<double>(), b.as<double>(),
-                                kB64.as<double>(), aniso ? kzB64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(),
-                                Fel.as<double>(), partials.as<double>(), MODE_RHS, d_ctl.as<SolveCtl>(), nullptr, 0,
-                                nullptr, celneg64.as<double>());
+                op_step_rhs(T.as<double>(), b.as<double>(), Fel.as<double>(), celneg64.as<double>());
             }
             launch_set_dirichlet(cfg, nrows, d_didx.as<int>(), d_dval.as<double>(), b.as<double>(), T.as<double>());
             ck(cudaEventRecord(ev2, stream), "event");
@@ -3030,7 +3056,6 @@ int plgpu_fem3d_batch_tune(plgpu_fem3d* const* handles, int count, int loops, in
 int plgpu_fem3d_set_dynamic(plgpu_fem3d* h, const double* cp, const double* dens, double timestep,
                             double methodparam, int lumping, int rebuildfreq, int logfreq) {
     return guarded(h, [&] {
-        if (h->planar) throw ArgError("time stepping is provided for 3D handles (Dynamic3D)");
         if (h->n_mat == 0) throw StateError("set the material table first");
         if (!cp || !dens) throw ArgError("cp and dens are required");
         if (!(timestep > 0.0) || !std::isfinite(timestep)) throw ArgError("timestep must be positive");
@@ -3052,7 +3077,6 @@ int plgpu_fem3d_set_dynamic(plgpu_fem3d* h, const double* cp, const double* dens
 int plgpu_fem3d_compute_dynamic(plgpu_fem3d* h, double time, double* elapsed, plgpu_stats* stats) {
     return guarded(h, [&] {
         if (!std::isfinite(time) || time < 0.0) throw ArgError("time must be finite and >= 0");
-        if (h->planar) throw ArgError("time stepping is provided for 3D handles (Dynamic3D)");
         h->compute_dynamic(time, stats);
         if (elapsed) *elapsed = h->elapstime;
     });

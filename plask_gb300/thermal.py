@@ -510,11 +510,11 @@ class Dynamic3D(Static3D):
     """Finite element time-stepping thermal solver for 3D geometry, on the GPU.
 
     A drop-in for PLaSK's ``thermal.dynamic.Dynamic3D`` (femT3d.cpp,
-    python/dynamic.cpp:34-45): ``compute(time)`` advances ``time`` ns with the theta
+    python/dynamic_python.cpp:70-90): ``compute(time)`` advances ``time`` ns with the theta
     method; attributes ``inittemp`` (300 K), ``timestep`` (0.1 ns), ``methodparam``
     (0.5: Crank-Nicolson), ``lumping`` (True: lumped heat capacity; False: the consistent
     matrix), ``rebuildfreq`` (0), ``logfreq`` (500), ``time`` / ``elapsed_time`` (read only,
-    python/dynamic.cpp:46-48),
+    python/dynamic_python.cpp:86-87),
     ``algorithm`` ("iterative"), ``temperature_boundary``, ``inHeat`` and the providers
     of Static3D.  The material table must carry ``cp`` and ``dens``.
     """

@@ -378,8 +378,67 @@ class StaticCyl(Static2D):
     _class_name = "thermal.StaticCyl"
 
 
+class Dynamic2D(Static2D):
+    """Finite element time-stepping thermal solver for 2D Cartesian geometry, on the GPU.
+
+    A drop-in for PLaSK's ``thermal.dynamic.Dynamic2D`` (femT2d.cpp,
+    python/dynamic_python.cpp:32-69): ``compute(time)`` advances ``time`` ns with the theta
+    method; attributes ``inittemp`` (300 K), ``timestep`` (0.1 ns), ``methodparam`` (0.5:
+    Crank-Nicolson), ``lumping`` (True: lumped heat capacity; False: the consistent matrix
+    c (4, 2, 1) / 9, femT2d.cpp:199-233), ``rebuildfreq`` (0), ``logfreq`` (500),
+    ``time`` / ``elapsed_time`` (read only), ``temperature_boundary``, ``inHeat`` and the
+    providers of Static2D.  The material table must carry ``cp`` and ``dens``.
+    """
+
+    _class_name = "thermal.Dynamic2D"
+
+    def __init__(self, name=""):
+        super().__init__(name)
+        self.timestep = 0.1
+        self.methodparam = 0.5
+        self.lumping = True
+        self.rebuildfreq = 0
+        self.logfreq = 500
+        self._elapstime = 0.0
+        # the time-stepping solvers have temperature conditions only (femT2d.cpp:48-70)
+        del self.heatflux_boundary, self.convection_boundary, self.radiation_boundary
+        self.heatflux_boundary = self.convection_boundary = self.radiation_boundary = ()
+
+    @property
+    def time(self):
+        """Time of calculations performed so far since the last invalidation [ns]."""
+        return self._elapstime
+
+    elapsed_time = time
+
+    def compute(self, time):
+        """Run thermal calculations for ``time`` ns (femT2d.cpp:387-445)."""
+        self.initialize()
+        mt = self._geometry.materials
+        if mt.cp is None or mt.dens is None:
+            raise BadInput(-1, f"{self.id}: the material table has no cp / dens")
+        self._fem.set_dynamic(mt.cp, mt.dens, self.timestep, self.methodparam, self.lumping, self.rebuildfreq,
+                              self.logfreq)
+        self.loop_log = []
+        el, st = self._fem.compute_dynamic(time)
+        self._elapstime = el
+        self.stats = st
+        self.iterative.converged = bool(st["converged"])
+        self.iterative.iters = st["inner_iterations"]
+        return 0.0
+
+
+class DynamicCyl(Dynamic2D):
+    """Finite element time-stepping thermal solver for 2D cylindrical geometry (axis 0 = r),
+    on the GPU (DynamicThermalFem2DSolver<Geometry2DCylindrical>, femT2d.cpp:256-384)."""
+
+    _geometry_kind = "cylindrical"
+    _class_name = "thermal.DynamicCyl"
+
+
 def solver_for_structure2d(s, cls=Static2D, ordering="best", algorithm="gpu-mixed", name="", **kw):
-    """A configured :class:`Static2D` / :class:`StaticCyl` for a generated 2D structure."""
+    """A configured :class:`Static2D` / :class:`StaticCyl` (or, with their temperature
+    conditions only, :class:`Dynamic2D` / :class:`DynamicCyl`) for a generated 2D structure."""
     mesh = RectangularMesh2D(*s.axes, ordering=ordering)
     sv = cls(name)
     sv.geometry = StructureGeometry2D.from_structure(s)
@@ -390,16 +449,17 @@ def solver_for_structure2d(s, cls=Static2D, ordering="best", algorithm="gpu-mixe
     sv.algorithm = algorithm
     for side, v in s.temperature:
         sv.temperature_boundary.append(RectangularMesh2D.side(side), v)
-    for side, v in s.heatflux:
-        sv.heatflux_boundary.append(RectangularMesh2D.side(side), v)
-    for side, h, ta in s.convection:
-        sv.convection_boundary.append(RectangularMesh2D.side(side), {"coeff": h, "ambient": ta})
-    for side, e, ta in s.radiation:
-        sv.radiation_boundary.append(RectangularMesh2D.side(side), {"emissivity": e, "ambient": ta})
+    if not issubclass(cls, Dynamic2D):
+        for side, v in s.heatflux:
+            sv.heatflux_boundary.append(RectangularMesh2D.side(side), v)
+        for side, h, ta in s.convection:
+            sv.convection_boundary.append(RectangularMesh2D.side(side), {"coeff": h, "ambient": ta})
+        for side, e, ta in s.radiation:
+            sv.radiation_boundary.append(RectangularMesh2D.side(side), {"emissivity": e, "ambient": ta})
     for k, v in kw.items():
         setattr(sv, k, v)
     return sv
 
 
-__all__ = ["Static2D", "StaticCyl", "StructureGeometry2D", "RectangularMesh2D", "solver_for_structure2d",
+__all__ = ["Static2D", "StaticCyl", "Dynamic2D", "DynamicCyl", "StructureGeometry2D", "RectangularMesh2D", "solver_for_structure2d",
            "mesh_index2d"]

@@ -9,7 +9,8 @@ What the reference reads there, and what this reader applies:
   ``<loop inittemp maxerr>``, ``<matrix algorithm>`` with ``<iterative ...>``
   (plask/common/fem/fem_solver.hpp:38-106), ``<mesh ref empty-elements>``
   (fem_solver.hpp:164-178), ``<geometry ref>``;
-* ``Dynamic3D`` (solvers/thermal/dynamic/femT3d.cpp:46-70): ``<temperature>``,
+* ``Dynamic3D``, ``Dynamic2D``, ``DynamicCyl`` (solvers/thermal/dynamic/femT3d.cpp:46-70;
+  femT2d.cpp:46-70): ``<temperature>``,
   ``<loop inittemp timestep rebuildfreq logfreq>``, ``<matrix methodparam lumping
   algorithm>``;
 * ``Shockley3D`` (solvers/electrical/shockley/electr3d.cpp:41-87, beta.cpp:26-62):
@@ -156,7 +157,7 @@ def configure(solver, xml, places=None, geometries=None, meshes=None):
     meshes = meshes or {}
     cls = type(solver).__name__
     electrical = hasattr(solver, "voltage_boundary")
-    dynamic = cls == "Dynamic3D"
+    dynamic = cls in ("Dynamic3D", "Dynamic2D", "DynamicCyl")
     for tag in root:
         t, a = tag.tag, tag.attrib
         if t in ("geometry", "mesh"):

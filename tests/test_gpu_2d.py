@@ -3,7 +3,8 @@
 temperatures within 1e-6 K after the full k(T) loop for both geometries, both
 iteration orders, masked meshes, anisotropy, and heat-flux / convection / radiation
 edge conditions in both placements; the operator against the assembled matrix; heat
-fluxes; the reference's own Static2D conductivity test (tests/therm.py:47-53)."""
+fluxes; the reference's own Static2D conductivity test (tests/therm.py:47-53); Dynamic2D /
+DynamicCyl time steps against oracle/dynamic2d.py (solvers/thermal/dynamic/femT2d.cpp)."""
 import numpy as np
 import pytest
 
@@ -142,12 +143,55 @@ def test_reference_static2d_layer_thickness_conductivity():
     assert conds[1][0] == pytest.approx(2.0, abs=1e-6)
 
 
-def test_time_stepping_is_3d_only():
+DYN_CASES = [
+    # (class, seed, n, order, etch, aniso, theta, rebuildfreq, algorithm, lumping)
+    (T2.Dynamic2D, 71, (24, 30), "01", False, True, 0.5, 0, "gpu-mixed", True),
+    (T2.Dynamic2D, 72, (21, 33), "10", True, False, 1.0, 2, "gpu-pcg", False),
+    (T2.DynamicCyl, 73, (24, 30), "10", False, False, 0.5, 3, "gpu-mixed", True),
+    (T2.DynamicCyl, 74, (22, 28), "01", True, True, 0.75, 0, "gpu-mixed", False),
+]
+
+
+@pytest.mark.parametrize("cls,seed,n,order,etch,aniso,theta,rebuild,algorithm,lumping", DYN_CASES)
+def test_time_steps_match_oracle(cls, seed, n, order, etch, aniso, theta, rebuild, algorithm, lumping):
+    """Dynamic2D / DynamicCyl against oracle/dynamic2d.py (femT2d.cpp): the same steps and
+    elapsed time, temperatures within 1e-6 K, lumped and consistent capacity, masked meshes."""
+    from oracle import dynamic2d as D2
+
+    s = S.layered_2d(seed=seed, n=n, etch=etch, anisotropic=aniso)
+    s.heatflux, s.convection, s.radiation = [], [], []
+    rng = np.random.default_rng(seed)
+    cp = rng.uniform(300.0, 900.0, s.k300.size)
+    dens = rng.uniform(2000.0, 7000.0, s.k300.size)
+    sv = T2.solver_for_structure2d(s, cls=cls, ordering=order, algorithm=algorithm, timestep=0.2,
+                                   methodparam=theta, rebuildfreq=rebuild, lumping=lumping)
+    sv.geometry.materials.cp, sv.geometry.materials.dens = cp, dens
+    sv.compute(2.0)
+    p = _oracle_problem(s, sv)
+    To, elaps, steps = D2.compute(p, 2.0, cp, dens, timestep=0.2, theta=theta, lumping=lumping, rebuildfreq=rebuild)
+    node_id, _ = O2.masked_numbering(p)
+    To_full = O2.to_full(p, node_id, To, fill=np.nan)
+    Tg = sv._full_temperature()
+    act = node_id >= 0
+    d = np.max(np.abs(Tg[act] - To_full[act]))
+    print(cls.__name__, seed, "steps", steps, sv.stats["loops"], "max|dT|", d, "maxT", np.max(To))
+    assert np.all(np.isnan(Tg[~act]))
+    assert sv.stats["loops"] == steps
+    assert sv.time == pytest.approx(elaps, abs=1e-12)
+    assert d <= TOL_T
+    assert np.max(To) > 300.2  # the source heated the structure
+
+
+def test_time_stepping_takes_temperature_conditions_only():
     s = S.layered_2d(seed=3, n=(10, 12))
-    sv = T2.solver_for_structure2d(s)
+    sv = T2.solver_for_structure2d(s, cls=T2.Dynamic2D)
+    sv.geometry.materials.cp = np.ones(s.k300.size)
+    sv.geometry.materials.dens = np.ones(s.k300.size)
     sv.initialize()
-    with pytest.raises(_native.BadInput):
+    sv._fem.add_bc(_native.BC_HEATFLUX, np.array([0, 1]), 1e5)
+    with pytest.raises(_native.NativeError):
         sv._fem.set_dynamic(np.ones(s.k300.size), np.ones(s.k300.size))
+        sv._fem.compute_dynamic(1.0)
 
 
 @pytest.mark.parametrize("cls", [T2.Static2D, T2.StaticCyl])

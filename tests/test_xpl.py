@@ -1,7 +1,8 @@
 """XPL solver configuration (plask_gb300.xpl) applied to the drop-in solver objects, on the
 CPU: the tags and attributes of ThermalFem3DSolver::loadConfiguration
 (solvers/thermal/static/therm3d.cpp:40-69), fem_solver.hpp:38-106 and 164-178,
-DynamicThermalFem3DSolver (femT3d.cpp:46-70) and the Shockley solver (electr3d.cpp:41-87,
+DynamicThermalFem3DSolver (femT3d.cpp:46-70), DynamicThermalFem2DSolver (femT2d.cpp:46-70)
+and the Shockley solver (electr3d.cpp:41-87,
 beta.cpp:26-62)."""
 import numpy as np
 import pytest
@@ -68,6 +69,24 @@ def test_dynamic3d_configuration():
     with pytest.raises(ValueError):
         xpl.configure(TH.Dynamic3D(), '<thermal><convection><condition place="top" coeff="1" ambient="300"/>'
                                       '</convection></thermal>')
+
+
+@pytest.mark.parametrize("cls", [T2.Dynamic2D, T2.DynamicCyl])
+def test_dynamic2d_configuration(cls):
+    """DynamicThermalFem2DSolver::loadConfiguration (femT2d.cpp:46-70)."""
+    sv = cls()
+    xpl.configure(sv, """<thermal>
+        <loop inittemp="310" timestep="0.5" rebuildfreq="2" logfreq="7"/>
+        <matrix methodparam="0.75" lumping="no"/>
+        <temperature><condition place="left" value="320"/></temperature></thermal>""")
+    assert (sv.inittemp, sv.timestep, sv.rebuildfreq, sv.logfreq) == (310.0, 0.5, 2, 7)
+    assert sv.methodparam == 0.75 and sv.lumping is False
+    assert sv.temperature_boundary[0][1] == (320.0,)
+    with pytest.raises(ValueError):
+        xpl.configure(cls(), '<thermal><radiation><condition place="top" emissivity="0.5" ambient="300"/>'
+                             '</radiation></thermal>')
+    with pytest.raises(ValueError):
+        xpl.configure(cls(), '<thermal><loop maxerr="0.1"/></thermal>')
 
 
 def test_shockley3d_configuration():
