@@ -33,6 +33,8 @@
 #include "fem3d_kernels.h"
 #include "unet.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 using namespace plgpu;
 
 namespace {
@@ -57,6 +59,15 @@ struct SolveError : std::runtime_error {
 inline void ck(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
+
+// NVTX range for the phases of a computation (outer loop, setMatrix, linear solve, time
+// step): visible on a profiler's timeline, a no-op when no tool is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // RAII device allocation
 struct DevBuf {
@@ -1077,6 +1088,7 @@ struct plgpu_fem3d {
     // residual reaches the target the true residual is recomputed; CG restarts from
     // the current iterate (at most 3 times) while it is still above twice the target.
     void solve_fp64(int& status, int& iters, double& relres) {
+        NvtxRange nv("solve fp64 pcg");
         SolveCtl* ctl = d_ctl.as<SolveCtl>();
         double* part = partials.as<double>();
         const double* w = norm_weights();
@@ -1142,6 +1154,7 @@ struct plgpu_fem3d {
 
     // FP32 Jacobi-PCG corrections inside FP64 iterative refinement
     void solve_mixed(int& status, int& iters, int& refinements, double& relres) {
+        NvtxRange nv("solve mixed");
         SolveCtl* ctl = d_ctl.as<SolveCtl>();
         double* part = partials.as<double>();
         const double* w = norm_weights();
@@ -1428,6 +1441,7 @@ struct plgpu_fem3d {
     // compute (therm3d.cpp:281-340)
 
     double compute(int loops, plgpu_stats* st) {
+        NvtxRange nv("thermal compute");
         if (!initialized) initialize();
         if (bc_dirty) materialize_bc();
         const long long launches0 = thread_launch_count();
@@ -1441,20 +1455,24 @@ struct plgpu_fem3d {
         const bool mixed = algorithm == PLGPU_ALGO_ITERATIVE || algorithm == PLGPU_ALGO_GPU_MIXED ||
                            algorithm == PLGPU_ALGO_GPU_LEARNED;
         do {
+            NvtxRange nv_loop("outer loop");
             ck(cudaMemcpyAsync(T0.p, T.p, (size_t)N * 8, cudaMemcpyDeviceToDevice, stream), "copy T0");
             // setMatrix: coefficients, Jacobi diagonal, right-hand side with Dirichlet elimination
-            update_coef();
-            update_diag();
-            if (algorithm == PLGPU_ALGO_GPU_LEARNED && pre != nullptr) {
-                ensure_unet_buffers();
-                refresh_features();
+            {
+                NvtxRange nv_set("setMatrix");
+                update_coef();
+                update_diag();
+                if (algorithm == PLGPU_ALGO_GPU_LEARNED && pre != nullptr) {
+                    ensure_unet_buffers();
+                    refresh_features();
+                }
+                op64(vD.as<double>(), b.as<double>(), F.as<double>(), MODE_RHS);
+                launch_radiation(cfg, rad_rows, rad_row.as<int>(), rad_ptr.as<int>(), rad_src.as<int>(),
+                                 rad_coef.as<double>(), rad_tamb.as<double>(), T.as<double>(), b.as<double>());
+                launch_set_dirichlet(cfg, (int)(d_didx.bytes / sizeof(int)), d_didx.as<int>(), d_dval.as<double>(),
+                                     b.as<double>(), T.as<double>());
+                ck(cudaGetLastError(), "launch");
             }
-            op64(vD.as<double>(), b.as<double>(), F.as<double>(), MODE_RHS);
-            launch_radiation(cfg, rad_rows, rad_row.as<int>(), rad_ptr.as<int>(), rad_src.as<int>(),
-                             rad_coef.as<double>(), rad_tamb.as<double>(), T.as<double>(), b.as<double>());
-            launch_set_dirichlet(cfg, (int)(d_didx.bytes / sizeof(int)), d_didx.as<int>(), d_dval.as<double>(),
-                                 b.as<double>(), T.as<double>());
-            ck(cudaGetLastError(), "launch");
             ck(cudaEventRecord(ev2, stream), "event");
             int status = 0, iters = 0, refs = 0;
             if (mixed)
@@ -1582,6 +1600,7 @@ struct plgpu_fem3d {
     }
 
     double compute_dynamic(double time, plgpu_stats* st) {
+        NvtxRange nv("time stepping");
         if (cp_tab.empty()) throw StateError("set the heat capacities first (plgpu_fem3d_set_dynamic)");
         for (int kind = 1; kind < 4; ++kind)
             if (!bcs[kind].empty())
@@ -1639,6 +1658,7 @@ struct plgpu_fem3d {
         float solve_ms = 0.f;
         time += dyn_dt / 2.0;
         for (double t = 0.0; t < time; t += dyn_dt) {
+            NvtxRange nv_step("time step");
             if (dyn_rebuild && r == 0) {
                 dyn_set_matrix();
                 r = dyn_rebuild;
@@ -2178,6 +2198,7 @@ struct plgpu_elec3d : plgpu_fem3d {
 
     // ElectricalFem3DSolver::compute (electr3d.cpp:356-442)
     double compute_e(int loops, plgpu_stats* st) {
+        NvtxRange nv("electrical compute");
         if (!initialized) initialize_e();
         if (bc_dirty) materialize_bc();
         upload_info();

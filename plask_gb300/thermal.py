@@ -204,6 +204,41 @@ def _interp_axis(axis, x):
     return i, np.clip(w, 0.0, 1.0), inside
 
 
+def save_state(solver, path):
+    """Write the solver's temperature field (masked-mesh numbering, mesh order) with the
+    mesh axes and iteration order to the ``.npz`` file ``path``: a checkpoint for
+    :func:`load_state`.  The reference keeps the temperatures between ``compute()`` calls
+    until ``invalidate()`` (therm3d.cpp:118-122); this makes that warm restart survive the
+    process."""
+    solver.initialize()
+    data = {"temperature": solver._fem.temperature(), "ordering": np.array(solver.mesh.ordering),
+            "solver": np.array(type(solver).__name__)}
+    for d, a in enumerate(solver.mesh.axes):
+        data[f"axis{d}"] = np.asarray(a, np.float64)
+    np.savez(path, **data)
+
+
+def load_state(solver, path):
+    """Restore a temperature field written by :func:`save_state` as the starting field of
+    the next ``compute()``.  The mesh (axes and iteration order) must be the one saved;
+    the field must have the solver's node count (the same masked mesh)."""
+    with np.load(path) as f:
+        axes = [f[k] for k in sorted(k for k in f.files if k.startswith("axis"))]
+        ordering = str(f["ordering"])
+        T = np.array(f["temperature"], np.float64)
+    mine = [np.asarray(a, np.float64) for a in solver.mesh.axes]
+    if len(axes) != len(mine) or any(a.shape != b.shape or not np.array_equal(a, b) for a, b in zip(axes, mine)):
+        raise BadInput(-1, f"{solver.id}: the saved field belongs to another mesh")
+    if ordering != solver.mesh.ordering:
+        raise BadInput(-1, f"{solver.id}: the saved field has iteration order {ordering}, "
+                           f"the mesh {solver.mesh.ordering}")
+    solver.initialize()
+    nn, _ = solver._fem.sizes()
+    if T.size != nn:
+        raise BadInput(-1, f"{solver.id}: the saved field has {T.size} nodes, the masked mesh {nn}")
+    solver._fem.set_temperature(T)
+
+
 class Static3D:
     """Finite element thermal solver for 3D geometry, computed on the GPU.
 
@@ -400,6 +435,14 @@ class Static3D:
         """Nodal temperatures in the solver's numbering (masked mesh, mesh order)."""
         self.initialize()
         return self._fem.temperature()
+
+    def save(self, path):
+        """Checkpoint the temperature field to an ``.npz`` file (:func:`save_state`)."""
+        save_state(self, path)
+
+    def load(self, path):
+        """Start the next ``compute()`` from a checkpointed field (:func:`load_state`)."""
+        load_state(self, path)
 
     def _full_temperature(self):
         """Canonical (n2, n1, n0) temperature with NaN at nodes outside the masked mesh."""

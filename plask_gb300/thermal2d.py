@@ -20,7 +20,7 @@ import numpy as np
 from . import _native
 from .mesh import RectangularMesh2D, mesh_index2d, to_mesh_order2d
 from .thermal import (BadInput, BoundaryConditions, IterativeParams, MaterialTable, Provider, _check_interpolation,
-                      _element_axis, _nearest_axis)
+                      _element_axis, _nearest_axis, load_state, save_state)
 
 log = logging.getLogger("plask_gb300.thermal2d")
 
@@ -278,6 +278,14 @@ class Static2D:
         """Nodal temperatures in the solver's numbering (masked mesh, mesh order)."""
         self.initialize()
         return self._fem.temperature()
+
+    def save(self, path):
+        """Checkpoint the temperature field to an ``.npz`` file (thermal.save_state)."""
+        save_state(self, path)
+
+    def load(self, path):
+        """Start the next ``compute()`` from a checkpointed field (thermal.load_state)."""
+        load_state(self, path)
 
     def _active_mask_mesh_order(self):
         mesh = self._mesh
