@@ -14,8 +14,8 @@ Fixtures:
   convective top, ORDER_201; Cholesky and NSPCG temperatures, loops, toterr.
 * ``static3d_mesa_faces_12x11x16``: an etched mesa (masked mesh) with heat-flux,
   convective and radiative faces in the reference's placement, ORDER_012.
-* ``staticcyl_etched_20x26``: StaticCyl (therm2d.cpp), masked mesh, edge conditions,
-  ORDER_10, the reference's convective edge stiffness (bc_compat).
+* ``staticcyl_etched_aniso_35x52``: StaticCyl (therm2d.cpp), an etched mesa (masked
+  mesh), anisotropic layers, ORDER_01.
 * ``dynamic3d_consistent_12x11x16``: Dynamic3D (femT3d.cpp), consistent capacity,
   theta = 0.75, 2 ns in 0.2 ns steps.
 * ``shockley3d_junction_21x19x30``: Shockley3D (electr3d.cpp), a layered junction
@@ -114,18 +114,15 @@ def static3d_mesa():
 
 
 def staticcyl():
-    s = S.layered_2d(seed=9, n=(20, 26), etch=True)
-    s.heatflux = [("right", -2e5)]
-    s.convection = [("top", 1e-3, 290.0)]
-    s.radiation = [("top", 0.8, 280.0)]
-    order = "10"
+    s = S.layered_2d(seed=22, n=(35, 52), etch=True, anisotropic=True)
+    order = "01"
     p = problem2d(s, "cylindrical", order)
     T, toterr, rec = O2.compute(p)
     arr, meta = G.pack_thermal(s)
     arr.update(T_cholesky=T)
     meta.update(kind="static2d", geometry="cylindrical", order=order, bc_compat=True, empty_elements="exclude",
                 toterr=toterr, records=records(rec))
-    G.save("staticcyl_etched_20x26", arr, meta)
+    G.save("staticcyl_etched_aniso_35x52", arr, meta)
 
 
 def dynamic3d():

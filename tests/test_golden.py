@@ -108,7 +108,11 @@ def _gpu_static3d(data, meta, algorithm):
     s = G.unpack_thermal(data, meta)
     sv = TH.solver_for_structure(s, ordering=meta["order"], algorithm=algorithm)
     tot = sv.compute()
-    return sv, sv._full_temperature(), tot
+    # nodes of the masked mesh (the oracle keeps the others at their initial value, the
+    # solver reports NaN there)
+    p = O.from_structure(s, order=meta["order"], empty_elements=meta["empty_elements"])
+    act = O.masked_numbering(p)[0] >= 0
+    return sv, sv._full_temperature(), tot, act
 
 
 @pytest.mark.gpu
@@ -116,30 +120,31 @@ def _gpu_static3d(data, meta, algorithm):
 @pytest.mark.parametrize("name", ["static3d_layered_aniso_12x10x18", "static3d_mesa_faces_12x11x16"])
 def test_gpu_static3d_matches_fixture(name, algorithm):
     data, meta = G.load(name)
-    sv, T, tot = _gpu_static3d(data, meta, algorithm)
+    sv, T, tot, act = _gpu_static3d(data, meta, algorithm)
     ref = data["T_cholesky"]
-    assert _same_nan(T, ref)
-    assert _maxdiff(T, ref) <= TOL_T
+    assert np.all(np.isnan(T[~act]))
+    assert np.max(np.abs(T[act] - ref[act])) <= TOL_T
     assert sv.stats["loops"] == len(meta["records"])
     assert abs(tot - meta["toterr"]) <= TOL_T
     if "T_nspcg" in data:
-        assert _maxdiff(T, data["T_nspcg"]) <= TOL_T
+        assert np.max(np.abs(T[act] - data["T_nspcg"][act])) <= TOL_T
 
 
 @pytest.mark.gpu
 def test_gpu_staticcyl_matches_fixture():
     from plask_gb300 import thermal2d as T2
 
-    data, meta = G.load("staticcyl_etched_20x26")
+    data, meta = G.load("staticcyl_etched_aniso_35x52")
     s = G.unpack_thermal(data, meta)
     sv = T2.solver_for_structure2d(s, cls=T2.StaticCyl, ordering=meta["order"], bc_compat=meta["bc_compat"])
     tot = sv.compute()
     T = sv._full_temperature()
     ref = data["T_cholesky"]
-    assert _same_nan(T, ref)
-    assert _maxdiff(T, ref) <= TOL_T
+    act = O2.masked_numbering(_problem2d(s, meta))[0] >= 0
+    assert np.all(np.isnan(T[~act]))
+    assert np.max(np.abs(T[act] - ref[act])) <= TOL_T
     assert sv.stats["loops"] == len(meta["records"])
-    assert abs(tot - meta["toterr"]) <= TOL_T
+    assert tot == pytest.approx(meta["toterr"], abs=1e-5)
 
 
 @pytest.mark.gpu
