@@ -16,8 +16,12 @@ Fixtures:
   convective and radiative faces in the reference's placement, ORDER_012.
 * ``staticcyl_etched_aniso_35x52``: StaticCyl (therm2d.cpp), an etched mesa (masked
   mesh), anisotropic layers, ORDER_01.
+* ``static2d_etched_aniso_33x47``: Static2D (therm2d.cpp), an etched mesa, anisotropic
+  layers, ORDER_10.
 * ``dynamic3d_consistent_12x11x16``: Dynamic3D (femT3d.cpp), consistent capacity,
   theta = 0.75, 2 ns in 0.2 ns steps.
+* ``dynamiccyl_lumped_24x30``: DynamicCyl (femT2d.cpp), lumped capacity,
+  Crank-Nicolson, k(T) rebuilt every 3 steps, 2 ns in 0.2 ns steps, ORDER_10.
 * ``shockley3d_junction_21x19x30``: Shockley3D (electr3d.cpp), a layered junction
   structure, 5 loops, ORDER_102.
 """
@@ -34,6 +38,7 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(HERE))
 
 import golden_io as G  # noqa: E402
+from oracle import dynamic2d as D2  # noqa: E402
 from oracle import dynamic3d as D3  # noqa: E402
 from oracle import electr3d as E  # noqa: E402
 from oracle import fem2d as O2  # noqa: E402
@@ -125,6 +130,35 @@ def staticcyl():
     G.save("staticcyl_etched_aniso_35x52", arr, meta)
 
 
+def static2d():
+    s = S.layered_2d(seed=12, n=(33, 47), etch=True, anisotropic=True)
+    order = "10"
+    p = problem2d(s, "cartesian", order)
+    T, toterr, rec = O2.compute(p)
+    arr, meta = G.pack_thermal(s)
+    arr.update(T_cholesky=T)
+    meta.update(kind="static2d", geometry="cartesian", order=order, bc_compat=True, empty_elements="exclude",
+                toterr=toterr, records=records(rec))
+    G.save("static2d_etched_aniso_33x47", arr, meta)
+
+
+def dynamiccyl():
+    s = S.layered_2d(seed=73, n=(24, 30))
+    s.heatflux, s.convection, s.radiation = [], [], []
+    rng = np.random.default_rng(73)
+    cp = rng.uniform(300.0, 900.0, s.k300.size)
+    dens = rng.uniform(2000.0, 7000.0, s.k300.size)
+    order = "10"
+    p = problem2d(s, "cylindrical", order)
+    T, elaps, steps = D2.compute(p, 2.0, cp, dens, timestep=0.2, theta=0.5, lumping=True, rebuildfreq=3)
+    node_id, _ = O2.masked_numbering(p)
+    arr, meta = G.pack_thermal(s)
+    arr.update(T_direct=O2.to_full(p, node_id, T, fill=np.nan), cp=cp, dens=dens)
+    meta.update(kind="dynamic2d", geometry="cylindrical", order=order, bc_compat=True, empty_elements="exclude",
+                time=2.0, timestep=0.2, theta=0.5, lumping=True, rebuildfreq=3, elapsed=elaps, steps=steps)
+    G.save("dynamiccyl_lumped_24x30", arr, meta)
+
+
 def dynamic3d():
     s = S.layered_c0(seed=5, n=(12, 11, 16))
     rng = np.random.default_rng(5 + 77)
@@ -161,7 +195,9 @@ def main():
     print(f"static3d layered: Cholesky vs the reference's NSPCG max |dT| = {d:.3e} K")
     static3d_mesa()
     staticcyl()
+    static2d()
     dynamic3d()
+    dynamiccyl()
     shockley3d()
     for n in G.names():
         print(n, (HERE / f"{n}.npz").stat().st_size, "bytes")

@@ -14,6 +14,7 @@ import pytest
 sys.path.insert(0, str(pathlib.Path(__file__).resolve().parent / "golden"))
 
 import golden_io as G  # noqa: E402
+from oracle import dynamic2d as D2  # noqa: E402
 from oracle import dynamic3d as D3  # noqa: E402
 from oracle import electr3d as E  # noqa: E402
 from oracle import fem2d as O2  # noqa: E402
@@ -78,6 +79,15 @@ def test_oracle_replays_fixture(name):
         node_id, _ = O.masked_numbering(p)
         assert _maxdiff(O.to_full(p, node_id, T), data["T_direct"]) <= 1e-9
         assert steps == meta["steps"] and elaps == pytest.approx(meta["elapsed"], abs=1e-12)
+    elif kind == "dynamic2d":
+        s = G.unpack_thermal(data, meta)
+        p = _problem2d(s, meta)
+        T, elaps, steps = D2.compute(p, meta["time"], data["cp"], data["dens"], timestep=meta["timestep"],
+                                     theta=meta["theta"], lumping=meta["lumping"], rebuildfreq=meta["rebuildfreq"])
+        node_id, _ = O2.masked_numbering(p)
+        T = O2.to_full(p, node_id, T, fill=np.nan)
+        assert _same_nan(T, data["T_direct"]) and _maxdiff(T, data["T_direct"]) <= 1e-9
+        assert steps == meta["steps"] and elaps == pytest.approx(meta["elapsed"], abs=1e-12)
     elif kind == "shockley3d":
         s = G.unpack_elec(data, meta)
         p = E.from_structure(s, order=meta["order"], convergence=meta["convergence"])
@@ -131,12 +141,14 @@ def test_gpu_static3d_matches_fixture(name, algorithm):
 
 
 @pytest.mark.gpu
-def test_gpu_staticcyl_matches_fixture():
+@pytest.mark.parametrize("name", ["staticcyl_etched_aniso_35x52", "static2d_etched_aniso_33x47"])
+def test_gpu_static2d_matches_fixture(name):
     from plask_gb300 import thermal2d as T2
 
-    data, meta = G.load("staticcyl_etched_aniso_35x52")
+    data, meta = G.load(name)
     s = G.unpack_thermal(data, meta)
-    sv = T2.solver_for_structure2d(s, cls=T2.StaticCyl, ordering=meta["order"], bc_compat=meta["bc_compat"])
+    cls = T2.StaticCyl if meta["geometry"] == "cylindrical" else T2.Static2D
+    sv = T2.solver_for_structure2d(s, cls=cls, ordering=meta["order"], bc_compat=meta["bc_compat"])
     tot = sv.compute()
     T = sv._full_temperature()
     ref = data["T_cholesky"]
@@ -167,6 +179,25 @@ def test_gpu_dynamic3d_matches_fixture():
     assert sv.stats["loops"] == meta["steps"]
     assert sv.time == pytest.approx(meta["elapsed"], abs=1e-12)
     assert _maxdiff(sv._full_temperature(), data["T_direct"]) <= TOL_T
+
+
+@pytest.mark.gpu
+def test_gpu_dynamiccyl_matches_fixture():
+    from plask_gb300 import thermal2d as T2
+
+    data, meta = G.load("dynamiccyl_lumped_24x30")
+    s = G.unpack_thermal(data, meta)
+    sv = T2.solver_for_structure2d(s, cls=T2.DynamicCyl, ordering=meta["order"], algorithm="gpu-mixed",
+                                   timestep=meta["timestep"], methodparam=meta["theta"],
+                                   rebuildfreq=meta["rebuildfreq"], lumping=meta["lumping"])
+    sv.geometry.materials.cp, sv.geometry.materials.dens = data["cp"], data["dens"]
+    sv.compute(meta["time"])
+    T = sv._full_temperature()
+    ref = data["T_direct"]
+    assert _same_nan(T, ref)
+    assert _maxdiff(T, ref) <= TOL_T
+    assert sv.stats["loops"] == meta["steps"]
+    assert sv.time == pytest.approx(meta["elapsed"], abs=1e-12)
 
 
 @pytest.mark.gpu
