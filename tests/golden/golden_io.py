@@ -1,6 +1,6 @@
 """Golden fixtures -- TEST INFRASTRUCTURE ONLY: (de)serialisation of the seeded structures
 and of the problems built from them, shared by ``make_golden.py`` (which writes the
-fixtures) and ``tests/test_golden.py`` (which replays them on the oracle and the GPU).
+fixtures) and ``tests/test_regression_golden.py`` (which replays them on the oracle and the GPU).
 
 A fixture is one ``.npz`` file holding the solver inputs (axes, element materials, the
 material table, heat, boundary conditions as mesh sides or node masks) and the outputs
