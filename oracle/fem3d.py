@@ -36,7 +36,6 @@ reference's own ``extlib/nspcg/nspcg.c`` where that build is available.
 from __future__ import annotations
 
 import dataclasses
-import math
 
 import numpy as np
 import scipy.linalg.lapack as lapack

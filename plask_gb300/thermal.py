@@ -20,7 +20,7 @@ import logging
 import numpy as np
 
 from . import _native
-from .mesh import RectangularMesh3D, mesh_index, to_mesh_order
+from .mesh import RectangularMesh3D, to_mesh_order
 
 log = logging.getLogger("plask_gb300.thermal")
 

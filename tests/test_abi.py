@@ -1,7 +1,6 @@
 """The C-ABI library builds, loads, and exports every entry point that include/*.h declares.
 
 No compute call is made here (no GPU in the CPU suite)."""
-import ctypes
 import pathlib
 import re
 
