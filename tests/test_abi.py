@@ -57,3 +57,37 @@ def test_creation_error_without_gpu_is_reported_not_raised_in_c():
         assert e.code != 0
     else:
         raise AssertionError("expected a CUDA error without a GPU")
+
+
+def test_headers_are_plain_c_and_the_library_links_from_c(tmp_path):
+    """A C99 program that includes every header and takes the address of every declared
+    entry point compiles warning-free and links against the library: the boundary a
+    cgo, JNI or ctypes binding sees, with no C++ type in it."""
+    import shutil
+    import subprocess
+
+    import pytest
+
+    from plask_gb300 import _native
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    lib = _native.load() and _native.library_path()
+    names = sorted(declared_functions())
+    headers = sorted(p.name for p in (ROOT / "include").glob("*.h"))
+    src = ["#include <stdio.h>"] + [f'#include "{h}"' for h in headers]
+    src += ["typedef void (*entry_point)(void);", "static const entry_point entry_points[] = {"]
+    src += [f"    (entry_point){n}," for n in names]
+    src += ["};", "int main(void) {",
+            '    printf("%u\\n", (unsigned)(sizeof entry_points / sizeof entry_points[0]));', "    return 0;", "}"]
+    c = tmp_path / "abi.c"
+    c.write_text("\n".join(src) + "\n")
+    exe = tmp_path / "abi"
+    cmd = [gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"), str(c), "-L",
+           str(lib.parent), "-lplgpu_fem3d", f"-Wl,-rpath,{lib.parent}", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    assert int(out.stdout.strip()) == len(names)
