@@ -188,13 +188,20 @@ def profiled_traffic():
 # CPU baseline (the reference's default iterative path restated on the host)
 
 
-def cpu_baseline(size, cg_iterations):
-    from oracle import baseline as B
+def baseline_problem(size):
+    """The bench case as the oracle's problem (the reference's iterative algorithm includes
+    empty elements, fem_solver.hpp:182-189)."""
     from oracle import fem3d as O
     from plask_gb300 import structures as S
 
-    s = S.layered_c1(n=size)
-    prob = O.from_structure(s, empty_elements="include")
+    return O.from_structure(S.layered_c1(n=size), empty_elements="include")
+
+
+def cpu_baseline(size, cg_iterations, prob=None):
+    from oracle import baseline as B
+
+    if prob is None:
+        prob = baseline_problem(size)
     r = B.sample(prob, cg_iterations=cg_iterations)
     char_path = ROOT / "oracle" / "c1_iterations.json"
     loops, iters, note = None, None, ""
@@ -229,13 +236,14 @@ def run_reference(args):
     if rank != 0:
         return 0
     size = tuple(int(v) for v in args.size.split(","))
-    for _ in range(args.warmup):
-        pass  # the CPU sample has no warm-up effects worth a repeated 10 s run
+    prob = baseline_problem(size)
+    for _ in range(args.warmup):  # untimed samples of the same work
+        cpu_baseline(size, args.cpu_iterations, prob)
     vals, times = [], []
     last = None
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        last = cpu_baseline(size, args.cpu_iterations)
+        last = cpu_baseline(size, args.cpu_iterations, prob)
         times.append(time.perf_counter() - t0)
         vals.append(last["value"])
     v = statistics.median(vals)
