@@ -15,6 +15,7 @@ per element (canonical shape), e.g. :class:`StructureGeometry`.
 from __future__ import annotations
 
 import dataclasses
+import itertools
 import logging
 
 import numpy as np
@@ -183,6 +184,91 @@ def _nearest_axis(axis, x):
     lo = np.maximum(lb - 1, 0)
     take_lo = (lb == axis.size) | ((lb > 0) & (x - axis[lo] <= axis[hi] - x))
     return np.where(take_lo, lo, hi)
+
+
+# boundary tolerance of the masked meshes, um (plask/mesh/rectangular_masked_common.hpp:36)
+MASKED_MIN_DISTANCE = 1e-9
+
+
+def masked_element_search(axes, active, pts):
+    """The element of a masked mesh that holds each point, found as
+    RectangularMaskedMesh3D::prepareInterpolation finds it (rectangular_masked3d.cpp:68-112;
+    2D: rectangular_masked2d.cpp:58-89): the element around the point (the upper one when
+    the point lies on a node line) or, for a point within 1e-9 um of that element's
+    faces, the neighbour across the face, tried with axis 0 varying fastest.
+
+    ``axes``: the node axes; ``active``: canonical element mask (axis 0 last);
+    ``pts``: (m, len(axes)).  Returns the low node index of the element per axis and a
+    mask of the points that an included element holds (the others read NaN in the
+    reference).  The reference compares the third coordinate with the upper node of
+    axis 1 when it looks for the upper neighbour along axis 2 (rectangular_masked3d.cpp:107);
+    that comparison is kept."""
+    dims = len(axes)
+    m = len(pts)
+    inbox = np.ones(m, bool)
+    lo, hi_c = [], []
+    for d, a in enumerate(axes):
+        x = pts[:, d]
+        inbox &= (a[0] - x < MASKED_MIN_DISTANCE) & (x - a[-1] < MASKED_MIN_DISTANCE)
+        hi = np.searchsorted(a, x, side="right")  # findUpIndex, then clamped to an element
+        hi = np.where(hi >= a.size, a.size - 1, np.where(hi == 0, 1, hi))
+        lo.append(hi - 1)
+        hi_c.append(a[hi])
+    alt, has_alt = [], []
+    for d, a in enumerate(axes):
+        x = pts[:, d]
+        lo_c = a[lo[d]]
+        upper = hi_c[1] if d == 2 else hi_c[d]
+        near_lo = (lo[d] > 0) & (lo_c <= x) & (x < lo_c + MASKED_MIN_DISTANCE)
+        near_hi = ~near_lo & (lo[d] < a.size - 2) & (hi_c[d] - MASKED_MIN_DISTANCE < x) & (x <= upper)
+        alt.append(np.where(near_lo, lo[d] - 1, lo[d] + 1))
+        has_alt.append(near_lo | near_hi)
+    elem = [np.zeros(m, np.int64) for _ in range(dims)]
+    found = np.zeros(m, bool)
+    for tt in itertools.product((0, 1), repeat=dims):
+        t = tt[::-1]  # axis 0 fastest
+        valid = inbox & ~found
+        for d in range(dims):
+            if t[d]:
+                valid &= has_alt[d]
+        sel = np.flatnonzero(valid)
+        if sel.size == 0:
+            continue
+        idx = [(alt[d] if t[d] else lo[d])[sel] for d in range(dims)]
+        hit = active[tuple(idx[::-1])]
+        rows = sel[hit]
+        for d in range(dims):
+            elem[d][rows] = idx[d][hit]
+        found[rows] = True
+    return elem, found
+
+
+def masked_interpolate(axes, F, active, pts, method):
+    """Nodal values F (canonical, NaN off the masked mesh) at points, as the masked mesh
+    interpolates them (rectangular_masked3d.hpp:555-603): multilinear over the corners of
+    the holding element, or its nearest corner (the lower one on a tie); NaN where no
+    included element holds the point."""
+    dims = len(axes)
+    elem, found = masked_element_search(axes, active, pts)
+    out = np.full(len(pts), np.nan)
+    s = np.flatnonzero(found)
+    lo = [elem[d][s] for d in range(dims)]
+    x = [pts[s, d] for d in range(dims)]
+    a_lo = [axes[d][lo[d]] for d in range(dims)]
+    a_hi = [axes[d][lo[d] + 1] for d in range(dims)]
+    if method == "nearest":
+        idx = [np.where(x[d] - a_lo[d] <= a_hi[d] - x[d], lo[d], lo[d] + 1) for d in range(dims)]
+        out[s] = F[tuple(idx[::-1])]
+        return out
+    w = [(x[d] - a_lo[d]) / (a_hi[d] - a_lo[d]) for d in range(dims)]
+    val = np.zeros(s.size)
+    for c in itertools.product((0, 1), repeat=dims):
+        wt = np.ones(s.size)
+        for d in range(dims):
+            wt = wt * (w[d] if c[d] else 1.0 - w[d])
+        val += wt * F[tuple((lo[d] + c[d]) for d in range(dims))[::-1]]
+    out[s] = val
+    return out
 
 
 def _element_axis(axis, x):
@@ -461,13 +547,18 @@ class Static3D:
             full = vals[canon_idx]
         return full.reshape(self._mesh.shape)
 
-    def _active_mask_mesh_order(self):
-        mesh = self._mesh
-        mat = self._geometry.material_ids(mesh)
+    def _active_elements(self):
+        """Canonical mask of the masked mesh's elements (fem_solver.hpp:164-189: empty
+        elements are left out unless included, by default with the iterative algorithm)."""
+        mat = self._geometry.material_ids(self._mesh)
         mt = self._geometry.materials
         excl = self._empty_elements in ("exclude", "excluded") or (
             self._empty_elements == "default" and self._algorithm != "iterative")
-        act_el = ~mt.empty[mat] if excl else np.ones(mat.shape, bool)
+        return ~mt.empty[mat] if excl else np.ones(mat.shape, bool)
+
+    def _active_mask_mesh_order(self):
+        mesh = self._mesh
+        act_el = self._active_elements()
         n2, n1, n0 = mesh.shape
         used = np.zeros(mesh.shape, bool)
         for ck in (0, 1):
@@ -485,8 +576,14 @@ class Static3D:
         if dst_mesh is None:
             return T
         pts = _points(dst_mesh)
-        if _check_interpolation(interpolation) == "nearest":
-            # the nearest node (rectilinear3d.hpp:853-860); masked-out nodes read 300 K
+        method = _check_interpolation(interpolation)
+        active = self._active_elements()
+        if not np.all(active):
+            # the masked mesh's interpolation; NaN (no included element) reads 300 K (SafeData)
+            out = masked_interpolate(self._mesh.axes, T, active, pts, method)
+            return np.where(np.isnan(out), 300.0, out)
+        if method == "nearest":
+            # the nearest node (rectilinear3d.hpp:853-860)
             i0, i1, i2 = (_nearest_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
             out = T[i2, i1, i0]
             return np.where(np.isnan(out), 300.0, out)

@@ -20,7 +20,7 @@ import numpy as np
 from . import _native
 from .mesh import RectangularMesh2D, mesh_index2d, to_mesh_order2d
 from .thermal import (BadInput, BoundaryConditions, IterativeParams, MaterialTable, Provider, _check_interpolation,
-                      _element_axis, _nearest_axis, load_state, save_state)
+                      _element_axis, _nearest_axis, load_state, masked_interpolate, save_state)
 
 log = logging.getLogger("plask_gb300.thermal2d")
 
@@ -287,13 +287,17 @@ class Static2D:
         """Start the next ``compute()`` from a checkpointed field (thermal.load_state)."""
         load_state(self, path)
 
-    def _active_mask_mesh_order(self):
-        mesh = self._mesh
-        mat = self._geometry.material_ids(mesh)
+    def _active_elements(self):
+        """Canonical mask of the masked mesh's elements (fem_solver.hpp:164-189)."""
+        mat = self._geometry.material_ids(self._mesh)
         mt = self._geometry.materials
         excl = self._empty_elements in ("exclude", "excluded") or (
             self._empty_elements == "default" and self._algorithm != "iterative")
-        act = ~mt.empty[mat] if excl else np.ones(mat.shape, bool)
+        return ~mt.empty[mat] if excl else np.ones(mat.shape, bool)
+
+    def _active_mask_mesh_order(self):
+        mesh = self._mesh
+        act = self._active_elements()
         n1, n0 = mesh.shape
         used = np.zeros(mesh.shape, bool)
         for cj in (0, 1):
@@ -321,7 +325,13 @@ class Static2D:
         if dst_mesh is None:
             return T
         pts = _points2d(dst_mesh)
-        if _check_interpolation(interpolation) == "nearest":
+        method = _check_interpolation(interpolation)
+        active = self._active_elements()
+        if not np.all(active):
+            # the masked mesh's interpolation; NaN (no included element) reads 300 K (SafeData)
+            out = masked_interpolate(self._mesh.axes, T, active, pts, method)
+            return np.where(np.isnan(out), 300.0, out)
+        if method == "nearest":
             i0, i1 = (_nearest_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
             out = T[i1, i0]
             return np.where(np.isnan(out), 300.0, out)

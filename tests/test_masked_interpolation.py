@@ -1,0 +1,84 @@
+"""Providers on masked meshes (CPU): the element search and interpolation of
+RectangularMaskedMesh2D/3D (plask/mesh/rectangular_masked3d.cpp:68-112,
+rectangular_masked2d.cpp:58-89, rectangular_masked3d.hpp:555-603) that the thermal
+providers use when empty elements are left out, with NaN read as 300 K by the solver
+(SafeData, solvers/thermal/static/therm3d.cpp:387-395)."""
+import numpy as np
+
+from plask_gb300.thermal import MASKED_MIN_DISTANCE, masked_element_search, masked_interpolate
+
+AX = (np.array([0.0, 1.0, 2.0, 4.0]), np.array([0.0, 0.5, 1.5]), np.array([10.0, 11.0, 13.0, 14.0]))
+
+
+def _field(axes, coef):
+    grids = np.meshgrid(*axes[::-1], indexing="ij")[::-1]  # canonical (axis 2, 1, 0)
+    return coef[0] + sum(c * g for c, g in zip(coef[1:], grids))
+
+
+def test_linear_field_is_reproduced_in_included_elements():
+    active = np.ones((3, 2, 3), bool)
+    active[1, 1, 2] = False
+    F = _field(AX, (300.0, 2.0, -3.0, 0.5))
+    rng = np.random.default_rng(1)
+    pts = np.stack([rng.uniform(a[0], a[-1], 400) for a in AX], axis=1)
+    elem, found = masked_element_search(AX, active, pts)
+    out = masked_interpolate(AX, F, active, pts, "linear")
+    want = 300.0 + 2.0 * pts[:, 0] - 3.0 * pts[:, 1] + 0.5 * pts[:, 2]
+    assert np.allclose(out[found], want[found], rtol=0, atol=1e-12)
+    # points inside the left-out element read NaN
+    inside = (pts[:, 0] > 2.0) & (pts[:, 1] > 0.5) & (pts[:, 2] > 11.0) & (pts[:, 2] < 13.0)
+    assert inside.any() and np.all(~found[inside]) and np.all(np.isnan(out[inside]))
+
+
+def test_hole_element_reads_nan_although_its_corners_are_on_the_mesh():
+    ax = (np.arange(4.0), np.arange(4.0), np.arange(4.0))
+    active = np.ones((3, 3, 3), bool)
+    active[1, 1, 1] = False  # every corner of the hole still belongs to other elements
+    F = _field(ax, (1.0, 1.0, 1.0, 1.0))
+    out = masked_interpolate(ax, F, active, np.array([[1.5, 1.5, 1.5], [0.5, 1.5, 1.5]]), "linear")
+    assert np.isnan(out[0]) and out[1] == 1.0 + 0.5 + 1.5 + 1.5
+
+
+def test_face_points_take_the_included_neighbour():
+    ax = (np.arange(3.0), np.arange(2.0), np.arange(2.0))
+    for act_left in (True, False):
+        active = np.array([[[act_left, not act_left]]])
+        F = _field(ax, (5.0, 1.0, 0.0, 0.0))
+        # on the node line x = 1 and a hair to either side of it
+        for x in (1.0, 1.0 - 0.5 * MASKED_MIN_DISTANCE, 1.0 + 0.5 * MASKED_MIN_DISTANCE):
+            elem, found = masked_element_search(ax, active, np.array([[x, 0.5, 0.5]]))
+            assert found[0] and elem[0][0] == (0 if act_left else 1)
+        # a point clearly inside the left-out element
+        elem, found = masked_element_search(ax, active, np.array([[1.5 if act_left else 0.5, 0.5, 0.5]]))
+        assert not found[0]
+
+
+def test_box_tolerance():
+    active = np.ones((3, 2, 3), bool)
+    eps = 0.5 * MASKED_MIN_DISTANCE
+    pts = np.array([[-eps, 0.2, 12.0], [4.0 + eps, 0.2, 12.0], [-3 * eps, 0.2, 12.0], [1.0, 0.2, 14.0 + 3 * eps]])
+    _, found = masked_element_search(AX, active, pts)
+    assert found.tolist() == [True, True, False, False]
+
+
+def test_nearest_corner_of_the_holding_element_lower_on_a_tie():
+    ax = (np.array([0.0, 2.0, 4.0]), np.array([0.0, 1.0]))
+    active = np.array([[True, False]])
+    F = np.array([[1.0, 2.0, 3.0], [10.0, 20.0, 30.0]])
+    pts = np.array([[1.0, 0.5], [1.2, 0.2], [0.9, 0.7], [3.0, 0.5], [2.0, 0.5]])
+    out = masked_interpolate(ax, F, active, pts, "nearest")
+    # ties go to the lower node; x = 2 lies on the face of the included element
+    assert out[0] == 1.0 and out[1] == 2.0 and out[2] == 10.0 and np.isnan(out[3]) and out[4] == 2.0
+
+
+def test_upper_neighbour_along_axis_2_compares_with_axis_1():
+    """rectangular_masked3d.cpp:107 compares the third coordinate with the upper node of
+    axis 1: a point a hair below a z node line does not find an included element above
+    it when z exceeds that y coordinate."""
+    ax_low_z = (np.arange(2.0), np.array([0.0, 5.0]), np.array([0.0, 1.0, 2.0]))
+    ax_high_z = (np.arange(2.0), np.array([0.0, 0.5]), np.array([0.0, 1.0, 2.0]))
+    active = np.array([[[False]], [[True]]])  # the lower element left out, the upper one included
+    z = 1.0 - 0.5 * MASKED_MIN_DISTANCE
+    _, found_low = masked_element_search(ax_low_z, active, np.array([[0.5, 0.2, z]]))
+    _, found_high = masked_element_search(ax_high_z, active, np.array([[0.5, 0.2, z]]))
+    assert found_low[0] and not found_high[0]
