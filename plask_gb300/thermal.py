@@ -271,6 +271,55 @@ def masked_interpolate(axes, F, active, pts, method):
     return out
 
 
+def masked_element_interpolate(axes, Q, active, pts, method):
+    """Element values Q (canonical, components last) at points on a masked mesh, as its
+    element mesh interpolates them (rectangular_masked3d.hpp:277-333,
+    rectangular_masked2d.hpp:196-237): the holding element's value (nearest), or
+    multilinear between its midpoint and the neighbouring midpoints on the point's side,
+    a left-out neighbour along one axis taking the holding element's value and one
+    along several axes the sum of the single-axis values less the holding value for
+    each axis beyond the first; NaN where no included element holds the point."""
+    dims = len(axes)
+    elem, found = masked_element_search(axes, active, pts)
+    out = np.full((len(pts),) + Q.shape[dims:], np.nan)
+    s = np.flatnonzero(found)
+    e = [elem[d][s] for d in range(dims)]
+    if method == "nearest":
+        out[s] = Q[tuple(e[::-1])]
+        return out
+    mids = [0.5 * (a[1:] + a[:-1]) for a in axes]
+    x = [pts[s, d] for d in range(dims)]
+    pa = [mids[d][e[d]] for d in range(dims)]
+    step = [np.where(x[d] < pa[d], np.where(e[d] == 0, 0, -1), np.where(e[d] + 2 == axes[d].size, 0, 1))
+            for d in range(dims)]
+    base = Q[tuple(e[::-1])]
+    corner = {(0,) * dims: base}
+    # corners in order of the number of stepped axes, so that the single-axis values exist
+    for c in sorted(itertools.product((0, 1), repeat=dims), key=sum):
+        if sum(c) == 0:
+            continue
+        idx = [e[d] + c[d] * step[d] for d in range(dims)]
+        inc = active[tuple(idx[::-1])]
+        val = Q[tuple(idx[::-1])]
+        if sum(c) == 1:
+            sub = base
+        else:
+            singles = [corner[tuple(int(k == d) for k in range(dims))] for d in range(dims) if c[d]]
+            sub = sum(singles) - (len(singles) - 1) * base
+        inc = inc.reshape(inc.shape + (1,) * (base.ndim - 1))
+        corner[c] = np.where(inc, val, sub)
+    pb = [mids[d][e[d] + step[d]] + (step[d] == 0) for d in range(dims)]
+    t = [(x[d] - pa[d]) / (pb[d] - pa[d]) for d in range(dims)]
+    val = np.zeros_like(base)
+    for c, v in corner.items():
+        wt = np.ones(s.size)
+        for d in range(dims):
+            wt = wt * (t[d] if c[d] else 1.0 - t[d])
+        val += wt.reshape(wt.shape + (1,) * (base.ndim - 1)) * v
+    out[s] = val
+    return out
+
+
 def _element_axis(axis, x):
     """Index of the element holding x, clamped to the mesh (findUpIndex - 1)."""
     return np.clip(np.searchsorted(axis, x, side="right") - 1, 0, axis.size - 2)
@@ -606,6 +655,11 @@ class Static3D:
             return q
         mids = [0.5 * (a[1:] + a[:-1]) for a in self._mesh.axes]
         pts = _points(dst_mesh)
+        active = self._active_elements()
+        if not np.all(active):
+            # the masked element mesh's interpolation; NaN reads 0 (SafeData)
+            out = masked_element_interpolate(self._mesh.axes, q, active, pts, _check_interpolation(interpolation))
+            return np.nan_to_num(out)
         if _check_interpolation(interpolation) == "nearest":
             # the element holding the point (the reference's element-mesh lookup,
             # rectilinear3d.hpp:282-297, searches axis 0 for the second coordinate as well;

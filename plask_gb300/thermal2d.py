@@ -20,7 +20,8 @@ import numpy as np
 from . import _native
 from .mesh import RectangularMesh2D, mesh_index2d, to_mesh_order2d
 from .thermal import (BadInput, BoundaryConditions, IterativeParams, MaterialTable, Provider, _check_interpolation,
-                      _element_axis, _nearest_axis, load_state, masked_interpolate, save_state)
+                      _element_axis, _nearest_axis, load_state, masked_element_interpolate, masked_interpolate,
+                      save_state)
 
 log = logging.getLogger("plask_gb300.thermal2d")
 
@@ -354,6 +355,11 @@ class Static2D:
             return q
         mids = [0.5 * (a[1:] + a[:-1]) for a in self._mesh.axes]
         pts = _points2d(dst_mesh)
+        active = self._active_elements()
+        if not np.all(active):
+            # the masked element mesh's interpolation; NaN reads 0 (SafeData)
+            out = masked_element_interpolate(self._mesh.axes, q, active, pts, _check_interpolation(interpolation))
+            return np.nan_to_num(out)
         if _check_interpolation(interpolation) == "nearest":
             i0, i1 = (_element_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
             out = q[i1, i0].copy()

@@ -5,7 +5,8 @@ providers use when empty elements are left out, with NaN read as 300 K by the so
 (SafeData, solvers/thermal/static/therm3d.cpp:387-395)."""
 import numpy as np
 
-from plask_gb300.thermal import MASKED_MIN_DISTANCE, masked_element_search, masked_interpolate
+from plask_gb300.thermal import (MASKED_MIN_DISTANCE, masked_element_interpolate, masked_element_search,
+                                  masked_interpolate)
 
 AX = (np.array([0.0, 1.0, 2.0, 4.0]), np.array([0.0, 0.5, 1.5]), np.array([10.0, 11.0, 13.0, 14.0]))
 
@@ -82,3 +83,43 @@ def test_upper_neighbour_along_axis_2_compares_with_axis_1():
     _, found_low = masked_element_search(ax_low_z, active, np.array([[0.5, 0.2, z]]))
     _, found_high = masked_element_search(ax_high_z, active, np.array([[0.5, 0.2, z]]))
     assert found_low[0] and not found_high[0]
+
+
+def _element_field(axes, coef):
+    mids = [0.5 * (a[1:] + a[:-1]) for a in axes]
+    return _field(mids, coef)
+
+
+def test_element_values_linear_between_midpoints_with_left_out_diagonals():
+    """A linear field over the midpoints is reproduced where the point lies between included
+    midpoints; a left-out diagonal neighbour takes the sum of the axis neighbours less the
+    holding value, which is exact for a linear field."""
+    ax = (np.arange(5.0), np.arange(4.0) * 2.0, np.arange(4.0) * 0.5)
+    active = np.ones((3, 3, 4), bool)
+    active[2, 2, 3] = False  # a diagonal neighbour of the element (2, 1, 1) for points toward it
+    Q = _element_field(ax, (1.0, 0.3, -0.2, 4.0))
+    pts = np.array([[2.8, 3.4, 0.9], [1.6, 2.5, 0.3], [2.6, 3.8, 1.1]])
+    out = masked_element_interpolate(ax, Q, active, pts, "linear")
+    want = 1.0 + 0.3 * pts[:, 0] - 0.2 * pts[:, 1] + 4.0 * pts[:, 2]
+    assert np.allclose(out, want, rtol=0, atol=1e-12)
+
+
+def test_element_values_left_out_axis_neighbour_and_edges_hold_the_element_value():
+    ax = (np.arange(4.0), np.arange(2.0))
+    active = np.array([[True, True, False]])
+    Q = np.array([[10.0, 20.0, 99.0]])
+    pts = np.array([[1.8, 0.5], [0.2, 0.5], [1.2, 0.5], [2.5, 0.5]])
+    out = masked_element_interpolate(ax, Q, active, pts, "linear")
+    # toward the left-out element: the holding value; below the first midpoint: the edge value;
+    # between the included midpoints 0.5 and 1.5: linear; inside the left-out element: NaN
+    assert out[0] == 20.0 and out[1] == 10.0 and np.isclose(out[2], 10.0 + 10.0 * 0.7) and np.isnan(out[3])
+    near = masked_element_interpolate(ax, Q, active, pts, "nearest")
+    assert near[0] == 20.0 and near[1] == 10.0 and near[2] == 20.0 and np.isnan(near[3])
+
+
+def test_element_values_with_components():
+    ax = (np.arange(3.0), np.arange(3.0))
+    active = np.array([[True, True], [True, False]])
+    Q = np.stack([_element_field(ax, (0.0, 1.0, 0.0)), _element_field(ax, (0.0, 0.0, 1.0))], axis=-1)
+    out = masked_element_interpolate(ax, Q, active, np.array([[0.9, 0.7], [1.5, 1.5]]), "linear")
+    assert np.allclose(out[0], [0.9, 0.7]) and np.all(np.isnan(out[1]))
