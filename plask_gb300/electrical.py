@@ -32,7 +32,8 @@ import numpy as np
 from . import _native
 from .mesh import RectangularMesh3D, to_mesh_order
 from .thermal import BadInput, BoundaryConditions, ComputationError, IterativeParams, Provider, Static3D
-from .thermal import _points, _trilinear
+from .thermal import (_check_interpolation, _element_axis, _nearest_axis, _points, _trilinear,
+                      masked_element_interpolate, masked_interpolate)
 
 log = logging.getLogger("plask_gb300.electrical")
 
@@ -118,7 +119,7 @@ class TemperatureReceiver:
                 eidx = v._mesh.element_index_array().ravel()
                 return t[eidx].reshape(v._mesh.element_shape)
             pts = mesh.element_midpoints().reshape(-1, 3)
-            return _trilinear(v._mesh.axes, v._full_temperature(), pts, fill=300.0).reshape(mesh.element_shape)
+            return v._get_temperatures(pts).reshape(mesh.element_shape)  # the thermal provider
         if isinstance(v, Provider):
             mids = mesh.element_midpoints().reshape(-1, 3)
             return np.asarray(v(mids), np.float64).reshape(mesh.element_shape)
@@ -483,15 +484,38 @@ class Shockley3D:
         return self._element_field(self._elec.conductivity(), 2)
 
     def _get_voltage(self, dst_mesh, interpolation="linear"):
-        """Potential on a destination mesh (electr3d.cpp:507-515): trilinear."""
+        """Potential on a destination mesh (electr3d.cpp:507-515): trilinear or the nearest
+        node; on a masked mesh its element search, NaN where no included element holds the
+        point."""
         V = self._full_potential()
         if dst_mesh is None:
             return V
-        return _trilinear(self._mesh.axes, V, _points(dst_mesh), fill=np.nan)
+        pts = _points(dst_mesh)
+        method = _check_interpolation(interpolation)
+        active = self._active_elements()
+        if not np.all(active):
+            return masked_interpolate(self._mesh.axes, V, active, pts, method)
+        if method == "nearest":
+            i0, i1, i2 = (_nearest_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
+            return V[i2, i1, i0]
+        return _trilinear(self._mesh.axes, V, pts, fill=np.nan)
 
-    def _element_interp(self, q, dst_mesh=None, pts=None):
+    def _element_interp(self, q, dst_mesh=None, pts=None, interpolation="linear"):
+        """Element values at points, 0 outside (electr3d.cpp:517-555): over the element
+        midpoints, or the holding element; on a masked mesh the masked element mesh's
+        interpolation with NaN read as 0."""
         mids = [0.5 * (a[1:] + a[:-1]) for a in self._mesh.axes]
         pts = _points(dst_mesh) if pts is None else pts
+        method = _check_interpolation(interpolation)
+        active = self._active_elements()
+        if not np.all(active):
+            return np.nan_to_num(masked_element_interpolate(self._mesh.axes, q, active, pts, method))
+        if method == "nearest":
+            i0, i1, i2 = (_element_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
+            out = q[i2, i1, i0].copy()
+            inside = np.all([(pts[:, d] >= a[0]) & (pts[:, d] <= a[-1]) for d, a in enumerate(self._mesh.axes)], axis=0)
+            out[~inside] = 0.0
+            return out
         if q.ndim == 3:
             return _trilinear(mids, q, pts, fill=0.0, clamp=True, box=self._mesh.axes)
         return np.stack([_trilinear(mids, q[..., c], pts, fill=0.0, clamp=True, box=self._mesh.axes)
@@ -500,28 +524,24 @@ class Shockley3D:
     def _get_current_density(self, dst_mesh, interpolation="linear"):
         """Current density on a destination mesh (electr3d.cpp:517-535): 0 outside."""
         j = np.nan_to_num(self.current_densities())
-        return j if dst_mesh is None else self._element_interp(j, dst_mesh)
+        return j if dst_mesh is None else self._element_interp(j, dst_mesh, interpolation=interpolation)
 
     def _get_heat(self, dst_mesh, interpolation="linear"):
         """Heat density on a destination mesh (electr3d.cpp:537-555): 0 outside."""
         h = np.nan_to_num(self.heat_densities())
-        return h if dst_mesh is None else self._element_interp(h, dst_mesh)
+        return h if dst_mesh is None else self._element_interp(h, dst_mesh, interpolation=interpolation)
+
+    def _active_elements(self):
+        mat = self._geometry.material_ids(self._mesh)
+        return ~self._geometry.materials.empty[mat] if self._excluding() else np.ones(mat.shape, bool)
 
     def _get_conductivity(self, dst_mesh, interpolation="nearest"):
-        """Conductivity of the element holding each point (electr3d.cpp:557-565)."""
+        """Conductivity of the element holding each point (electr3d.cpp:557-565): the masked
+        element mesh's nearest lookup, NaN where no included element holds the point."""
         c = self.conductivities()
         if dst_mesh is None:
             return c
-        pts = _points(dst_mesh)
-        idx = []
-        ok = np.ones(len(pts), bool)
-        for d, a in enumerate(self._mesh.axes):
-            u = np.searchsorted(a, pts[:, d], side="left")
-            ok &= (u > 0) & (u < a.size)
-            idx.append(np.clip(u - 1, 0, a.size - 2))
-        out = c[idx[2], idx[1], idx[0]]
-        out[~ok] = np.nan
-        return out
+        return masked_element_interpolate(self._mesh.axes, c, self._active_elements(), _points(dst_mesh), "nearest")
 
 
 class ThermoElectric3D:

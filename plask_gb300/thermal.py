@@ -320,6 +320,20 @@ def masked_element_interpolate(axes, Q, active, pts, method):
     return out
 
 
+def conductivity_elements(axes, pts):
+    """Element of each point for the conductivity providers (ThermalConductivityData::at,
+    therm3d.cpp:421-435, therm2d.cpp:581-594): findUpIndex (the first node above the
+    coordinate) less one per axis, so a point on a node line takes the upper element; a
+    point below the first node or on or above the last one has none.  Returns the element
+    indices per axis and the mask of points that have one."""
+    idx, ok = [], np.ones(len(pts), bool)
+    for d, a in enumerate(axes):
+        u = np.searchsorted(a, pts[:, d], side="right")
+        ok &= (u > 0) & (u < a.size)
+        idx.append(np.clip(u - 1, 0, a.size - 2))
+    return idx, ok
+
+
 def _element_axis(axis, x):
     """Index of the element holding x, clamped to the mesh (findUpIndex - 1)."""
     return np.clip(np.searchsorted(axis, x, side="right") - 1, 0, axis.size - 2)
@@ -681,13 +695,7 @@ class Static3D:
         k = k[eidx].reshape(self._mesh.element_shape + (2,))
         if dst_mesh is None:
             return k
-        pts = _points(dst_mesh)
-        idx = []
-        ok = np.ones(len(pts), bool)
-        for d, a in enumerate(self._mesh.axes):
-            u = np.searchsorted(a, pts[:, d], side="left")  # findUpIndex
-            ok &= (u > 0) & (u < a.size)
-            idx.append(np.clip(u - 1, 0, a.size - 2))
+        idx, ok = conductivity_elements(self._mesh.axes, _points(dst_mesh))
         out = k[idx[2], idx[1], idx[0]]
         out[~ok] = np.nan
         return out

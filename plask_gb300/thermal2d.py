@@ -20,8 +20,8 @@ import numpy as np
 from . import _native
 from .mesh import RectangularMesh2D, mesh_index2d, to_mesh_order2d
 from .thermal import (BadInput, BoundaryConditions, IterativeParams, MaterialTable, Provider, _check_interpolation,
-                      _element_axis, _nearest_axis, load_state, masked_element_interpolate, masked_interpolate,
-                      save_state)
+                      _element_axis, _nearest_axis, conductivity_elements, load_state, masked_element_interpolate,
+                      masked_interpolate, save_state)
 
 log = logging.getLogger("plask_gb300.thermal2d")
 
@@ -376,12 +376,7 @@ class Static2D:
         k = k[eidx].reshape(self._mesh.element_shape + (2,))
         if dst_mesh is None:
             return k
-        pts = _points2d(dst_mesh)
-        idx, ok = [], np.ones(len(pts), bool)
-        for d, a in enumerate(self._mesh.axes):
-            u = np.searchsorted(a, pts[:, d], side="left")  # findUpIndex
-            ok &= (u > 0) & (u < a.size)
-            idx.append(np.clip(u - 1, 0, a.size - 2))
+        idx, ok = conductivity_elements(self._mesh.axes, _points2d(dst_mesh))
         out = k[idx[1], idx[0]].copy()
         out[~ok] = np.nan
         return out

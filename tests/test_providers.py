@@ -4,7 +4,7 @@ axis) and the element lookup (findUpIndex - 1, clamped)."""
 import numpy as np
 import pytest
 
-from plask_gb300.thermal import BadInput, _check_interpolation, _element_axis, _nearest_axis
+from plask_gb300.thermal import BadInput, _check_interpolation, _element_axis, _nearest_axis, conductivity_elements
 
 
 def test_nearest_node_rule():
@@ -24,3 +24,13 @@ def test_interpolation_names():
     assert _check_interpolation("nearest") == "nearest"
     with pytest.raises(BadInput):
         _check_interpolation("spline")
+
+
+def test_conductivity_lookup_takes_the_upper_element_and_none_at_the_last_node():
+    """ThermalConductivityData::at (therm3d.cpp:421-435): findUpIndex - 1 per axis, NaN
+    when findUpIndex is 0 or the axis size."""
+    a = np.array([0.0, 1.0, 3.0, 4.0])
+    pts = np.array([[-0.5], [0.0], [0.5], [1.0], [3.9], [4.0], [5.0]])
+    idx, ok = conductivity_elements((a,), pts)
+    assert ok.tolist() == [False, True, True, True, True, False, False]
+    assert idx[0][ok].tolist() == [0, 0, 1, 2]
