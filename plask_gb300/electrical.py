@@ -485,8 +485,8 @@ class Shockley3D:
 
     def _get_voltage(self, dst_mesh, interpolation="linear"):
         """Potential on a destination mesh (electr3d.cpp:507-515): trilinear or the nearest
-        node; on a masked mesh its element search, NaN where no included element holds the
-        point."""
+        node, the edge values continuing outside the mesh; on a masked mesh its element
+        search, NaN where no included element holds the point."""
         V = self._full_potential()
         if dst_mesh is None:
             return V
@@ -498,7 +498,7 @@ class Shockley3D:
         if method == "nearest":
             i0, i1, i2 = (_nearest_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
             return V[i2, i1, i0]
-        return _trilinear(self._mesh.axes, V, pts, fill=np.nan)
+        return _trilinear(self._mesh.axes, V, pts, fill=None)
 
     def _element_interp(self, q, dst_mesh=None, pts=None, interpolation="linear"):
         """Element values at points, 0 outside (electr3d.cpp:517-555): over the element

@@ -631,7 +631,9 @@ class Static3D:
         return to_mesh_order(used, mesh.ordering)
 
     def _get_temperatures(self, dst_mesh, interpolation="linear"):
-        """Temperatures on a destination mesh (therm3d.cpp:387-395): trilinear, 300 K outside."""
+        """Temperatures on a destination mesh (therm3d.cpp:387-395): trilinear or the nearest
+        node, the edge values continuing outside the mesh; on a masked mesh its element
+        search, 300 K where no included element holds the point."""
         if self._fem is None:
             n = len(dst_mesh) if dst_mesh is not None else 0
             return np.full(n, self.inittemp)
@@ -650,7 +652,7 @@ class Static3D:
             i0, i1, i2 = (_nearest_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
             out = T[i2, i1, i0]
             return np.where(np.isnan(out), 300.0, out)
-        return _trilinear(self._mesh.axes, T, pts, fill=300.0)
+        return _trilinear(self._mesh.axes, T, pts, fill=None)
 
     def heat_fluxes(self):
         """Per-element heat flux [W/m^2], canonical (ne2, ne1, ne0, 3) (saveHeatFluxes)."""
@@ -660,7 +662,9 @@ class Static3D:
         return q[eidx].reshape(self._mesh.element_shape + (3,))
 
     def _get_heat_fluxes(self, dst_mesh, interpolation="linear"):
-        """Heat flux on a destination mesh (therm3d.cpp:398-411): linear over element midpoints, 0 outside."""
+        """Heat flux on a destination mesh (therm3d.cpp:398-411): linear over the element
+        midpoints or the holding element, the edge values continuing outside; on a masked
+        mesh its element mesh's interpolation, 0 where no included element holds the point."""
         if self._fem is None:
             n = len(dst_mesh) if dst_mesh is not None else 0
             return np.zeros((n, 3))
@@ -679,13 +683,8 @@ class Static3D:
             # rectilinear3d.hpp:282-297, searches axis 0 for the second coordinate as well;
             # that slip is not reproduced)
             i0, i1, i2 = (_element_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
-            out = q[i2, i1, i0].copy()
-            inside = np.all([(pts[:, d] >= a[0]) & (pts[:, d] <= a[-1]) for d, a in enumerate(self._mesh.axes)], axis=0)
-            out[~inside] = 0.0
-            return out
-        out = np.stack([_trilinear(mids, q[..., c], pts, fill=0.0, clamp=True, box=self._mesh.axes)
-                        for c in range(3)], axis=-1)
-        return out
+            return q[i2, i1, i0].copy()
+        return np.stack([_trilinear(mids, q[..., c], pts, fill=None) for c in range(3)], axis=-1)
 
     def _get_conductivity(self, dst_mesh, interpolation="linear"):
         """(k_xy, k_z) of the element holding each point (therm3d.cpp:421-435)."""
@@ -773,7 +772,10 @@ def _points(dst):
 
 
 def _trilinear(axes, F, pts, fill, clamp=False, box=None):
-    """Trilinear interpolation of canonical F (n2, n1, n0) at points (m, 3)."""
+    """Trilinear interpolation of canonical F (n2, n1, n0) at points (m, 3).  Outside the
+    axes the edge values continue (prepareInterpolationForAxis, plask/mesh/axis1d.cpp:99-154,
+    gives both bracketing nodes the edge index); ``fill`` (unless None) replaces the values
+    of points outside the axes (or outside ``box`` with ``clamp``)."""
     ii, ww, ok = [], [], np.ones(len(pts), bool)
     for d in range(3):
         a = axes[d]
@@ -798,7 +800,8 @@ def _trilinear(axes, F, pts, fill, clamp=False, box=None):
                 j = np.minimum(ii[1] + cj, F.shape[1] - 1)
                 i = np.minimum(ii[0] + ci, F.shape[2] - 1)
                 out += wt * F[k, j, i]
-    out[~ok] = fill
+    if fill is not None:
+        out[~ok] = fill
     return out
 
 

@@ -83,7 +83,9 @@ def _points2d(dst):
 
 
 def _bilinear(axes, F, pts, fill, box=None):
-    """Bilinear interpolation of canonical F (n1, n0) at points (m, 2); ``fill`` outside."""
+    """Bilinear interpolation of canonical F (n1, n0) at points (m, 2); outside the axes
+    the edge values continue (plask/mesh/axis1d.cpp:99-154), or ``fill`` (unless None)
+    outside the axes (``box``)."""
     ii, ww, ok = [], [], np.ones(len(pts), bool)
     for d in range(2):
         a = axes[d]
@@ -99,7 +101,8 @@ def _bilinear(axes, F, pts, fill, box=None):
         for ci in (0, 1):
             wt = (ww[0] if ci else 1 - ww[0]) * (ww[1] if cj else 1 - ww[1])
             out += wt * F[np.minimum(ii[1] + cj, F.shape[0] - 1), np.minimum(ii[0] + ci, F.shape[1] - 1)]
-    out[~ok] = fill
+    if fill is not None:
+        out[~ok] = fill
     return out
 
 
@@ -318,7 +321,9 @@ class Static2D:
         return vals[idx].reshape(self._mesh.shape)
 
     def _get_temperatures(self, dst_mesh, interpolation="linear"):
-        """Temperatures on a destination mesh or points (therm2d.cpp:544-553): bilinear, 300 K outside."""
+        """Temperatures on a destination mesh or points (therm2d.cpp:544-553): bilinear or the
+        nearest node, the edge values continuing outside the mesh; on a masked mesh its
+        element search, 300 K where no included element holds the point."""
         if self._fem is None:
             n = len(dst_mesh) if dst_mesh is not None else 0
             return np.full(n, self.inittemp)
@@ -336,7 +341,7 @@ class Static2D:
             i0, i1 = (_nearest_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
             out = T[i1, i0]
             return np.where(np.isnan(out), 300.0, out)
-        return _bilinear(self._mesh.axes, T, pts, fill=300.0)
+        return _bilinear(self._mesh.axes, T, pts, fill=None)
 
     def heat_fluxes(self):
         """Per-element heat flux [W/m^2], canonical (ne1, ne0, 2) (saveHeatFluxes)."""
@@ -346,7 +351,9 @@ class Static2D:
         return q[eidx].reshape(self._mesh.element_shape + (2,))
 
     def _get_heat_fluxes(self, dst_mesh, interpolation="linear"):
-        """Heat flux at points (therm2d.cpp:556-571): bilinear over element midpoints, 0 outside the mesh."""
+        """Heat flux at points (therm2d.cpp:556-571): bilinear over the element midpoints or the
+        holding element, the edge values continuing outside; on a masked mesh its element
+        mesh's interpolation, 0 where no included element holds the point."""
         if self._fem is None:
             n = len(dst_mesh) if dst_mesh is not None else 0
             return np.zeros((n, 2))
@@ -362,11 +369,8 @@ class Static2D:
             return np.nan_to_num(out)
         if _check_interpolation(interpolation) == "nearest":
             i0, i1 = (_element_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
-            out = q[i1, i0].copy()
-            inside = np.all([(pts[:, d] >= a[0]) & (pts[:, d] <= a[-1]) for d, a in enumerate(self._mesh.axes)], axis=0)
-            out[~inside] = 0.0
-            return out
-        return np.stack([_bilinear(mids, q[..., c], pts, fill=0.0, box=self._mesh.axes) for c in range(2)], axis=-1)
+            return q[i1, i0].copy()
+        return np.stack([_bilinear(mids, q[..., c], pts, fill=None) for c in range(2)], axis=-1)
 
     def _get_conductivity(self, dst_mesh, interpolation="linear"):
         """(k_0, k_1) of the element holding each point (therm2d.cpp:574-597), NaN outside."""

@@ -34,3 +34,21 @@ def test_conductivity_lookup_takes_the_upper_element_and_none_at_the_last_node()
     idx, ok = conductivity_elements((a,), pts)
     assert ok.tolist() == [False, True, True, True, True, False, False]
     assert idx[0][ok].tolist() == [0, 0, 1, 2]
+
+
+def test_full_mesh_interpolation_continues_the_edge_values_outside():
+    """prepareInterpolationForAxis (plask/mesh/axis1d.cpp:99-154) gives both bracketing
+    nodes the edge index outside an axis, so a full mesh's linear interpolation returns
+    the edge values there (no NaN for the solver's SafeData to replace)."""
+    from plask_gb300.thermal import _trilinear
+    from plask_gb300.thermal2d import _bilinear
+
+    ax = (np.array([0.0, 1.0, 2.0]), np.array([0.0, 2.0]), np.array([0.0, 1.0]))
+    F = np.arange(12, dtype=float).reshape(2, 2, 3)
+    pts = np.array([[-5.0, 1.0, 0.5], [9.0, 1.0, 0.5], [0.5, -1.0, 3.0]])
+    out = _trilinear(ax, F, pts, fill=None)
+    inside = _trilinear(ax, F, np.array([[0.0, 1.0, 0.5], [2.0, 1.0, 0.5], [0.5, 0.0, 1.0]]), fill=None)
+    np.testing.assert_allclose(out, inside)
+    G = F[0]
+    out2 = _bilinear(ax[:2], G, np.array([[-1.0, 0.5], [3.0, 5.0]]), fill=None)
+    np.testing.assert_allclose(out2, _bilinear(ax[:2], G, np.array([[0.0, 0.5], [2.0, 2.0]]), fill=None))
