@@ -33,7 +33,7 @@ from . import _native
 from .mesh import RectangularMesh3D, to_mesh_order
 from .thermal import BadInput, BoundaryConditions, ComputationError, IterativeParams, Provider, Static3D
 from .thermal import (_check_interpolation, _element_axis, _nearest_axis, _points, _trilinear,
-                      masked_element_interpolate, masked_interpolate)
+                      masked_element_interpolate, masked_interpolate, spline_interpolate)
 
 log = logging.getLogger("plask_gb300.electrical")
 
@@ -491,9 +491,12 @@ class Shockley3D:
         if dst_mesh is None:
             return V
         pts = _points(dst_mesh)
-        method = _check_interpolation(interpolation)
+        method = _check_interpolation(interpolation, splines=True)
         active = self._active_elements()
-        if not np.all(active):
+        masked = not np.all(active)
+        if method in ("spline", "smooth_spline"):
+            return spline_interpolate(self._mesh.axes, V, pts, method, active if masked else None)
+        if masked:
             return masked_interpolate(self._mesh.axes, V, active, pts, method)
         if method == "nearest":
             i0, i1, i2 = (_nearest_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))

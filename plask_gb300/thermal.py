@@ -334,15 +334,164 @@ def conductivity_elements(axes, pts):
     return idx, ok
 
 
+def _along(F, d, sl):
+    """Index F (canonical: axis 0 last) with slice ``sl`` along mesh axis d."""
+    idx = [slice(None)] * F.ndim
+    idx[F.ndim - 1 - d] = sl
+    return F[tuple(idx)]
+
+
+def _axis_shape(F, d, v):
+    """v (along mesh axis d) shaped to broadcast against canonical F."""
+    shp = [1] * F.ndim
+    shp[F.ndim - 1 - d] = v.size
+    return v.reshape(shp)
+
+
+def hyman_diffs(axes, F):
+    """Node derivatives along every axis for the "spline" interpolation
+    (hyman::computeDiffs, plask/mesh/rectangular_spline.cpp:285-360; on a masked mesh
+    masked_hyman::computeDiffs, rectangular_masked_spline.cpp:436-500), without symmetry or
+    periodicity: the parabolic estimate (da sb + db sa) / (da + db) from the one-sided
+    slopes sa, sb, limited to 3 min(|sa|, |sb|) (Hyman's filter, plask/mesh/hyman.hpp:26-31);
+    0 at the first and last node and, on a masked mesh (NaN off it), next to a node off
+    the mesh."""
+    diffs = []
+    for d, a in enumerate(axes):
+        D = np.zeros_like(F)
+        n = a.size
+        if n > 2:
+            Fm, F0, Fp = _along(F, d, slice(0, n - 2)), _along(F, d, slice(1, n - 1)), _along(F, d, slice(2, n))
+            h = np.diff(a)
+            da, db = _axis_shape(F, d, h[:-1]), _axis_shape(F, d, h[1:])
+            with np.errstate(invalid="ignore"):
+                sa, sb = (F0 - Fm) / da, (Fp - F0) / db
+                v = (da * sb + db * sa) / (da + db)
+                lim = 3.0 * np.minimum(np.abs(sa), np.abs(sb))
+                v = np.where(v > lim, lim, np.where(v < -lim, -lim, v))
+            v = np.where(np.isnan(Fm) | np.isnan(Fp) | np.isnan(F0), 0.0, v)
+            idx = [slice(None)] * F.ndim
+            idx[F.ndim - 1 - d] = slice(1, n - 1)
+            D[tuple(idx)] = v
+        diffs.append(D)
+    return diffs
+
+
+def smooth_spline_diffs(axes, F):
+    """Node derivatives along every axis for the "smooth_spline" interpolation
+    (spline::computeDiffs, plask/mesh/rectangular_spline.cpp:440-600), without symmetry or
+    periodicity: the cubic spline with continuous second derivatives and zero slopes at the
+    first and last node, db s[i-1] + 2 (da + db) s[i] + da s[i+1] =
+    3 (da/db (y[i+1] - y[i]) + db/da (y[i] - y[i-1])), solved per mesh line."""
+    from scipy.linalg import solve_banded
+
+    diffs = []
+    for d, a in enumerate(axes):
+        n = a.size
+        if n < 3:
+            diffs.append(np.zeros_like(F))
+            continue
+        nd = F.ndim - 1 - d
+        Y = np.moveaxis(F, nd, 0).reshape(n, -1)
+        h = np.diff(a)
+        da, db = h[:-1], h[1:]
+        ab = np.zeros((3, n))
+        ab[1, 0] = ab[1, -1] = 1.0
+        ab[0, 2:] = da            # super-diagonal: du[i] = da of row i
+        ab[1, 1:-1] = 2.0 * (da + db)
+        ab[2, :-2] = db           # sub-diagonal: dl[i-1] = db of row i
+        rhs = np.zeros_like(Y)
+        rhs[1:-1] = 3.0 * ((da / db)[:, None] * (Y[2:] - Y[1:-1]) + (db / da)[:, None] * (Y[1:-1] - Y[:-2]))
+        S = solve_banded((1, 1), ab, rhs)
+        diffs.append(np.moveaxis(S.reshape((n,) + np.moveaxis(F, nd, 0).shape[1:]), 0, nd))
+    return diffs
+
+
+def _hermite(x, dlen):
+    """Cubic Hermite basis (values at the low and high node, slopes times the interval)."""
+    return (((2.0 * x - 3.0) * x * x + 1.0), ((-2.0 * x + 3.0) * x * x),
+            (((x - 2.0) * x + 1.0) * x * dlen), ((x - 1.0) * x * x * dlen))
+
+
+def _spline_combine(F, diffs, lo, hi, x, dlen):
+    """The spline formula of SplineRect2D/3DLazyDataImpl::at (rectangular_spline.cpp:30-237):
+    products of the value bases at the element's corners, plus along each axis the slope
+    bases times the corner derivatives weighted by the value bases of the other axes."""
+    dims = len(lo)
+    H = [_hermite(x[d], dlen[d]) for d in range(dims)]
+    val = 0.0
+    for c in itertools.product((0, 1), repeat=dims):
+        w = 1.0
+        for d in range(dims):
+            w = w * H[d][c[d]]
+        val = val + w * F[tuple((hi[d] if c[d] else lo[d]) for d in range(dims))[::-1]]
+    for d in range(dims):
+        others = [e for e in range(dims) if e != d]
+        for c in itertools.product((0, 1), repeat=dims - 1):
+            w = 1.0
+            for e, ce in zip(others, c):
+                w = w * H[e][ce]
+            at = {e: (hi[e] if ce else lo[e]) for e, ce in zip(others, c)}
+            il = tuple((lo[k] if k == d else at[k]) for k in range(dims))[::-1]
+            ih = tuple((hi[k] if k == d else at[k]) for k in range(dims))[::-1]
+            val = val + w * (H[d][2] * diffs[d][il] + H[d][3] * diffs[d][ih])
+    return val
+
+
+def spline_interpolate(axes, F, pts, method, active=None):
+    """Spline interpolation of nodal values on a rectilinear mesh ("spline": Hyman-filtered
+    parabolic slopes; "smooth_spline": the C2 spline, full meshes only).  A full mesh
+    brackets each coordinate as prepareInterpolationForAxis does (plask/mesh/axis1d.cpp:
+    99-154: outside the axis both nodes are the edge node, 1 um apart); a masked mesh
+    (``active``) uses the holding element of its element search and gives NaN where there
+    is none."""
+    dims = len(axes)
+    if active is not None and method != "spline":
+        raise BadInput(-1, f"{method} interpolation is not provided on masked meshes (the reference has the Hyman spline only)")
+    diffs = hyman_diffs(axes, F) if method == "spline" else smooth_spline_diffs(axes, F)
+    out = np.full(len(pts), np.nan)
+    if active is None:
+        sel = np.arange(len(pts))
+        lo, hi, lo_c, hi_c = [], [], [], []
+        for d, a in enumerate(axes):
+            xd = pts[:, d]
+            n = a.size
+            up = np.searchsorted(a, xd, side="right")
+            lo.append(np.where(up == 0, 0, up - 1))
+            lo_c.append(np.where(up == 0, a[0] - 1.0, a[np.maximum(up - 1, 0)]))
+            hi.append(np.where(up == n, n - 1, up))
+            hi_c.append(np.where(up == n, a[n - 1] + 1.0, a[np.minimum(up, n - 1)]))
+    else:
+        elem, found = masked_element_search(axes, active, pts)
+        sel = np.flatnonzero(found)
+        lo = [elem[d][sel] for d in range(dims)]
+        hi = [lo[d] + 1 for d in range(dims)]
+        lo_c = [axes[d][lo[d]] for d in range(dims)]
+        hi_c = [axes[d][hi[d]] for d in range(dims)]
+    dlen = [hi_c[d] - lo_c[d] for d in range(dims)]
+    x = [(pts[sel, d] - lo_c[d]) / dlen[d] for d in range(dims)]
+    out[sel] = _spline_combine(F, diffs, lo, hi, x, dlen)
+    return out
+
+
 def _element_axis(axis, x):
     """Index of the element holding x, clamped to the mesh (findUpIndex - 1)."""
     return np.clip(np.searchsorted(axis, x, side="right") - 1, 0, axis.size - 2)
 
 
-def _check_interpolation(method):
-    if method not in ("linear", "nearest", "default", None):
-        raise BadInput(-1, f"unsupported interpolation {method!r} (linear or nearest)")
-    return "linear" if method in ("default", None) else method
+_METHODS = {"default": "linear", None: "linear", "linear": "linear", "nearest": "nearest", "spline": "spline",
+            "smooth_spline": "smooth_spline", "smooth spline": "smooth_spline"}
+
+
+def _check_interpolation(method, splines=False):
+    """PLaSK's interpolation method names (plask/mesh/interpolation.cpp:18-28, lower case);
+    ``splines``: the provider also offers "spline" (Hyman-filtered) and "smooth_spline"."""
+    key = method.lower() if isinstance(method, str) else method
+    m = _METHODS.get(key)
+    if m is None or (not splines and m in ("spline", "smooth_spline")):
+        names = "linear, nearest, spline or smooth_spline" if splines else "linear or nearest"
+        raise BadInput(-1, f"unsupported interpolation {method!r} ({names})")
+    return m
 
 
 def _interp_axis(axis, x):
@@ -641,9 +790,13 @@ class Static3D:
         if dst_mesh is None:
             return T
         pts = _points(dst_mesh)
-        method = _check_interpolation(interpolation)
+        method = _check_interpolation(interpolation, splines=True)
         active = self._active_elements()
-        if not np.all(active):
+        masked = not np.all(active)
+        if method in ("spline", "smooth_spline"):
+            out = spline_interpolate(self._mesh.axes, T, pts, method, active if masked else None)
+            return np.where(np.isnan(out), 300.0, out)
+        if masked:
             # the masked mesh's interpolation; NaN (no included element) reads 300 K (SafeData)
             out = masked_interpolate(self._mesh.axes, T, active, pts, method)
             return np.where(np.isnan(out), 300.0, out)
@@ -674,11 +827,16 @@ class Static3D:
         mids = [0.5 * (a[1:] + a[:-1]) for a in self._mesh.axes]
         pts = _points(dst_mesh)
         active = self._active_elements()
+        method = _check_interpolation(interpolation, splines=True)
+        if method in ("spline", "smooth_spline"):
+            if not np.all(active):
+                raise BadInput(-1, f"{self.id}: spline interpolation of heat fluxes on a masked mesh is not provided")
+            return np.stack([spline_interpolate(mids, q[..., c], pts, method) for c in range(3)], axis=-1)
         if not np.all(active):
             # the masked element mesh's interpolation; NaN reads 0 (SafeData)
-            out = masked_element_interpolate(self._mesh.axes, q, active, pts, _check_interpolation(interpolation))
+            out = masked_element_interpolate(self._mesh.axes, q, active, pts, method)
             return np.nan_to_num(out)
-        if _check_interpolation(interpolation) == "nearest":
+        if method == "nearest":
             # the element holding the point (the reference's element-mesh lookup,
             # rectilinear3d.hpp:282-297, searches axis 0 for the second coordinate as well;
             # that slip is not reproduced)

@@ -21,7 +21,7 @@ from . import _native
 from .mesh import RectangularMesh2D, mesh_index2d, to_mesh_order2d
 from .thermal import (BadInput, BoundaryConditions, IterativeParams, MaterialTable, Provider, _check_interpolation,
                       _element_axis, _nearest_axis, conductivity_elements, load_state, masked_element_interpolate,
-                      masked_interpolate, save_state)
+                      masked_interpolate, save_state, spline_interpolate)
 
 log = logging.getLogger("plask_gb300.thermal2d")
 
@@ -331,9 +331,13 @@ class Static2D:
         if dst_mesh is None:
             return T
         pts = _points2d(dst_mesh)
-        method = _check_interpolation(interpolation)
+        method = _check_interpolation(interpolation, splines=True)
         active = self._active_elements()
-        if not np.all(active):
+        masked = not np.all(active)
+        if method in ("spline", "smooth_spline"):
+            out = spline_interpolate(self._mesh.axes, T, pts, method, active if masked else None)
+            return np.where(np.isnan(out), 300.0, out)
+        if masked:
             # the masked mesh's interpolation; NaN (no included element) reads 300 K (SafeData)
             out = masked_interpolate(self._mesh.axes, T, active, pts, method)
             return np.where(np.isnan(out), 300.0, out)
@@ -363,11 +367,16 @@ class Static2D:
         mids = [0.5 * (a[1:] + a[:-1]) for a in self._mesh.axes]
         pts = _points2d(dst_mesh)
         active = self._active_elements()
+        method = _check_interpolation(interpolation, splines=True)
+        if method in ("spline", "smooth_spline"):
+            if not np.all(active):
+                raise BadInput(-1, f"{self.id}: spline interpolation of heat fluxes on a masked mesh is not provided")
+            return np.stack([spline_interpolate(mids, q[..., c], pts, method) for c in range(2)], axis=-1)
         if not np.all(active):
             # the masked element mesh's interpolation; NaN reads 0 (SafeData)
-            out = masked_element_interpolate(self._mesh.axes, q, active, pts, _check_interpolation(interpolation))
+            out = masked_element_interpolate(self._mesh.axes, q, active, pts, method)
             return np.nan_to_num(out)
-        if _check_interpolation(interpolation) == "nearest":
+        if method == "nearest":
             i0, i1 = (_element_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
             return q[i1, i0].copy()
         return np.stack([_bilinear(mids, q[..., c], pts, fill=None) for c in range(2)], axis=-1)
