@@ -26,6 +26,9 @@ from __future__ import annotations
 
 import dataclasses
 import logging
+import pathlib
+import sys
+import time
 
 import numpy as np
 
@@ -554,7 +557,18 @@ class ThermoElectric3D:
     connected: the electrical solver reads the thermal temperatures, the thermal
     solver the Joule heat.  ``compute`` alternates ``electrical.compute(tfreq)`` and
     ``thermal.compute(1)`` until both return errors within their ``maxerr``.
-    Saving the fields to HDF5 is not provided (``save`` must stay False)."""
+    ``save`` writes the fields the reference saves to HDF5 (thermoelectric.py:259-290) to
+    an ``.npz`` file instead (no HDF5 library here), and only on request: ``compute``'s
+    ``save`` defaults to False."""
+
+    # the solvers' providers (thermoelectric.py:651-670)
+    outTemperature = property(lambda self: self.thermal.outTemperature)
+    outHeatFlux = property(lambda self: self.thermal.outHeatFlux)
+    outThermalConductivity = property(lambda self: self.thermal.outThermalConductivity)
+    outVoltage = property(lambda self: self.electrical.outVoltage)
+    outCurrentDensity = property(lambda self: self.electrical.outCurrentDensity)
+    outHeat = property(lambda self: self.electrical.outHeat)
+    outConductivity = property(lambda self: self.electrical.outConductivity)
 
     def __init__(self, name=""):
         self.name = name
@@ -588,9 +602,9 @@ class ThermoElectric3D:
             q = self.electrical._element_interp(np.nan_to_num(self.electrical.heat_densities()), pts=pts)
             self.thermal.inHeat = q.reshape(tm.element_shape)
 
-    def compute(self, save=False, invalidate=True):
-        if save:
-            raise NotImplementedError("saving the thermo-electric fields to HDF5 is not provided")
+    def compute(self, save=False, invalidate=True, group="ThermoElectric"):
+        """Run the loop (thermoelectric.py:181-219); ``save`` (True or a file name) writes the
+        fields afterwards (:meth:`save`)."""
         if invalidate:
             self.invalidate()
         self.initialize()
@@ -602,7 +616,59 @@ class ThermoElectric3D:
             self._move_heat()
             terr = self.thermal.compute(1)
             self.history.append((verr, terr))
+        if save:
+            self.save(None if save is True else save, group)
         return verr, terr
+
+    def get_temperature(self):
+        """Temperature on the thermal mesh, in its order (thermoelectric.py:292-296)."""
+        return self.thermal.outTemperature(self.thermal.mesh)
+
+    def get_voltage(self):
+        """Potential on the electrical mesh, in its order (thermoelectric.py:298-302)."""
+        return self.electrical.outVoltage(self.electrical.mesh)
+
+    def get_vertical_voltage(self, at=0):
+        """Potential along the vertical axis at horizontal position ``at`` (a number for
+        both horizontal axes, or a pair) on the electrical mesh's vertical nodes
+        (thermoelectric.py:304-322)."""
+        try:
+            at0, at1 = at
+        except TypeError:
+            at0 = at1 = at
+        z = np.asarray(self.electrical.mesh.axis2, np.float64)
+        pts = np.stack([np.full(z.size, float(at0)), np.full(z.size, float(at1)), z], axis=1)
+        return self.electrical.outVoltage(pts)
+
+    def save(self, filename=None, group="ThermoElectric"):
+        """Write the temperature on the thermal mesh, the potential on the electrical mesh and
+        the current density of the electrical elements (the fields of
+        thermoelectric.py:259-271) to the ``.npz`` file ``filename`` under the keys
+        ``<group>/Temperature``, ``<group>/Potential``, ``<group>/CurrentDensity``, each with
+        its mesh axes (``.../axis0`` ...) and iteration order (``.../ordering``); canonical
+        array shapes (axis 0 last).  Without ``filename`` the name is the script's with the
+        current time.  Returns the file name."""
+        if filename is None:
+            stem = pathlib.Path(sys.argv[0]).stem if sys.argv and sys.argv[0] else "plask"
+            filename = f"{stem or 'plask'}-{time.strftime('%Y%m%d-%H%M%S')}.npz"
+        tm, vm = self.thermal.mesh, self.electrical.mesh
+
+        def canonical(values, mesh):
+            # provider values come in the mesh's order; index_array maps canonical to mesh order
+            return np.asarray(values)[mesh.index_array().ravel()].reshape(mesh.shape)
+
+        data = {f"{group}/Temperature": canonical(self.get_temperature(), tm),
+                f"{group}/Potential": canonical(self.get_voltage(), vm),
+                f"{group}/CurrentDensity": np.asarray(self.electrical.outCurrentDensity(None))}
+        for key, mesh, mids in ((f"{group}/Temperature", tm, False), (f"{group}/Potential", vm, False),
+                                (f"{group}/CurrentDensity", vm, True)):
+            for d, a in enumerate(mesh.axes):
+                a = np.asarray(a, np.float64)
+                data[f"{key}/axis{d}"] = 0.5 * (a[1:] + a[:-1]) if mids else a
+            data[f"{key}/ordering"] = np.array(mesh.ordering)
+        np.savez(filename, **data)
+        log.info("Fields saved to file '%s' in group '%s'", filename, group)
+        return str(filename)
 
     def get_total_current(self, nact=0):
         return self.electrical.get_total_current(nact)
