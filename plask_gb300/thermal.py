@@ -84,7 +84,10 @@ class StructureGeometry:
 
 
 class BoundaryConditions:
-    """Ordered list of (place, value) pairs (BoundaryConditions, boundary_conditions.hpp)."""
+    """Ordered list of (place, value) pairs (BoundaryConditions, boundary_conditions.hpp;
+    the Python interface of python/plask/python/boundaries.hpp:53-160: indexing from the end
+    with negative numbers, assignment of a (place, value) tuple, append, prepend, insert,
+    clear, deletion, iteration)."""
 
     def __init__(self, owner, kind, nvals):
         self._owner = owner
@@ -104,8 +107,26 @@ class BoundaryConditions:
         self._items.append((place, self._norm(value)))
         self._owner._bc_changed()
 
+    def prepend(self, place, value):
+        self._items.insert(0, (place, self._norm(value)))
+        self._owner._bc_changed()
+
     def insert(self, index, place, value):
         self._items.insert(index, (place, self._norm(value)))
+        self._owner._bc_changed()
+
+    def _index(self, i):
+        j = i + len(self._items) if i < 0 else i
+        if not 0 <= j < len(self._items):
+            raise IndexError("boundary conditions index out of range")
+        return j
+
+    def __setitem__(self, i, item):
+        try:
+            place, value = item
+        except (TypeError, ValueError):
+            raise TypeError("you can only assign a tuple (boundary, value)") from None
+        self._items[self._index(i)] = (place, self._norm(value))
         self._owner._bc_changed()
 
     def clear(self):
@@ -117,7 +138,10 @@ class BoundaryConditions:
         self._owner._bc_changed()
 
     def __getitem__(self, i):
-        return self._items[i]
+        return self._items[self._index(i)]
+
+    def __repr__(self):
+        return "[" + ", ".join(f"({p!r}, {v[0] if len(v) == 1 else v})" for p, v in self._items) + "]"
 
     def __len__(self):
         return len(self._items)

@@ -52,3 +52,27 @@ def test_full_mesh_interpolation_continues_the_edge_values_outside():
     G = F[0]
     out2 = _bilinear(ax[:2], G, np.array([[-1.0, 0.5], [3.0, 5.0]]), fill=None)
     np.testing.assert_allclose(out2, _bilinear(ax[:2], G, np.array([[0.0, 0.5], [2.0, 2.0]]), fill=None))
+
+
+def test_boundary_condition_list_interface():
+    """python/plask/python/boundaries.hpp:53-160: append, prepend, insert, negative indices,
+    tuple assignment, deletion, clear."""
+    from plask_gb300 import thermal as TH
+
+    sv = TH.Static3D()
+    bc = sv.convection_boundary
+    bc.append("top", {"coeff": 10.0, "ambient": 300.0})
+    bc.prepend("bottom", (5.0, 290.0))
+    bc.insert(1, "left", {"coeff": 1.0, "ambient": 280.0})
+    assert [p for p, _ in bc] == ["bottom", "left", "top"]
+    assert bc[-1] == ("top", (10.0, 300.0))
+    bc[0] = ("front", {"coeff": 2.0, "ambient": 310.0})
+    assert bc[0] == ("front", (2.0, 310.0))
+    with pytest.raises(TypeError):
+        bc[0] = "front"
+    with pytest.raises(IndexError):
+        bc[5]
+    del bc[-1]
+    assert len(bc) == 2 and "front" in repr(bc)
+    bc.clear()
+    assert len(bc) == 0
