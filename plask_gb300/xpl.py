@@ -15,7 +15,12 @@ What the reference reads there, and what this reader applies:
   algorithm>``;
 * ``Shockley3D`` (solvers/electrical/shockley/electr3d.cpp:41-87, beta.cpp:26-62):
   ``<voltage>``, ``<loop start-cond start-cond-inplane convergence maxerr>``,
-  ``<contacts pcond ncond>``, ``<junction js beta beta<n> js<n>>``.
+  ``<contacts pcond ncond>``, ``<junction js beta beta<n> js<n>>``;
+* ``ThermoElectric3D`` (solvers/meta/shockley/thermoelectric.py:94-172): ``<geometry
+  thermal electrical>``, ``<mesh thermal electrical empty-elements>``, ``<junction pnjcond
+  beta<n> js<n>>``, ``<contacts pcond ncond>``, ``<loop tfreq inittemp maxterr maxcerr>``,
+  ``<tmatrix>`` / ``<ematrix>`` (algorithm, ``<iterative>``), the thermal conditions and
+  ``<voltage>``.
 
 A boundary condition is ``<condition place="SIDE" .../>`` (a side of the mesh:
 ``bottom``, ``top``, ``left``, ``right`` and in 3D ``back``, ``front``),
@@ -147,6 +152,49 @@ def _junction(solver, tag):
             raise ValueError(f"unexpected attribute {k!r} of <junction>")
 
 
+def _thermoelectric(te, root, places, geometries, meshes):
+    """ThermoElectric._parse_xpl (thermoelectric.py:131-172) onto the two solvers."""
+    th, el = te.thermal, te.electrical
+    for tag in root:
+        t, a = tag.tag, tag.attrib
+        if t in ("geometry", "mesh"):
+            table = geometries if t == "geometry" else meshes
+            for key, solver in (("thermal", th), ("electrical", el)):
+                if key in a:
+                    if a[key] not in table:
+                        raise ValueError(f"unknown {t} {a[key]!r}")
+                    setattr(solver, t, table[a[key]])
+            if t == "mesh" and "empty-elements" in a:
+                if a["empty-elements"] not in _EMPTY:
+                    raise ValueError(f"unknown empty-elements {a['empty-elements']!r}")
+                el.empty_elements = a["empty-elements"]
+        elif t == "junction":
+            for k, v in a.items():
+                if k == "pnjcond" or k.startswith("beta") or k.startswith("js"):
+                    setattr(el, k, float(v))
+        elif t == "contacts":
+            for k in ("pcond", "ncond"):
+                if k in a:
+                    setattr(el, k, float(a[k]))
+        elif t == "loop":
+            te.tfreq = int(a.get("tfreq", te.tfreq))
+            if "inittemp" in a:
+                th.inittemp = float(a["inittemp"])
+            if "maxterr" in a:
+                th.maxerr = float(a["maxterr"])
+            if "maxcerr" in a:
+                el.maxerr = float(a["maxcerr"])
+        elif t in ("tmatrix", "ematrix"):
+            _matrix(th if t == "tmatrix" else el, tag)
+        elif t in ("temperature", "heatflux", "convection", "radiation"):
+            _conditions(th, tag, getattr(th, f"{t}_boundary"), t, places)
+        elif t == "voltage":
+            _conditions(el, tag, el.voltage_boundary, "voltage", places)
+        else:
+            raise ValueError(f"unexpected <{t}> in the configuration of ThermoElectric3D")
+    return te
+
+
 def configure(solver, xml, places=None, geometries=None, meshes=None):
     """Apply the XPL configuration ``xml`` (the solver tag or its body, as text or an
     ElementTree element) to ``solver``.  ``places``, ``geometries`` and ``meshes`` map the
@@ -156,6 +204,8 @@ def configure(solver, xml, places=None, geometries=None, meshes=None):
     geometries = geometries or {}
     meshes = meshes or {}
     cls = type(solver).__name__
+    if hasattr(solver, "thermal") and hasattr(solver, "electrical"):
+        return _thermoelectric(solver, root, places, geometries, meshes)
     electrical = hasattr(solver, "voltage_boundary")
     dynamic = cls in ("Dynamic3D", "Dynamic2D", "DynamicCyl")
     for tag in root:

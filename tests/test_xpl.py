@@ -103,3 +103,32 @@ def test_shockley3d_configuration():
     assert sv.js == 2.0 and sv.beta == 19.0 and sv.beta1 == 17.0 and sv.js1 == 1.5
     xpl.configure(sv, '<electrical><loop start-cond="3"/></electrical>')
     assert sv.start_cond == (0.1, 3.0)
+
+
+def test_thermoelectric3d_configuration():
+    """ThermoElectric._parse_xpl (solvers/meta/shockley/thermoelectric.py:131-172)."""
+    te = EL.ThermoElectric3D()
+    tmesh, emesh = object(), object()
+    xpl.configure(te, """<thermoelectric>
+        <mesh thermal="tm" electrical="em" empty-elements="include"/>
+        <junction beta0="19" js0="1.5" pnjcond="0.3"/>
+        <contacts pcond="7" ncond="8"/>
+        <loop tfreq="4" inittemp="295" maxterr="0.1" maxcerr="0.2"/>
+        <tmatrix algorithm="iterative"><iterative maxit="500"/></tmatrix>
+        <ematrix algorithm="cholesky"/>
+        <temperature><condition place="bottom" value="300"/></temperature>
+        <convection><condition place="top" coeff="10" ambient="300"/></convection>
+        <voltage><condition place="top" value="2"/><condition place="bottom" value="0"/></voltage>
+        </thermoelectric>""", meshes={"tm": tmesh, "em": emesh})
+    assert te.thermal.mesh is tmesh and te.electrical.mesh is emesh
+    assert te.electrical.empty_elements == "include"
+    assert (te.electrical.beta0, te.electrical.js0) == (19.0, 1.5)
+    assert tuple(te.electrical.start_cond) == (0.0, 0.3)  # pnjcond sets the junction's start conductivity
+    assert (te.electrical.pcond, te.electrical.ncond) == (7.0, 8.0)
+    assert (te.tfreq, te.thermal.inittemp, te.thermal.maxerr, te.electrical.maxerr) == (4, 295.0, 0.1, 0.2)
+    assert te.thermal.algorithm == "iterative" and te.thermal.iterative.maxit == 500
+    assert te.electrical.algorithm == "cholesky"
+    assert len(te.thermal.temperature_boundary) == 1 and len(te.thermal.convection_boundary) == 1
+    assert [v for _, v in te.electrical.voltage_boundary] == [(2.0,), (0.0,)]
+    with pytest.raises(ValueError):
+        xpl.configure(EL.ThermoElectric3D(), "<thermoelectric><optical/></thermoelectric>")
