@@ -123,3 +123,32 @@ def test_element_values_with_components():
     Q = np.stack([_element_field(ax, (0.0, 1.0, 0.0)), _element_field(ax, (0.0, 0.0, 1.0))], axis=-1)
     out = masked_element_interpolate(ax, Q, active, np.array([[0.9, 0.7], [1.5, 1.5]]), "linear")
     assert np.allclose(out[0], [0.9, 0.7]) and np.all(np.isnan(out[1]))
+
+
+def test_electrical_voltage_provider_on_the_masked_diode():
+    """Shockley3D.outVoltage on the reference diode's masked mesh (air left out), with the
+    potential read from a stand-in for the device handle: NaN in the air, the trilinear
+    value of the holding element in the conductors (electr3d.cpp:507-515)."""
+    from plask_gb300 import electrical as EL
+    from plask_gb300 import structures as S
+
+    s = S.shockley_diode()
+    sv = EL.solver_for_structure(s, ordering="012", algorithm="gpu-mixed")
+
+    class _Handle:
+        @staticmethod
+        def potential(nn):
+            return np.linspace(0.0, 1.0, nn)
+
+    sv._elec = _Handle()
+    V = sv._full_potential()
+    x, y, z = s.axes
+    air = np.array([[480.0, 480.0, 0.5]])          # in the bottom contact layer, beside the contact: air
+    metal = np.array([[0.0, 0.0, 450.0]])           # inside the upper conductor block
+    assert np.isnan(sv.outVoltage(air)[0])
+    got = sv.outVoltage(metal)[0]
+    i = [np.searchsorted(a, p, side="right") - 1 for a, p in zip(s.axes, metal[0])]
+    w = [(metal[0][d] - s.axes[d][i[d]]) / (s.axes[d][i[d] + 1] - s.axes[d][i[d]]) for d in range(3)]
+    want = sum((w[0] if a else 1 - w[0]) * (w[1] if b else 1 - w[1]) * (w[2] if c else 1 - w[2])
+               * V[i[2] + c, i[1] + b, i[0] + a] for a in (0, 1) for b in (0, 1) for c in (0, 1))
+    assert np.isfinite(got) and np.isclose(got, want, rtol=0, atol=1e-12)
