@@ -152,3 +152,44 @@ def test_electrical_voltage_provider_on_the_masked_diode():
     want = sum((w[0] if a else 1 - w[0]) * (w[1] if b else 1 - w[1]) * (w[2] if c else 1 - w[2])
                * V[i[2] + c, i[1] + b, i[0] + a] for a in (0, 1) for b in (0, 1) for c in (0, 1))
     assert np.isfinite(got) and np.isclose(got, want, rtol=0, atol=1e-12)
+
+
+def test_thermal_temperature_provider_on_a_masked_mesa():
+    """Static3D.outTemperature on an etched mesa (a masked mesh), the temperatures read from a
+    stand-in for the device handle: 300 K where no included element holds the point
+    (SafeData, therm3d.cpp:387-395), the holding element's trilinear value elsewhere; the
+    spline method through the same path."""
+    from plask_gb300 import structures as S
+    from plask_gb300 import thermal as TH
+
+    s = S.layered_c0(seed=2, n=(8, 8, 12), power=1e15)
+    n_mat = s.k300.size
+    s.k300, s.p = np.append(s.k300, 0.026), np.append(s.p, 0.0)
+    s.kz_ratio, s.hexp, s.empty = np.append(s.kz_ratio, 1.0), np.append(s.hexp, 0.0), np.append(s.empty, True)
+    xm = 0.5 * (s.axes[0][1:] + s.axes[0][:-1])
+    mat = s.mat.copy()
+    mat[-3:, :, xm > 10.0] = n_mat  # the top three element layers etched away beyond x = 10 um
+    s.mat = mat
+    sv = TH.solver_for_structure(s, ordering="201", algorithm="gpu-mixed")
+    nn = int(sv._active_mask_mesh_order().sum())
+
+    class _Handle:
+        @staticmethod
+        def temperature():
+            return np.linspace(300.0, 400.0, nn)
+
+        @staticmethod
+        def sizes():
+            return nn, 0
+
+    sv._fem = _Handle()
+    T = sv._full_temperature()
+    z = s.axes[2]
+    etched = np.array([[40.0, 5.0, 0.5 * (z[-1] + z[-2])]])
+    inside = np.array([[2.0, 3.0, 0.5 * (z[-1] + z[-2])]])
+    assert sv.outTemperature(etched)[0] == 300.0
+    assert sv.outTemperature(etched, "spline")[0] == 300.0
+    got = sv.outTemperature(inside)[0]
+    assert np.isfinite(got) and T[np.isfinite(T)].min() <= got <= T[np.isfinite(T)].max()
+    # outside the mesh box a masked mesh has no element: 300 K
+    assert sv.outTemperature(np.array([[-5.0, 3.0, 1.0]]))[0] == 300.0
