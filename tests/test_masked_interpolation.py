@@ -193,3 +193,77 @@ def test_thermal_temperature_provider_on_a_masked_mesa():
     assert np.isfinite(got) and T[np.isfinite(T)].min() <= got <= T[np.isfinite(T)].max()
     # outside the mesh box a masked mesh has no element: 300 K
     assert sv.outTemperature(np.array([[-5.0, 3.0, 1.0]]))[0] == 300.0
+
+
+def _search_by_loops(axes, active, p):
+    """The nested loops of RectangularMaskedMesh3D::prepareInterpolation
+    (rectangular_masked3d.cpp:68-112), one point at a time."""
+    MIN = MASKED_MIN_DISTANCE
+    if not all(a[0] - x < MIN and x - a[-1] < MIN for a, x in zip(axes, p)):
+        return None
+    lo, hi = [], []
+    for a, x in zip(axes, p):
+        h = int(np.searchsorted(a, x, side="right"))
+        h = a.size - 1 if h == a.size else (1 if h == 0 else h)
+        lo.append(h - 1)
+        hi.append(h)
+    lo_c = [a[i] for a, i in zip(axes, lo)]
+    hi_c = [a[i] for a, i in zip(axes, hi)]
+    i0, i1, i2 = lo
+    for _ in range(2):
+        for _ in range(2):
+            for _ in range(2):
+                if active[i2, i1, i0]:
+                    return (i0, i1, i2)
+                if i0 > 0 and lo_c[0] <= p[0] < lo_c[0] + MIN:
+                    i0 = hi[0] - 2
+                elif i0 < axes[0].size - 2 and hi_c[0] - MIN < p[0] <= hi_c[0]:
+                    i0 = hi[0]
+                else:
+                    break
+            i0 = hi[0] - 1
+            if i1 > 0 and lo_c[1] <= p[1] < lo_c[1] + MIN:
+                i1 = hi[1] - 2
+            elif i1 < axes[1].size - 2 and hi_c[1] - MIN < p[1] <= hi_c[1]:
+                i1 = hi[1]
+            else:
+                break
+        i1 = hi[1] - 1
+        if i2 > 0 and lo_c[2] <= p[2] < lo_c[2] + MIN:
+            i2 = hi[2] - 2
+        elif i2 < axes[2].size - 2 and hi_c[2] - MIN < p[2] <= hi_c[1]:
+            i2 = hi[2]
+        else:
+            break
+    return None
+
+
+def test_vectorised_search_matches_the_reference_loops():
+    rng = np.random.default_rng(11)
+    axes = (np.array([0.0, 1.0, 2.0, 3.5]), np.array([0.0, 0.8, 3.0, 3.2]), np.array([0.0, 2.0, 2.5, 4.0]))
+    for trial in range(20):
+        active = rng.random((3, 3, 3)) < 0.5
+        # points on and within the tolerance of node lines, inside elements and just outside the box
+        pts = []
+        for _ in range(150):
+            p = []
+            for a in axes:
+                kind = rng.integers(4)
+                node = a[rng.integers(a.size)]
+                if kind == 0:
+                    p.append(node)
+                elif kind == 1:
+                    p.append(node + rng.choice([-0.5, 0.5]) * MASKED_MIN_DISTANCE)
+                elif kind == 2:
+                    p.append(rng.uniform(a[0], a[-1]))
+                else:
+                    p.append(node + rng.choice([-3.0, 3.0]) * MASKED_MIN_DISTANCE)
+            pts.append(p)
+        pts = np.array(pts)
+        elem, found = masked_element_search(axes, active, pts)
+        for k, p in enumerate(pts):
+            want = _search_by_loops(axes, active, p)
+            if want is None:
+                assert not found[k], (trial, p)
+            else:
+                assert found[k] and (elem[0][k], elem[1][k], elem[2][k]) == want, (trial, p, want)
