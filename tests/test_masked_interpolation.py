@@ -267,3 +267,61 @@ def test_vectorised_search_matches_the_reference_loops():
                 assert not found[k], (trial, p)
             else:
                 assert found[k] and (elem[0][k], elem[1][k], elem[2][k]) == want, (trial, p, want)
+
+
+def _element_linear_by_loops(axes, Q, active, p):
+    """RectangularMaskedMesh3D::ElementMesh::interpolateLinear (rectangular_masked3d.hpp:277-333)."""
+    hit = _search_by_loops(axes, active, p)
+    if hit is None:
+        return np.nan
+    i0, i1, i2 = hit
+    mids = [0.5 * (a[1:] + a[:-1]) for a in axes]
+    pa = [mids[0][i0], mids[1][i1], mids[2][i2]]
+
+    def step(d, i):
+        if p[d] < pa[d]:
+            return 0 if i == 0 else -1
+        return 0 if i + 1 == mids[d].size else 1
+
+    s0, s1, s2 = step(0, i0), step(1, i1), step(2, i2)
+
+    def val(a, b, c):
+        return Q[c, b, a] if active[c, b, a] else None
+
+    aaa = Q[i2, i1, i0]
+    if s0 == 0 and s1 == 0 and s2 == 0:
+        return aaa
+    aab = val(i0, i1, i2 + s2)
+    aba = val(i0, i1 + s1, i2)
+    baa = val(i0 + s0, i1, i2)
+    aab = aaa if aab is None else aab
+    aba = aaa if aba is None else aba
+    baa = aaa if baa is None else baa
+    abb = val(i0, i1 + s1, i2 + s2)
+    bab = val(i0 + s0, i1, i2 + s2)
+    bba = val(i0 + s0, i1 + s1, i2)
+    bbb = val(i0 + s0, i1 + s1, i2 + s2)
+    abb = aab + aba - aaa if abb is None else abb
+    bab = baa + aab - aaa if bab is None else bab
+    bba = aba + baa - aaa if bba is None else bba
+    bbb = aab + aba + baa - 2 * aaa if bbb is None else bbb
+    pb = [mids[0][i0 + s0] + (s0 == 0), mids[1][i1 + s1] + (s1 == 0), mids[2][i2 + s2] + (s2 == 0)]
+    t = [(p[d] - pa[d]) / (pb[d] - pa[d]) for d in range(3)]
+    corners = {(0, 0, 0): aaa, (1, 0, 0): baa, (0, 1, 0): aba, (0, 0, 1): aab,
+               (1, 1, 0): bba, (1, 0, 1): bab, (0, 1, 1): abb, (1, 1, 1): bbb}
+    return sum(v * (t[0] if c[0] else 1 - t[0]) * (t[1] if c[1] else 1 - t[1]) * (t[2] if c[2] else 1 - t[2])
+               for c, v in corners.items())
+
+
+def test_vectorised_element_interpolation_matches_the_reference_loops():
+    rng = np.random.default_rng(12)
+    axes = (np.array([0.0, 1.0, 2.0, 3.5, 4.0]), np.array([0.0, 0.8, 3.0, 3.2]), np.array([0.0, 2.0, 2.5, 4.0]))
+    for trial in range(10):
+        active = rng.random((3, 3, 4)) < 0.6
+        Q = rng.normal(size=(3, 3, 4))
+        pts = np.stack([rng.uniform(a[0], a[-1], 300) for a in axes], axis=1)
+        out = masked_element_interpolate(axes, Q, active, pts, "linear")
+        want = np.array([_element_linear_by_loops(axes, Q, active, p) for p in pts])
+        assert np.array_equal(np.isnan(out), np.isnan(want))
+        ok = ~np.isnan(want)
+        np.testing.assert_allclose(out[ok], want[ok], rtol=0, atol=1e-12)
