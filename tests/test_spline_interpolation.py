@@ -85,3 +85,53 @@ def test_masked_spline():
     assert np.isnan(out[0]) and np.isfinite(out[1:]).all()
     with pytest.raises(BadInput):
         spline_interpolate(ax, F, np.array([[1.5, 0.5]]), "smooth_spline", active)
+
+
+def test_spline_formula_matches_a_transcription_of_the_reference():
+    """SplineRect3DLazyDataImpl::at (rectangular_spline.cpp:102-237, no symmetry) written out
+    term by term for random data, against the vectorised evaluation."""
+    from plask_gb300.thermal import _hermite
+
+    rng = np.random.default_rng(4)
+    F = rng.normal(size=(AX[2].size, AX[1].size, AX[0].size))
+    D0, D1, D2 = hyman_diffs(AX, F)
+    pts = np.stack([rng.uniform(a[0] - 0.5, a[-1] + 0.5, 60) for a in AX], axis=1)
+    got = spline_interpolate(AX, F, pts, "spline")
+    for k, p in enumerate(pts):
+        idx, bounds = [], []
+        for a, x in zip(AX, p):
+            up = int(np.searchsorted(a, x, side="right"))
+            lo = 0 if up == 0 else up - 1
+            lo_c = a[0] - 1.0 if up == 0 else a[up - 1]
+            hi = a.size - 1 if up == a.size else up
+            hi_c = a[-1] + 1.0 if up == a.size else a[up]
+            idx.append((lo, hi))
+            bounds.append((lo_c, hi_c))
+        (l0, h0), (l1, h1), (l2, h2) = idx
+        d = [b[1] - b[0] for b in bounds]
+        x = [(p[i] - bounds[i][0]) / d[i] for i in range(3)]
+        (h0l, h0h, g0l, g0h), (h1l, h1h, g1l, g1h), (h2l, h2h, g2l, g2h) = (_hermite(x[i], d[i]) for i in range(3))
+
+        def f(a, b, c, A=F):
+            return A[c, b, a]
+
+        D_ll = g0l * f(l0, l1, l2, D0) + g0h * f(h0, l1, l2, D0)
+        Dl_l = g1l * f(l0, l1, l2, D1) + g1h * f(l0, h1, l2, D1)
+        Dll_ = g2l * f(l0, l1, l2, D2) + g2h * f(l0, l1, h2, D2)
+        D_lh = g0l * f(l0, l1, h2, D0) + g0h * f(h0, l1, h2, D0)
+        Dl_h = g1l * f(l0, l1, h2, D1) + g1h * f(l0, h1, h2, D1)
+        Dlh_ = g2l * f(l0, h1, l2, D2) + g2h * f(l0, h1, h2, D2)
+        D_hl = g0l * f(l0, h1, l2, D0) + g0h * f(h0, h1, l2, D0)
+        Dh_l = g1l * f(h0, l1, l2, D1) + g1h * f(h0, h1, l2, D1)
+        Dhl_ = g2l * f(h0, l1, l2, D2) + g2h * f(h0, l1, h2, D2)
+        D_hh = g0l * f(l0, h1, h2, D0) + g0h * f(h0, h1, h2, D0)
+        Dh_h = g1l * f(h0, l1, h2, D1) + g1h * f(h0, h1, h2, D1)
+        Dhh_ = g2l * f(h0, h1, l2, D2) + g2h * f(h0, h1, h2, D2)
+        want = (h0l * h1l * h2l * f(l0, l1, l2) + h0l * h1l * h2h * f(l0, l1, h2) + h0l * h1h * h2l * f(l0, h1, l2)
+                + h0l * h1h * h2h * f(l0, h1, h2) + h0h * h1l * h2l * f(h0, l1, l2) + h0h * h1l * h2h * f(h0, l1, h2)
+                + h0h * h1h * h2l * f(h0, h1, l2) + h0h * h1h * h2h * f(h0, h1, h2)
+                + h1l * h2l * D_ll + h0l * h2l * Dl_l + h0l * h1l * Dll_
+                + h1l * h2h * D_lh + h0l * h2h * Dl_h + h0l * h1h * Dlh_
+                + h1h * h2l * D_hl + h0h * h2l * Dh_l + h0h * h1l * Dhl_
+                + h1h * h2h * D_hh + h0h * h2h * Dh_h + h0h * h1h * Dhh_)
+        assert abs(got[k] - want) <= 1e-12 * max(1.0, abs(want)), (k, got[k], want)
