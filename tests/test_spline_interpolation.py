@@ -135,3 +135,27 @@ def test_spline_formula_matches_a_transcription_of_the_reference():
                 + h1h * h2l * D_hl + h0h * h2l * Dh_l + h0h * h1l * Dhl_
                 + h1h * h2h * D_hh + h0h * h2h * Dh_h + h0h * h1h * Dhh_)
         assert abs(got[k] - want) <= 1e-12 * max(1.0, abs(want)), (k, got[k], want)
+
+
+def test_masked_hyman_slopes_match_a_transcription_of_the_reference():
+    """masked_hyman::computeDiffs (rectangular_masked_spline.cpp:436-500, no symmetry): 0 at
+    the ends and next to a node off the mesh, else the limited parabolic estimate."""
+    rng = np.random.default_rng(8)
+    a = np.cumsum(rng.uniform(0.2, 1.5, 9))
+    for _ in range(30):
+        y = rng.normal(size=a.size)
+        y[rng.random(a.size) < 0.25] = np.nan
+        want = np.zeros(a.size)
+        for i in range(1, a.size - 1):
+            if np.isnan(y[i]):
+                continue
+            if np.isnan(y[i - 1]) or np.isnan(y[i + 1]):
+                continue
+            da, db = a[i] - a[i - 1], a[i + 1] - a[i]
+            sa, sb = (y[i] - y[i - 1]) / da, (y[i + 1] - y[i]) / db
+            v = (da * sb + db * sa) / (da + db)
+            lim = 3 * min(abs(sa), abs(sb))
+            want[i] = lim if v > lim else (-lim if v < -lim else v)
+        got = hyman_diffs((a,), y)[0]
+        ok = ~np.isnan(y)
+        np.testing.assert_allclose(got[ok], want[ok], rtol=0, atol=1e-14)
