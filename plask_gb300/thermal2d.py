@@ -320,6 +320,20 @@ class Static2D:
         vals[np.flatnonzero(self._active_mask_mesh_order())] = t
         return vals[idx].reshape(self._mesh.shape)
 
+    def _wrap(self, pts):
+        """Points as the providers see them (InterpolationFlags::wrap,
+        plask/mesh/interpolation.hpp:232-250): the cylindrical geometry is symmetric in r
+        (plask/geometry/space.hpp:1068-1072), so r < 0 reads at |r|.  Returns the wrapped
+        points and the mask of mirrored ones (their radial vector components change sign,
+        InterpolationFlags::postprocess, interpolation.hpp:272-287)."""
+        if self._geometry_kind != "cylindrical":
+            return pts, np.zeros(len(pts), bool)
+        mirrored = pts[:, 0] < 0.0
+        w = pts.copy()
+        w[:, 0] = np.abs(w[:, 0])
+        w[w[:, 0] == 0.0, 0] = 1e-12
+        return w, mirrored
+
     def _get_temperatures(self, dst_mesh, interpolation="linear"):
         """Temperatures on a destination mesh or points (therm2d.cpp:544-553): bilinear or the
         nearest node, the edge values continuing outside the mesh; on a masked mesh its
@@ -330,7 +344,7 @@ class Static2D:
         T = self._full_temperature()
         if dst_mesh is None:
             return T
-        pts = _points2d(dst_mesh)
+        pts, _ = self._wrap(_points2d(dst_mesh))
         method = _check_interpolation(interpolation, splines=True)
         active = self._active_elements()
         masked = not np.all(active)
@@ -365,21 +379,23 @@ class Static2D:
         if dst_mesh is None:
             return q
         mids = [0.5 * (a[1:] + a[:-1]) for a in self._mesh.axes]
-        pts = _points2d(dst_mesh)
+        pts, mirrored = self._wrap(_points2d(dst_mesh))
         active = self._active_elements()
         method = _check_interpolation(interpolation, splines=True)
         if method in ("spline", "smooth_spline"):
             if not np.all(active):
                 raise BadInput(-1, f"{self.id}: spline interpolation of heat fluxes on a masked mesh is not provided")
-            return np.stack([spline_interpolate(mids, q[..., c], pts, method) for c in range(2)], axis=-1)
-        if not np.all(active):
+            out = np.stack([spline_interpolate(mids, q[..., c], pts, method) for c in range(2)], axis=-1)
+        elif not np.all(active):
             # the masked element mesh's interpolation; NaN reads 0 (SafeData)
-            out = masked_element_interpolate(self._mesh.axes, q, active, pts, method)
-            return np.nan_to_num(out)
-        if method == "nearest":
+            out = np.nan_to_num(masked_element_interpolate(self._mesh.axes, q, active, pts, method))
+        elif method == "nearest":
             i0, i1 = (_element_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
-            return q[i1, i0].copy()
-        return np.stack([_bilinear(mids, q[..., c], pts, fill=None) for c in range(2)], axis=-1)
+            out = q[i1, i0].copy()
+        else:
+            out = np.stack([_bilinear(mids, q[..., c], pts, fill=None) for c in range(2)], axis=-1)
+        out[mirrored, 0] *= -1.0  # the radial component of a mirrored point (Symmetry::NP)
+        return out
 
     def _get_conductivity(self, dst_mesh, interpolation="linear"):
         """(k_0, k_1) of the element holding each point (therm2d.cpp:574-597), NaN outside."""
@@ -389,7 +405,7 @@ class Static2D:
         k = k[eidx].reshape(self._mesh.element_shape + (2,))
         if dst_mesh is None:
             return k
-        idx, ok = conductivity_elements(self._mesh.axes, _points2d(dst_mesh))
+        idx, ok = conductivity_elements(self._mesh.axes, self._wrap(_points2d(dst_mesh))[0])
         out = k[idx[1], idx[0]].copy()
         out[~ok] = np.nan
         return out

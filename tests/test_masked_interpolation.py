@@ -325,3 +325,34 @@ def test_vectorised_element_interpolation_matches_the_reference_loops():
         assert np.array_equal(np.isnan(out), np.isnan(want))
         ok = ~np.isnan(want)
         np.testing.assert_allclose(out[ok], want[ok], rtol=0, atol=1e-12)
+
+
+def test_cylindrical_providers_mirror_negative_radii():
+    """The cylindrical geometry is symmetric in r (plask/geometry/space.hpp:1068-1072): a
+    StaticCyl provider reads r < 0 at |r| (InterpolationFlags::wrap)."""
+    from plask_gb300 import structures as S
+    from plask_gb300 import thermal2d as T2
+
+    s = S.layered_2d(seed=5, n=(12, 14))
+    sv = T2.solver_for_structure2d(s, cls=T2.StaticCyl, ordering="10")
+    n = len(sv.mesh)
+
+    class _Handle:
+        @staticmethod
+        def temperature():
+            return 300.0 + np.arange(n, dtype=float) % 17
+
+        @staticmethod
+        def sizes():
+            return n, 0
+
+    sv._fem = _Handle()
+    z = 0.5 * (s.axes[1][3] + s.axes[1][4])
+    pts = np.array([[7.3, z], [-7.3, z], [0.0, z]])
+    for m in ("linear", "nearest", "spline"):
+        out = sv.outTemperature(pts, m)
+        assert out[0] == out[1]
+    w, mirrored = sv._wrap(pts)
+    assert mirrored.tolist() == [False, True, False] and w[1, 0] == 7.3 and w[2, 0] == 1e-12
+    flat = T2.solver_for_structure2d(s, cls=T2.Static2D, ordering="10")
+    assert not flat._wrap(pts)[1].any()
