@@ -486,6 +486,23 @@ class Shockley3D:
         self._load_conductivity()
         return self._element_field(self._elec.conductivity(), 2)
 
+    def _wrap(self, pts):
+        """Points as the providers see them (InterpolationFlags::wrap,
+        plask/mesh/interpolation.hpp:232-250): along an axis mirrored at 0 (the structure's
+        ``symmetric`` flags) a negative coordinate reads at its absolute value.  Returns the
+        wrapped points and, per mirrored axis, the mask of reflected points."""
+        sym = tuple(getattr(self._geometry, "symmetric", ())) if self._geometry is not None else ()
+        flips = {}
+        if not any(sym):
+            return pts, flips
+        w = pts.copy()
+        for d, on in enumerate(sym):
+            if on:
+                flips[d] = w[:, d] < 0.0
+                w[:, d] = np.abs(w[:, d])
+                w[w[:, d] == 0.0, d] = 1e-12
+        return w, flips
+
     def _get_voltage(self, dst_mesh, interpolation="linear"):
         """Potential on a destination mesh (electr3d.cpp:507-515): trilinear or the nearest
         node, the edge values continuing outside the mesh; on a masked mesh its element
@@ -493,7 +510,7 @@ class Shockley3D:
         V = self._full_potential()
         if dst_mesh is None:
             return V
-        pts = _points(dst_mesh)
+        pts, _ = self._wrap(_points(dst_mesh))
         method = _check_interpolation(interpolation, splines=True)
         active = self._active_elements()
         masked = not np.all(active)
@@ -511,7 +528,14 @@ class Shockley3D:
         midpoints, or the holding element; on a masked mesh the masked element mesh's
         interpolation with NaN read as 0."""
         mids = [0.5 * (a[1:] + a[:-1]) for a in self._mesh.axes]
-        pts = _points(dst_mesh) if pts is None else pts
+        pts, flips = self._wrap(_points(dst_mesh) if pts is None else pts)
+        out = self._element_values(q, mids, pts, interpolation)
+        if q.ndim == 4:
+            for d, m in flips.items():  # the normal component of a mirrored point (Symmetry NPP / PNP)
+                out[m, d] *= -1.0
+        return out
+
+    def _element_values(self, q, mids, pts, interpolation):
         method = _check_interpolation(interpolation)
         active = self._active_elements()
         if not np.all(active):
@@ -547,7 +571,8 @@ class Shockley3D:
         c = self.conductivities()
         if dst_mesh is None:
             return c
-        return masked_element_interpolate(self._mesh.axes, c, self._active_elements(), _points(dst_mesh), "nearest")
+        return masked_element_interpolate(self._mesh.axes, c, self._active_elements(), self._wrap(_points(dst_mesh))[0],
+                                          "nearest")
 
 
 class ThermoElectric3D:

@@ -356,3 +356,29 @@ def test_cylindrical_providers_mirror_negative_radii():
     assert mirrored.tolist() == [False, True, False] and w[1, 0] == 7.3 and w[2, 0] == 1e-12
     flat = T2.solver_for_structure2d(s, cls=T2.Static2D, ordering="10")
     assert not flat._wrap(pts)[1].any()
+
+
+def test_electrical_providers_mirror_the_symmetric_axes():
+    """The quarter-device structure (symmetric in axes 0 and 1): the voltage at (-x, -y) is
+    the one at (x, y) and the current density's x and y components change sign."""
+    from plask_gb300 import electrical as EL
+    from plask_gb300 import structures as S
+
+    s = S.shockley_c4(seed=4001, n=(9, 8, 10), voltage=1.9)
+    sv = EL.solver_for_structure(s, ordering="012", algorithm="gpu-mixed")
+    n = len(sv.mesh)
+
+    class _Handle:
+        @staticmethod
+        def potential(nn):
+            return np.linspace(0.0, 1.9, nn)
+
+    sv._elec = _Handle()
+    z = 0.5 * (s.axes[2][2] + s.axes[2][3])
+    pts = np.array([[3.0, 2.0, z], [-3.0, -2.0, z], [3.0, -2.0, z]])
+    v = sv.outVoltage(pts)
+    assert v[0] == v[1] == v[2]
+    j = np.zeros(sv.mesh.element_shape + (3,))
+    j[..., 0], j[..., 1], j[..., 2] = 1.0, 2.0, 3.0
+    out = sv._element_interp(j, pts=pts)
+    np.testing.assert_allclose(out, [[1.0, 2.0, 3.0], [-1.0, -2.0, 3.0], [1.0, -2.0, 3.0]])
