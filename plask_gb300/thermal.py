@@ -57,13 +57,19 @@ class MaterialTable:
 
 
 class StructureGeometry:
-    """Geometry given directly as element material ids on a fixed mesh (or a callable of midpoints)."""
+    """Geometry given directly as element material ids on a fixed mesh (or a callable of midpoints).
 
-    def __init__(self, materials: MaterialTable, mat=None, material_at=None, leaf_height=None):
+    ``symmetric``: per axis, whether the geometry is mirrored at 0 (a ``mirror`` edge in
+    PLaSK, plask/geometry/space.hpp:147-150); the providers then read negative coordinates
+    at their absolute values."""
+
+    def __init__(self, materials: MaterialTable, mat=None, material_at=None, leaf_height=None,
+                 symmetric=(False, False, False)):
         self.materials = materials
         self._mat = None if mat is None else np.asarray(mat, np.int32)
         self._at = material_at
         self._leaf = leaf_height
+        self.symmetric = tuple(bool(v) for v in symmetric)
 
     def material_ids(self, mesh: RectangularMesh3D):
         if self._mat is not None:
@@ -803,6 +809,23 @@ class Static3D:
                     used[ck:n2 - 1 + ck, cj:n1 - 1 + cj, ci:n0 - 1 + ci] |= act_el
         return to_mesh_order(used, mesh.ordering)
 
+    def _wrap(self, pts):
+        """Points as the providers see them (InterpolationFlags::wrap,
+        plask/mesh/interpolation.hpp:232-250): along an axis the geometry mirrors at 0 a
+        negative coordinate reads at its absolute value.  Returns the wrapped points and, per
+        mirrored axis, the mask of reflected points."""
+        sym = tuple(getattr(self._geometry, "symmetric", ())) if self._geometry is not None else ()
+        flips = {}
+        if not any(sym):
+            return pts, flips
+        w = pts.copy()
+        for d, on in enumerate(sym):
+            if on:
+                flips[d] = w[:, d] < 0.0
+                w[:, d] = np.abs(w[:, d])
+                w[w[:, d] == 0.0, d] = 1e-12
+        return w, flips
+
     def _get_temperatures(self, dst_mesh, interpolation="linear"):
         """Temperatures on a destination mesh (therm3d.cpp:387-395): trilinear or the nearest
         node, the edge values continuing outside the mesh; on a masked mesh its element
@@ -813,7 +836,7 @@ class Static3D:
         T = self._full_temperature()
         if dst_mesh is None:
             return T
-        pts = _points(dst_mesh)
+        pts, _ = self._wrap(_points(dst_mesh))
         method = _check_interpolation(interpolation, splines=True)
         active = self._active_elements()
         masked = not np.all(active)
@@ -849,24 +872,27 @@ class Static3D:
         if dst_mesh is None:
             return q
         mids = [0.5 * (a[1:] + a[:-1]) for a in self._mesh.axes]
-        pts = _points(dst_mesh)
+        pts, flips = self._wrap(_points(dst_mesh))
         active = self._active_elements()
         method = _check_interpolation(interpolation, splines=True)
         if method in ("spline", "smooth_spline"):
             if not np.all(active):
                 raise BadInput(-1, f"{self.id}: spline interpolation of heat fluxes on a masked mesh is not provided")
-            return np.stack([spline_interpolate(mids, q[..., c], pts, method) for c in range(3)], axis=-1)
-        if not np.all(active):
+            out = np.stack([spline_interpolate(mids, q[..., c], pts, method) for c in range(3)], axis=-1)
+        elif not np.all(active):
             # the masked element mesh's interpolation; NaN reads 0 (SafeData)
-            out = masked_element_interpolate(self._mesh.axes, q, active, pts, method)
-            return np.nan_to_num(out)
-        if method == "nearest":
+            out = np.nan_to_num(masked_element_interpolate(self._mesh.axes, q, active, pts, method))
+        elif method == "nearest":
             # the element holding the point (the reference's element-mesh lookup,
             # rectilinear3d.hpp:282-297, searches axis 0 for the second coordinate as well;
             # that slip is not reproduced)
             i0, i1, i2 = (_element_axis(a, pts[:, d]) for d, a in enumerate(self._mesh.axes))
-            return q[i2, i1, i0].copy()
-        return np.stack([_trilinear(mids, q[..., c], pts, fill=None) for c in range(3)], axis=-1)
+            out = q[i2, i1, i0].copy()
+        else:
+            out = np.stack([_trilinear(mids, q[..., c], pts, fill=None) for c in range(3)], axis=-1)
+        for d, m in flips.items():  # the normal component of a mirrored point (Symmetry NPP / PNP / PPN)
+            out[m, d] *= -1.0
+        return out
 
     def _get_conductivity(self, dst_mesh, interpolation="linear"):
         """(k_xy, k_z) of the element holding each point (therm3d.cpp:421-435)."""
@@ -876,7 +902,7 @@ class Static3D:
         k = k[eidx].reshape(self._mesh.element_shape + (2,))
         if dst_mesh is None:
             return k
-        idx, ok = conductivity_elements(self._mesh.axes, _points(dst_mesh))
+        idx, ok = conductivity_elements(self._mesh.axes, self._wrap(_points(dst_mesh))[0])
         out = k[idx[2], idx[1], idx[0]]
         out[~ok] = np.nan
         return out

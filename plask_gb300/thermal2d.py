@@ -27,13 +27,18 @@ log = logging.getLogger("plask_gb300.thermal2d")
 
 
 class StructureGeometry2D:
-    """Geometry given as element material ids on a fixed mesh, or a callable of midpoints (x, y)."""
+    """Geometry given as element material ids on a fixed mesh, or a callable of midpoints (x, y).
 
-    def __init__(self, materials: MaterialTable, mat=None, material_at=None, leaf_height=None):
+    ``symmetric``: per axis, whether the geometry is mirrored at 0 (a ``mirror`` edge,
+    plask/geometry/space.hpp:147-150); the cylindrical solvers mirror r in any case."""
+
+    def __init__(self, materials: MaterialTable, mat=None, material_at=None, leaf_height=None,
+                 symmetric=(False, False)):
         self.materials = materials
         self._mat = None if mat is None else np.asarray(mat, np.int32)
         self._at = material_at
         self._leaf = leaf_height
+        self.symmetric = tuple(bool(v) for v in symmetric)
 
     def material_ids(self, mesh: RectangularMesh2D):
         if self._mat is not None:
@@ -322,17 +327,25 @@ class Static2D:
 
     def _wrap(self, pts):
         """Points as the providers see them (InterpolationFlags::wrap,
-        plask/mesh/interpolation.hpp:232-250): the cylindrical geometry is symmetric in r
-        (plask/geometry/space.hpp:1068-1072), so r < 0 reads at |r|.  Returns the wrapped
-        points and the mask of mirrored ones (their radial vector components change sign,
+        plask/mesh/interpolation.hpp:232-250): along an axis the geometry mirrors at 0 -- r in
+        the cylindrical geometry always (plask/geometry/space.hpp:1068-1072) -- a negative
+        coordinate reads at its absolute value.  Returns the wrapped points and, per mirrored
+        axis, the mask of reflected points (their normal vector components change sign,
         InterpolationFlags::postprocess, interpolation.hpp:272-287)."""
-        if self._geometry_kind != "cylindrical":
-            return pts, np.zeros(len(pts), bool)
-        mirrored = pts[:, 0] < 0.0
+        sym = list(getattr(self._geometry, "symmetric", (False, False)) or (False, False)) + [False, False]
+        sym = sym[:2]
+        if self._geometry_kind == "cylindrical":
+            sym[0] = True
+        flips = {}
+        if not any(sym):
+            return pts, flips
         w = pts.copy()
-        w[:, 0] = np.abs(w[:, 0])
-        w[w[:, 0] == 0.0, 0] = 1e-12
-        return w, mirrored
+        for d, on in enumerate(sym):
+            if on:
+                flips[d] = w[:, d] < 0.0
+                w[:, d] = np.abs(w[:, d])
+                w[w[:, d] == 0.0, d] = 1e-12
+        return w, flips
 
     def _get_temperatures(self, dst_mesh, interpolation="linear"):
         """Temperatures on a destination mesh or points (therm2d.cpp:544-553): bilinear or the
@@ -379,7 +392,7 @@ class Static2D:
         if dst_mesh is None:
             return q
         mids = [0.5 * (a[1:] + a[:-1]) for a in self._mesh.axes]
-        pts, mirrored = self._wrap(_points2d(dst_mesh))
+        pts, flips = self._wrap(_points2d(dst_mesh))
         active = self._active_elements()
         method = _check_interpolation(interpolation, splines=True)
         if method in ("spline", "smooth_spline"):
@@ -394,7 +407,8 @@ class Static2D:
             out = q[i1, i0].copy()
         else:
             out = np.stack([_bilinear(mids, q[..., c], pts, fill=None) for c in range(2)], axis=-1)
-        out[mirrored, 0] *= -1.0  # the radial component of a mirrored point (Symmetry::NP)
+        for d, m in flips.items():  # the normal component of a mirrored point (Symmetry NP / PN)
+            out[m, d] *= -1.0
         return out
 
     def _get_conductivity(self, dst_mesh, interpolation="linear"):

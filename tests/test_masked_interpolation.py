@@ -352,10 +352,10 @@ def test_cylindrical_providers_mirror_negative_radii():
     for m in ("linear", "nearest", "spline"):
         out = sv.outTemperature(pts, m)
         assert out[0] == out[1]
-    w, mirrored = sv._wrap(pts)
-    assert mirrored.tolist() == [False, True, False] and w[1, 0] == 7.3 and w[2, 0] == 1e-12
+    w, flips = sv._wrap(pts)
+    assert flips[0].tolist() == [False, True, False] and w[1, 0] == 7.3 and w[2, 0] == 1e-12
     flat = T2.solver_for_structure2d(s, cls=T2.Static2D, ordering="10")
-    assert not flat._wrap(pts)[1].any()
+    assert flat._wrap(pts)[1] == {}
 
 
 def test_electrical_providers_mirror_the_symmetric_axes():
@@ -382,3 +382,31 @@ def test_electrical_providers_mirror_the_symmetric_axes():
     j[..., 0], j[..., 1], j[..., 2] = 1.0, 2.0, 3.0
     out = sv._element_interp(j, pts=pts)
     np.testing.assert_allclose(out, [[1.0, 2.0, 3.0], [-1.0, -2.0, 3.0], [1.0, -2.0, 3.0]])
+
+
+def test_symmetric_thermal_geometry_mirrors_the_providers():
+    """A Static3D geometry mirrored at x = 0 and y = 0 (PLaSK's mirror edges): the temperature
+    at (-x, -y) is the one at (x, y)."""
+    from plask_gb300 import structures as S
+    from plask_gb300 import thermal as TH
+
+    s = S.layered_c0(seed=2, n=(7, 6, 9), power=1e15)
+    sv = TH.solver_for_structure(s, ordering="012", algorithm="gpu-mixed")
+    sv.geometry = TH.StructureGeometry(sv.geometry.materials, mat=s.mat, symmetric=(True, True, False))
+    n = len(sv.mesh)
+
+    class _Handle:
+        @staticmethod
+        def temperature():
+            return 300.0 + (np.arange(n) % 11).astype(float)
+
+        @staticmethod
+        def sizes():
+            return n, 0
+
+    sv._fem = _Handle()
+    z = 0.5 * (s.axes[2][2] + s.axes[2][3])
+    pts = np.array([[4.0, 6.0, z], [-4.0, -6.0, z], [4.0, -6.0, z]])
+    for m in ("linear", "nearest", "smooth_spline"):
+        out = sv.outTemperature(pts, m)
+        assert out[0] == out[1] == out[2]
