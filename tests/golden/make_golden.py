@@ -24,6 +24,9 @@ Fixtures:
   Crank-Nicolson, k(T) rebuilt every 3 steps, 2 ns in 0.2 ns steps, ORDER_10.
 * ``shockley3d_junction_21x19x30``: Shockley3D (electr3d.cpp), a layered junction
   structure, 5 loops, ORDER_102.
+* ``thermoelectric3d_19x19x28``: the ThermoElectric3D loop (thermoelectric.py:181-219):
+  electrical compute(6), its Joule heat to the thermal problem, thermal compute(1),
+  until both errors are within maxerr, ORDER_012.
 """
 from __future__ import annotations
 
@@ -188,6 +191,24 @@ def shockley3d():
     G.save("shockley3d_junction_21x19x30", arr, meta)
 
 
+def thermoelectric3d():
+    s = S.shockley_c4(seed=4003, n=(19, 19, 28), voltage=2.1)
+    order, tfreq = "012", 6
+    p = E.from_structure(s, order=order)
+    tp = O.from_structure(s.thermal, order=order)
+    state, T, rounds = {}, None, []
+    ve, tt = 2 * s.maxerr, 2 * tp.maxerr
+    while tt > tp.maxerr or ve > s.maxerr:
+        V, conds, ve, _ = E.compute(p, loops=tfreq, state=state)
+        tp.heat = E.heat(p, V, conds)
+        T, tt, _ = O.compute(tp, loops=1, T=T)
+        rounds.append([ve, tt])
+    arr, meta = G.pack_elec(s)
+    arr.update(T_cholesky=T, V_cholesky=V)
+    meta.update(kind="thermoelectric3d", order=order, tfreq=tfreq, rounds=rounds)
+    G.save("thermoelectric3d_19x19x28", arr, meta)
+
+
 def main():
     if not N.available():
         raise SystemExit("oracle/_ref/libnspcg_ref.so is not built: make -C oracle ref (needs the reference tree)")
@@ -199,6 +220,7 @@ def main():
     dynamic3d()
     dynamiccyl()
     shockley3d()
+    thermoelectric3d()
     for n in G.names():
         print(n, (HERE / f"{n}.npz").stat().st_size, "bytes")
 

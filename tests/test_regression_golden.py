@@ -88,6 +88,19 @@ def test_oracle_replays_fixture(name):
         T = O2.to_full(p, node_id, T, fill=np.nan)
         assert _same_nan(T, data["T_direct"]) and _maxdiff(T, data["T_direct"]) <= 1e-9
         assert steps == meta["steps"] and elaps == pytest.approx(meta["elapsed"], abs=1e-12)
+    elif kind == "thermoelectric3d":
+        s = G.unpack_elec(data, meta)
+        p = E.from_structure(s, order=meta["order"])
+        tp = O.from_structure(s.thermal, order=meta["order"])
+        state, T, n = {}, None, 0
+        ve, tt = 2 * s.maxerr, 2 * tp.maxerr
+        while tt > tp.maxerr or ve > s.maxerr:
+            V, conds, ve, _ = E.compute(p, loops=meta["tfreq"], state=state)
+            tp.heat = E.heat(p, V, conds)
+            T, tt, _ = O.compute(tp, loops=1, T=T)
+            n += 1
+        assert n == len(meta["rounds"])
+        assert _maxdiff(T, data["T_cholesky"]) <= 1e-9 and _maxdiff(V, data["V_cholesky"]) <= 1e-12
     elif kind == "shockley3d":
         s = G.unpack_elec(data, meta)
         p = E.from_structure(s, order=meta["order"], convergence=meta["convergence"])
@@ -211,3 +224,21 @@ def test_gpu_shockley3d_matches_fixture():
     assert _maxdiff(sv._full_potential(), data["V_cholesky"]) <= TOL_V
     assert sv.err == pytest.approx(meta["toterr"], rel=1e-6)
     assert sv.get_total_current() == pytest.approx(meta["total_current"], rel=1e-7)
+
+
+@pytest.mark.gpu
+def test_gpu_thermoelectric3d_matches_fixture():
+    from plask_gb300 import electrical as EL
+    from plask_gb300 import thermal as TH
+
+    data, meta = G.load("thermoelectric3d_19x19x28")
+    s = G.unpack_elec(data, meta)
+    te = EL.ThermoElectric3D()
+    te.thermal = TH.solver_for_structure(s.thermal, ordering=meta["order"], algorithm="gpu-mixed")
+    te.electrical = EL.solver_for_structure(s, ordering=meta["order"], algorithm="gpu-mixed")
+    te.reconnect()
+    verr, terr = te.compute()
+    assert verr <= te.electrical.maxerr and terr <= te.thermal.maxerr
+    assert len(te.history) == len(meta["rounds"])
+    assert _maxdiff(te.thermal._full_temperature(), data["T_cholesky"]) <= TOL_T
+    assert _maxdiff(te.electrical._full_potential(), data["V_cholesky"]) <= TOL_V
