@@ -219,9 +219,13 @@ int plgpu_fem3d_mult(plgpu_fem3d* h, int precision, const double* x, double* y);
      that every GPU loading this library keeps until the process exits; meshes
      with more nodes are rejected with PLGPU_ERR_ARG.
    - The handle must already be set up on the device (PLGPU_ERR_STATE otherwise):
-     call plgpu_fem3d_compute or plgpu_fem3d_mult on it once first.
-   - The first call on a device looks up the array's device address
-     (cudaGetSymbolAddress); make that first call before any stream capture.
+     call plgpu_fem3d_compute or plgpu_fem3d_mult on it once first.  The call
+     must run with the handle's device current (PLGPU_ERR_STATE otherwise).
+   - The array's device address is looked up (cudaGetSymbolAddress) once per
+     device when a handle is created on that device, not in this call.  Under
+     CUDA's lazy module loading that look-up is when the driver places the array
+     on the device, so the 16 MiB are taken at handle creation.
+   - Works on 3D and planar (plgpu_fem2d_create) handles alike.
    - All calls share the array, which keeps the last call's contents; calls that
      overlap on the GPU (two handles on two streams at once) race on it. */
 int plgpu_fem3d_mult_noalloc(plgpu_fem3d* h, int precision, const double* x, double* y);

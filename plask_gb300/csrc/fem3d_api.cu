@@ -103,6 +103,56 @@ void upload(DevBuf& d, const std::vector<T>& v, cudaStream_t s) {
 
 }  // namespace
 
+// ---------------------------------------------------------------------------------------
+// Multiply without allocation (plgpu_fem3d_mult_noalloc).
+//
+// Some callers cannot allocate device memory at the moment they need A x: a host
+// framework that has reserved the whole GPU for its own caching allocator (cudaMalloc
+// fails), or a latency-critical loop on other streams that cannot afford the
+// device-wide synchronisation cudaMalloc and cudaFree may cause.  plgpu_fem3d_mult stages the vectors in a
+// buffer it allocates per call; plgpu_fem3d_mult_noalloc stages them in the
+// file-scope array below instead (16 MiB).
+//
+// Host code cannot use the array's name as a device address (in host code it names a
+// host-side shadow), so its address is looked up with cudaGetSymbolAddress, once per
+// device, when a handle is set up on that device (noalloc_setup, called from
+// setup_mesh).  Looking it up loads this file's module onto the device, which under
+// CUDA's lazy module loading is when the driver allocates the array; doing it at set-up,
+// where the handle allocates its own buffers anyway, keeps that allocation out of the
+// call.  From then on the device holds the array until the process exits.
+//
+// The array is shared by all calls and all handles and keeps the last call's
+// contents.  Nothing in it needs to start at zero: every word a call reads is
+// written by the same call first.  Calls that overlap on the GPU (two handles on
+// two streams at the same time) race on it.
+
+namespace {
+constexpr size_t kNoAllocMaxNodes = size_t(1) << 21;  // 2,097,152 nodes
+constexpr int kNoAllocMaxDevices = 64;
+__device__ __align__(256) double g_noalloc_stage[kNoAllocMaxNodes];
+
+std::mutex g_noalloc_mutex;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};  // device address of g_noalloc_stage, per device
+
+// Look up the staging array's device address on device `dev` (the current device) once.
+void noalloc_setup(int dev) {
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return;  // mult_noalloc rejects such devices
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        ck(cudaGetSymbolAddress(&p, g_noalloc_stage), "cudaGetSymbolAddress");
+        g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+}
+
+// The address looked up at set-up for device `dev`, or nullptr.
+double* noalloc_stage(int dev) {
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return nullptr;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    return g_noalloc_ptr[dev];
+}
+}  // namespace
+
 struct plgpu_unet {
     std::string err;
     UNetModel model;
@@ -123,6 +173,7 @@ struct plgpu_fem3d {
     int planar = 0;
     DevBuf rmid64, rmid32;  // cylindrical: midpoint radius of every element column
     cudaStream_t stream = nullptr;
+    int device = 0;  // the device current at set-up, which owns the stream and every buffer
     LaunchCfg cfg{};
     int sm_count = 0;
 
@@ -290,7 +341,9 @@ struct plgpu_fem3d {
         ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
         int dev = 0;
         ck(cudaGetDevice(&dev), "cudaGetDevice");
+        device = dev;
         ck(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+        noalloc_setup(dev);  // the no-allocation multiply's staging array, looked up here and not in the call
         cfg.stream = stream;
         cfg.sm_count = sm_count;
         if (const char* e = std::getenv("PLGPU_NO_GRAPHS")) use_graphs = !(e[0] == '1');
@@ -1795,7 +1848,17 @@ struct plgpu_fem3d {
 
     // y = A x with the system matrix of the current temperature (FemMatrix::mult, matrix.hpp:89):
     // after Dirichlet elimination, including the convective face terms.  Mesh-order arrays.
+    // the handle's buffers and stream belong to the device current at set-up
+    void check_device() const {
+        int dev = 0;
+        ck(cudaGetDevice(&dev), "cudaGetDevice");
+        if (dev != device)
+            throw StateError("the current CUDA device (" + std::to_string(dev) + ") is not the device the handle "
+                             "was created on (" + std::to_string(device) + ")");
+    }
+
     void mult(int precision, const double* xin, double* yout) {
+        check_device();
         if (!initialized) initialize();
         if (bc_dirty) materialize_bc();
         update_coef();
@@ -1910,46 +1973,6 @@ struct plgpu_fem3d {
     }
 };
 
-// ---------------------------------------------------------------------------------------
-// Multiply without allocation.
-//
-// Some callers cannot allocate device memory at the moment they need A x: a host
-// framework that has reserved the whole GPU for its own caching allocator (cudaMalloc
-// fails), or a latency-critical loop on other streams that cannot afford the
-// device-wide synchronisation cudaMalloc and cudaFree may cause.  plgpu_fem3d_mult stages the vectors in a
-// buffer it allocates per call; plgpu_fem3d_mult_noalloc stages them in the
-// file-scope array below instead, which every GPU that loads this library keeps for
-// the life of the process (16 MiB).
-//
-// The array is shared by all calls and all handles and keeps the last call's
-// contents.  Nothing in it needs to start at zero: every word a call reads is
-// written by the same call first.  Calls that overlap on the GPU (two handles on
-// two streams at the same time) race on it.
-
-namespace {
-constexpr size_t kNoAllocMaxNodes = size_t(1) << 21;  // 2,097,152 nodes
-__device__ __align__(256) double g_noalloc_stage[kNoAllocMaxNodes];
-
-std::mutex g_noalloc_mutex;
-double* g_noalloc_ptr[64] = {};  // device address of g_noalloc_stage, per device
-
-// Device address of the staging array on the current device.  Obtained once per
-// device with cudaGetSymbolAddress (host code cannot use the symbol itself: in host
-// code its name stands for a host-side shadow, not a device address).
-double* noalloc_stage() {
-    int dev = 0;
-    ck(cudaGetDevice(&dev), "cudaGetDevice");
-    if (dev < 0 || dev >= 64) throw StateError("device index out of range for the no-allocation multiply");
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
-        void* p = nullptr;
-        ck(cudaGetSymbolAddress(&p, g_noalloc_stage), "cudaGetSymbolAddress");
-        g_noalloc_ptr[dev] = static_cast<double*>(p);
-    }
-    return g_noalloc_ptr[dev];
-}
-}  // namespace
-
 void plgpu_fem3d::mult_noalloc(int precision, const double* xin, double* yout) {
     if ((size_t)N > kNoAllocMaxNodes)
         throw ArgError("plgpu_fem3d_mult_noalloc handles meshes of at most " + std::to_string(kNoAllocMaxNodes) +
@@ -1957,7 +1980,11 @@ void plgpu_fem3d::mult_noalloc(int precision, const double* xin, double* yout) {
     if (!initialized || bc_dirty)
         throw StateError("plgpu_fem3d_mult_noalloc needs a handle whose mesh, materials and boundary conditions "
                          "are already set up on the device: call plgpu_fem3d_compute or plgpu_fem3d_mult once first");
-    double* stage = noalloc_stage();
+    check_device();
+    double* stage = noalloc_stage(device);
+    if (!stage)
+        throw StateError("the no-allocation staging array has no device address on device " +
+                         std::to_string(device));
     update_coef();
     ck(cudaMemcpyAsync(stage, xin, (size_t)N * 8, cudaMemcpyHostToDevice, stream), "H2D x");
     launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], n[1], n[2], ns[0], ns[1], ns[2], stage, p64.as<double>(),

@@ -4,16 +4,28 @@ It exists for callers that cannot allocate device memory when they need the
 product -- a framework that has reserved the whole GPU for its own allocator, or
 a latency-critical loop that cannot afford the device-wide synchronisation of
 cudaMalloc/cudaFree.  Its staging buffer is a static device array of 2,097,152
-doubles shared by all calls.  These tests call it through the C ABI and compare
-it with plgpu_fem3d_mult on the same inputs, two calls in a row; this file is
-collected last so that a failure here stops a -x run only after every other test.
+doubles shared by all calls, whose address is looked up when a handle is created.
+These tests call it through the C ABI and compare it with plgpu_fem3d_mult on the
+same inputs, two calls in a row, on 3D and planar handles, and check in a fresh
+process (CUDA's default lazy module loading) that repeated calls leave the
+device's free memory unchanged.  This file is collected last so that a failure
+here stops a -x run only after every other test.
 """
+import os
+import pathlib
+import subprocess
+import sys
+import textwrap
+
 import numpy as np
 import pytest
 
 from plask_gb300 import _native
 from plask_gb300 import structures as S
 from plask_gb300 import thermal as TH
+from plask_gb300 import thermal2d as T2
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
 
 pytestmark = pytest.mark.gpu
 
@@ -74,3 +86,61 @@ def test_noalloc_rejects_meshes_above_the_limit_and_unprepared_handles():
             small.mult_noalloc(np.zeros(125), 64)
     finally:
         small.close()
+
+
+@pytest.mark.parametrize("cls", [T2.Static2D, T2.StaticCyl])
+def test_noalloc_on_planar_handles(cls):
+    s = S.layered_2d(seed=71, n=(25, 31), anisotropic=True)
+    s.convection = [("top", 3e3, 300.0)]
+    sv = T2.solver_for_structure2d(s, cls=cls, ordering="10")
+    sv.compute(1)
+    fem = sv._fem
+    nn, _ = fem.sizes()
+    rng = np.random.default_rng(6)
+    for precision, rtol in ((64, RTOL64), (32, RTOL32)):
+        for _ in range(2):
+            x = 300.0 + rng.standard_normal(nn)
+            ref = fem.mult(x, precision)
+            got = fem.mult_noalloc(x, precision)
+            assert np.max(np.abs(got - ref)) <= rtol * np.max(np.abs(ref))
+
+
+_FREE_MEMORY_PROBE = textwrap.dedent("""
+    import sys
+    import numpy as np
+    import torch
+    sys.path.insert(0, sys.argv[1])
+    from plask_gb300 import structures as S
+    from plask_gb300 import thermal as TH
+    s = S.layered_c1(seed=34, n=(21, 18, 24))
+    sv = TH.solver_for_structure(s, ordering="201", algorithm="gpu-mixed")
+    sv.compute(1)
+    fem = sv._fem
+    nn, _ = fem.sizes()
+    x = np.random.default_rng(7).standard_normal(nn)
+    ref = fem.mult(x, 64)
+    fem.mult_noalloc(x, 64)   # warm-up: the kernels of the multiply are loaded by now
+    fem.mult_noalloc(x, 32)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(0)[0]
+    for _ in range(5):
+        y64 = fem.mult_noalloc(x, 64)
+        y32 = fem.mult_noalloc(x, 32)
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info(0)[0]
+    err = float(np.max(np.abs(y64 - ref)) / np.max(np.abs(ref)))
+    print("FREE", free0, free1, "ERR", err)
+""")
+
+
+def test_noalloc_leaves_free_memory_unchanged_in_a_fresh_process():
+    pytest.importorskip("torch")
+    env = dict(os.environ)
+    env.pop("CUDA_MODULE_LOADING", None)  # the driver's default: lazy loading
+    r = subprocess.run([sys.executable, "-c", _FREE_MEMORY_PROBE, str(ROOT)], capture_output=True, text=True,
+                       timeout=600, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("FREE")][-1].split()
+    free0, free1, err = int(line[1]), int(line[2]), float(line[4])
+    assert free1 == free0, f"free device memory changed across no-allocation calls: {free0} -> {free1}"
+    assert err <= RTOL64
