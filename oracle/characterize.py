@@ -60,7 +60,8 @@ def run(solver, zeta, maxit=1000, max_loops=12):
     return {"solver": solver, "zeta": zeta, "maxit": maxit, "loops": loops, "wall_s": time.perf_counter() - t_start}
 
 
-def _nspcg_solve(sv, coef, off, b, x0):
+def build_matrix(coef, off):
+    """The symmetric CSR matrix of the reference's 14-diagonal storage coef[d, c] = A(c, c + off[d])."""
     import scipy.sparse as sp
 
     nd, n = coef.shape
@@ -70,8 +71,12 @@ def _nspcg_solve(sv, coef, off, b, x0):
         o = int(off[d])
         diags += [coef[d, :-o], coef[d, :-o]]
         offs += [o, -o]
-    A = sp.diags(diags, offs, shape=(n, n), format="csr")
-    return sv.solve(A, b, x0)
+    return sp.diags(diags, offs, shape=(n, n), format="csr")
+
+
+def _nspcg_solve(sv, coef, off, b, x0):
+    # NSPCG takes the eliminated matrix; rebuild it from the diagonal storage
+    return sv.solve(build_matrix(coef, off), b, x0)
 
 
 if __name__ == "__main__":
