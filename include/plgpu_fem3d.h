@@ -230,6 +230,18 @@ int plgpu_fem3d_mult(plgpu_fem3d* h, int precision, const double* x, double* y);
      overlap on the GPU (two handles on two streams at once) race on it. */
 int plgpu_fem3d_mult_noalloc(plgpu_fem3d* h, int precision, const double* x, double* y);
 
+/* The FP32 stiffness operator exactly as one inner CG iteration of the
+   mixed-precision solve applies it: the convective surface rows and the
+   stencil kernel the solve runs (the TMA-staged kernel where the mesh allows
+   it), on the mesh-order vector x rounded to FP32; y = A x widened to double,
+   without the Dirichlet identity rows (the CG direction is zero on Dirichlet
+   nodes: pass x with zeros there to get the solve's product).  *xax (may be
+   NULL) receives the sum of the kernel's per-block partials of (x, A x) in the
+   solve's fixed order; *staged (may be NULL) is 1 when the TMA-staged kernel
+   ran.  No counterpart in the reference (verification of the inner solve's
+   kernel). */
+int plgpu_fem3d_cg_operator(plgpu_fem3d* h, const double* x, double* y, double* xax, int* staged);
+
 /* Time the operator kernel (one matrix-free stiffness application, the
    inner kernel of every CG iteration) on the handle's stream with CUDA
    events: `reps` launches on the current coefficients, optionally with the

@@ -98,6 +98,7 @@ SIGNATURES = {
     "plgpu_fem3d_set_preconditioner": (C.c_int, [_h, _h]),
     "plgpu_fem3d_mult": (C.c_int, [_h, C.c_int, _dp, _dp]),
     "plgpu_fem3d_mult_noalloc": (C.c_int, [_h, C.c_int, _dp, _dp]),
+    "plgpu_fem3d_cg_operator": (C.c_int, [_h, _dp, _dp, _dp, C.POINTER(C.c_int)]),
     # include/plgpu_elec3d.h
     "plgpu_elec3d_create": (C.c_int, [_dp, C.c_int, _dp, C.c_int, _dp, C.c_int, C.c_int, C.POINTER(_h)]),
     "plgpu_elec3d_destroy": (C.c_int, [_h]),
@@ -346,6 +347,18 @@ class Fem3D:
         self._check(self._lib.plgpu_fem3d_mult_noalloc(self._h, int(precision), _ptr(xv, C.c_double),
                                                        _ptr(y, C.c_double)))
         return y
+
+    def cg_operator(self, x):
+        """(A x, (x, A x), staged) with the FP32 operator of the inner CG iteration.
+
+        ``staged`` is True when the TMA-staged kernel ran.  No Dirichlet replacement."""
+        xv = _f64(x).ravel()
+        y = np.empty_like(xv)
+        xax = C.c_double(0.0)
+        st = C.c_int(0)
+        self._check(self._lib.plgpu_fem3d_cg_operator(self._h, _ptr(xv, C.c_double), _ptr(y, C.c_double),
+                                                      C.byref(xax), C.byref(st)))
+        return y, xax.value, bool(st.value)
 
     def time_operator(self, precision=32, reps=20, flush_l2=True):
         """(mean ms per launch, algorithmic bytes per launch) of the stiffness-operator kernel."""

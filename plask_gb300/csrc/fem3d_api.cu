@@ -217,6 +217,8 @@ struct plgpu_fem3d {
     SurfaceT<float> s32{};
     DevBuf s_row, s_ptr, s_col, s_val64, s_val32;
     DevBuf smask;  // bit per node: the node has a surface row (CG mode adds k_surface_cg's S x)
+    DevBuf splane, smap;  // the TMA operator's surface rows (TmaSurface): plane index, node -> row maps
+    TmaSurface tsurf{};
     int rad_rows = 0;
     DevBuf rad_row, rad_ptr, rad_src, rad_coef, rad_tamb;
     int n_fbc = 0;
@@ -265,6 +267,14 @@ struct plgpu_fem3d {
 
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
 
+    // TMA-staged FP32 CG operator (fem3d_operator_tma.cu) on the direction p32, with its
+    // pre-scaled conductances; created on the first coefficient update of a mesh it supports
+    TmaOperator* tma = nullptr;
+    bool tma_tried = false;
+    bool tma_fresh = false;  // tmaP / tmaQ hold the current coefficients
+    DevBuf tmaP, tmaQ;
+    DevBuf cgpart;  // partial regions of the CG on the TMA operator
+
     // CUDA graphs of CG chunks: one per (precision, chunk length)
     struct ChunkGraph {
         int len = 0;
@@ -283,6 +293,7 @@ struct plgpu_fem3d {
 
     ~plgpu_fem3d() {
         invalidate_graphs();
+        if (tma) tma_operator_destroy(tma);
         if (h_ctl) cudaFreeHost(h_ctl);
         for (cudaEvent_t e : {ev0, ev1, ev2, ev3})
             if (e) cudaEventDestroy(e);
@@ -903,6 +914,23 @@ struct plgpu_fem3d {
             std::vector<uint32_t> sm((size_t)(N + 31) / 32 + 1, 0u);
             for (int r : srow) sm[(size_t)r >> 5] |= 1u << (r & 31);
             upload(smask, sm, stream);
+            // the TMA operator's node -> surface row maps of the planes that hold surface rows
+            const long long plane = (long long)n[0] * n[1];
+            std::vector<int> sp((size_t)n[2], 0);
+            int nplanes = 0;
+            for (int r : srow)
+                if (sp[(size_t)(r / plane)] == 0) sp[(size_t)(r / plane)] = -1;
+            for (int k = 0; k < n[2]; ++k)
+                if (sp[k] == -1) sp[k] = ++nplanes;
+            std::vector<int> smap_h((size_t)std::max(nplanes, 1) * plane, -1);
+            for (size_t q = 0; q < srow.size(); ++q) {
+                const long long r = srow[q];
+                smap_h[(size_t)(sp[(size_t)(r / plane)] - 1) * plane + (size_t)(r % plane)] = (int)q;
+            }
+            upload(splane, sp, stream);
+            upload(smap, smap_h, stream);
+            tsurf = TmaSurface{nplanes > 0 ? splane.as<int>() : nullptr, smap.as<int>(), s_ptr.as<int>(),
+                               s_col.as<int>(), s_val32.as<float>()};
         }
 
         std::vector<int> fi;
@@ -973,6 +1001,38 @@ struct plgpu_fem3d {
             launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab,
                         k64.as<double>(), k32.as<float>(), aniso ? kz64.as<double>() : nullptr,
                         aniso ? kz32.as<float>() : nullptr, aniso);
+        refresh_tma();
+    }
+
+    // The pre-scaled conductances of the TMA operator from the current FP64 ones; called after
+    // every write of k64 / kz64 outside a stream capture.  The first call on a mesh the kernel
+    // supports (n0 <= 224 and a multiple of 4) creates the operator.
+    void refresh_tma() {
+        tma_fresh = false;
+        if (planar) return;
+        if (tma && tma_operator_aniso(tma) != aniso) {
+            invalidate_graphs();  // captured chunks carry the old operator
+            tma_operator_destroy(tma);
+            tma = nullptr;
+            tma_tried = false;
+        }
+        if (!tma_tried) {
+            tma_tried = true;
+            if (std::getenv("PLGPU_NO_TMA") == nullptr && tma_operator_supported(n[0], n[1], n[2])) {
+                if (!tmaP.p) tmaP.alloc((size_t)N * 4);
+                if (aniso && !tmaQ.p) tmaQ.alloc((size_t)N * 4);
+                if (!cgpart.p) cgpart.alloc(sizeof(double) * 3 * kMaxPartialBlocks);
+                std::vector<double> hh[3];
+                for (int d = 0; d < 3; ++d)
+                    for (int i = 0; i + 1 < n[d]; ++i) hh[d].push_back(ax[d][i + 1] - ax[d][i]);
+                tma = tma_operator_create(cfg, g64, hh[0], hh[1], hh[2], aniso, p32.as<float>(), tmaP.as<float>(),
+                                          aniso ? tmaQ.as<float>() : nullptr);
+                if (tma) invalidate_graphs();
+            }
+        }
+        if (!tma) return;
+        launch_tma_coef(cfg, tma, g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr);
+        tma_fresh = true;
     }
     // Jacobi diagonal of the current operator and its inverse (FP64 and FP32); `shift` adds
     // the capacity's diagonal of a time step
@@ -1199,6 +1259,30 @@ struct plgpu_fem3d {
         status = floor_ok(relres) ? SOLVE_CONVERGED : SOLVE_MAXIT;
     }
 
+    // The CG of fem3d_cg_fused.cu runs where the TMA operator does
+    bool fused_ready() const { return !planar && tma != nullptr && tma_fresh && !dyn_active; }
+    TmaCg fused_args() {
+        return TmaCg{N, x32.as<float>(), r32v.as<float>(), p32.as<float>(), q32.as<float>(), minv32.as<float>(),
+                     cgpart.as<double>(), cfg.vec_blocks, tma_operator_blocks(tma)};
+    }
+    // x32 = the FP32 Jacobi-PCG solution of A x = r32v to inner_rtol: the TMA operator with
+    // the surface rows, then the update and direction kernels
+    void fused_cg(int& status, int& iters, int cap) {
+        SolveCtl* ctl = d_ctl.as<SolveCtl>();
+        const TmaCg f = fused_args();
+        launch_tmacg_start(cfg, f, ctl, inner_rtol, -1, cap, cap);
+        auto enqueue = [&](int len) {  // len is even: every chunk starts at parity 0
+            for (int it = 0; it < len; ++it) {
+                const int q = it & 1;
+                launch_operator_tma(cfg, tma, q32.as<float>(), tmacg_op_partials(f), tmacg_op_run(ctl, q), ctl,
+                                    tsurf);
+                launch_tmacg_update(cfg, f, ctl, q);
+                launch_tmacg_direction(cfg, f, ctl, q);
+            }
+        };
+        run_chunks(3, chunk, 256, enqueue, status, iters, cap);
+    }
+
     // r64 = b - A T (Dirichlet columns eliminated)
     void residual64() {
         op64(T.as<double>(), r64v.as<double>(), b.as<double>(), MODE_RESID);
@@ -1244,6 +1328,8 @@ struct plgpu_fem3d {
             int st = 0, it = 0;
             if (algorithm == PLGPU_ALGO_GPU_LEARNED && pre != nullptr) {
                 fcg_inner(st, it, cap - iters);
+            } else if (fused_ready()) {
+                fused_cg(st, it, cap - iters);
             } else {
                 launch_cg_start(cfg, N, x32.as<float>(), true, r32v.as<float>(), p32.as<float>(), minv32.as<float>(),
                                 part, ctl, inner_rtol, -1, cap - iters, cap);
@@ -1252,7 +1338,7 @@ struct plgpu_fem3d {
                                      cap - iters);
             }
             iters += it;
-            if (st == SOLVE_NONFINITE || st == SOLVE_BREAKDOWN) {
+            if (st == SOLVE_NONFINITE || st == SOLVE_BREAKDOWN || st == SOLVE_DEVICE_TIMEOUT) {
                 status = st;
                 return;
             }
@@ -1304,6 +1390,7 @@ struct plgpu_fem3d {
         if (bc_dirty) materialize_bc();
         launch_coef(cfg, n[0], n[1], n[2], T.as<double>(), d_mat.as<int>(), d_th.as<double>(), tab, k64.as<double>(),
                     k32.as<float>(), aniso ? kz64.as<double>() : nullptr, aniso ? kz32.as<float>() : nullptr, aniso);
+        refresh_tma();
         launch_diag(cfg, g64, k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, s64, dmask.as<uint32_t>(),
                     diag.as<double>(), minv64.as<double>(), minv32.as<float>());
         ensure_unet_buffers();
@@ -1535,6 +1622,8 @@ struct plgpu_fem3d {
             ck(cudaEventRecord(ev3, stream), "event");
             total_iters += iters;
             total_ref += refs;
+            if (status == SOLVE_DEVICE_TIMEOUT)
+                throw SolveError(PLGPU_ERR_CUDA, "a device-side wait for staged copies timed out");
             if (status == SOLVE_NONFINITE)
                 throw SolveError(PLGPU_ERR_NONFINITE, "non-finite value in the linear solve");
             if (status == SOLVE_BREAKDOWN)
@@ -1634,6 +1723,7 @@ struct plgpu_fem3d {
         if (aniso) ck(cudaMemcpyAsync(kzB64.p, kz64.p, N8, cudaMemcpyDeviceToDevice, stream), "copy kz");
         launch_scale4(cfg, N, dyn_theta, k64.as<double>(), k32.as<float>(), aniso ? kz64.as<double>() : nullptr,
                       aniso ? kz32.as<float>() : nullptr);
+        refresh_tma();
         if (dyn_lumping) {
             lumped_capacity(cap64.as<double>(), cap32.as<float>(), 1.0);
         } else {
@@ -1735,6 +1825,8 @@ struct plgpu_fem3d {
             ck(cudaEventRecord(ev3, stream), "event");
             total_iters += iters;
             total_ref += refs;
+            if (status == SOLVE_DEVICE_TIMEOUT)
+                throw SolveError(PLGPU_ERR_CUDA, "a device-side wait for staged copies timed out");
             if (status == SOLVE_NONFINITE) throw SolveError(PLGPU_ERR_NONFINITE, "non-finite value in the linear solve");
             if (status == SOLVE_BREAKDOWN)
                 throw SolveError(PLGPU_ERR_NOT_SPD, "system matrix is not positive definite (CG breakdown)");
@@ -1829,6 +1921,9 @@ struct plgpu_fem3d {
                 launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), p64.as<double>(), q64.as<double>(),
                                 k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(),
                                 nullptr, partials.as<double>(), MODE_CG, ctl);
+            else if (fused_ready())  // the kernel the FP32 CG solve runs, without surface rows
+                launch_operator_tma(cfg, tma, q32.as<float>(), partials.as<double>(), &ctl->status, ctl,
+                                    TmaSurface{});
             else
                 launch_operator(cfg, g32, zf32.as<float>(), zr32.as<float>(), p32.as<float>(), q32.as<float>(),
                                 k32.as<float>(), aniso ? kz32.as<float>() : nullptr, aniso, dmask.as<uint32_t>(),
@@ -1848,6 +1943,41 @@ struct plgpu_fem3d {
 
     // y = A x with the system matrix of the current temperature (FemMatrix::mult, matrix.hpp:89):
     // after Dirichlet elimination, including the convective face terms.  Mesh-order arrays.
+    // The FP32 operator exactly as one inner CG iteration applies it (the surface rows and
+    // the stencil kernel the solve uses, with its (x, A x) partials reduced in a fixed order)
+    // on a mesh-order vector; no Dirichlet replacement (the CG direction is zero on Dirichlet
+    // nodes).  *staged: 1 when that kernel is the TMA-staged one.
+    void cg_operator(const double* xin, double* yout, double* xax, int* staged) {
+        check_device();
+        if (!initialized) initialize();
+        if (bc_dirty) materialize_bc();
+        update_coef();
+        DevBuf tmp, scratch;
+        tmp.alloc((size_t)N * 8);
+        scratch.alloc(sizeof(SolveCtl));
+        SolveCtl* ctl = scratch.as<SolveCtl>();
+        ck(cudaMemsetAsync(ctl, 0, sizeof(SolveCtl), stream), "memset");  // SOLVE_RUNNING
+        ck(cudaMemcpyAsync(tmp.p, xin, (size_t)N * 8, cudaMemcpyHostToDevice, stream), "H2D x");
+        launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], n[1], n[2], ns[0], ns[1], ns[2], tmp.as<double>(),
+                                   p64.as<double>(), 0.0);
+        launch_norm2(cfg, N, p64.as<double>(), p32.as<float>(), partials.as<double>(), d_ctl.as<SolveCtl>(), 4);
+        const bool fused = fused_ready();
+        if (fused) {
+            launch_operator_tma(cfg, tma, q32.as<float>(), partials.as<double>(), &ctl->status, ctl, tsurf);
+            launch_partials_to_ctl(cfg, partials.as<double>(), tma_operator_blocks(tma), ctl);
+        } else {
+            op32(p32.as<float>(), q32.as<float>(), MODE_CG, ctl);
+        }
+        launch_widen(cfg, N, q32.as<float>(), q64.as<double>());
+        launch_to_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], (long long)n[0] * n[1], ns[0], ns[1], ns[2], 1,
+                                 q64.as<double>(), tmp.as<double>());
+        ck(cudaMemcpyAsync(yout, tmp.p, (size_t)N * 8, cudaMemcpyDeviceToHost, stream), "D2H y");
+        ck(cudaMemcpyAsync(h_ctl, ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, stream), "D2H ctl");
+        ck(cudaStreamSynchronize(stream), "sync");
+        if (xax) *xax = h_ctl->pq;
+        if (staged) *staged = fused ? 1 : 0;
+    }
+
     // the handle's buffers and stream belong to the device current at set-up
     void check_device() const {
         int dev = 0;
@@ -2249,6 +2379,7 @@ struct plgpu_elec3d : plgpu_fem3d {
                                             sig.as<double>());
             launch_elec_coef(cfg, N, sig.as<double>(), k64.as<double>(), k32.as<float>(), kz64.as<double>(),
                              kz32.as<float>());
+            refresh_tma();
             launch_diag(cfg, g64, k64.as<double>(), kz64.as<double>(), true, s64, dmask.as<uint32_t>(),
                         diag.as<double>(), minv64.as<double>(), minv32.as<float>());
             op64(vD.as<double>(), b.as<double>(), F.as<double>(), MODE_RHS);
@@ -2264,6 +2395,8 @@ struct plgpu_elec3d : plgpu_fem3d {
             ck(cudaEventRecord(ev3, stream), "event");
             total_iters += iters;
             total_ref += refs;
+            if (status == SOLVE_DEVICE_TIMEOUT)
+                throw SolveError(PLGPU_ERR_CUDA, "a device-side wait for staged copies timed out");
             if (status == SOLVE_NONFINITE)
                 throw SolveError(PLGPU_ERR_NONFINITE, "non-finite value in the linear solve");
             if (status == SOLVE_BREAKDOWN)
@@ -2651,6 +2784,13 @@ int plgpu_fem3d_mult_noalloc(plgpu_fem3d* h, int precision, const double* x, dou
         if (precision != 32 && precision != 64) throw ArgError("precision must be 32 or 64");
         if (!x || !y) throw ArgError("null vector");
         h->mult_noalloc(precision, x, y);
+    });
+}
+
+int plgpu_fem3d_cg_operator(plgpu_fem3d* h, const double* x, double* y, double* xax, int* staged) {
+    return guarded(h, [&] {
+        if (!x || !y) throw ArgError("null vector");
+        h->cg_operator(x, y, xax, staged);
     });
 }
 

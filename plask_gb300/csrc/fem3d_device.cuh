@@ -45,10 +45,17 @@ struct SolveCtl {
     int plain;        // nonzero: judge convergence on (r, r) instead of the Jacobi-scaled (r, M^-1 r)
     unsigned int arrive[4];   // arrival counters of the grid reductions
     double red[8];            // results of auxiliary reductions (norms, err, maxT)
+    // FP32 CG on the TMA operator (fem3d_cg_fused.cu): the kernels of iteration parity q
+    // read slot q of these and the direction kernel writes slot 1 - q, so that no block
+    // reads a word another block of the same launch writes
+    double rz2[2];     // (r, M^-1 r) of the current iterate
+    int status2[2];    // solve status before the iteration
+    int ustatus;       // the update kernel's verdict on (p, A p), read by the direction kernel
 };
 
+// SOLVE_DEVICE_TIMEOUT: a kernel's bounded wait for its own asynchronous copies ran out
 enum { SOLVE_RUNNING = 0, SOLVE_CONVERGED = 1, SOLVE_MAXIT = 2, SOLVE_BREAKDOWN = 3, SOLVE_NONFINITE = 4,
-       SOLVE_STAGNATED = 5 };
+       SOLVE_STAGNATED = 5, SOLVE_DEVICE_TIMEOUT = 6 };
 
 // Sparse symmetric surface operator (convective boundary terms), rows unique,
 // restricted to free (non-Dirichlet) rows and columns.

@@ -2,6 +2,8 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 #include "fem3d_device.cuh"
@@ -64,6 +66,57 @@ void launch_operator(const LaunchCfg& c, const GridT<double>& g, const double* z
                      double* y, const double* kxy, const double* kz, bool aniso, const uint32_t* dmask,
                      const double* rhs, double* partials, int mode, SolveCtl* ctl, const uint32_t* smask = nullptr,
                      int sslots = 0, const double* dshift = nullptr, const double* cmass = nullptr);
+// TMA-staged FP32 operator of the inner CG (fem3d_operator_tma.cu) on one fixed input
+// vector x (the tensor map is encoded for it), for meshes with n0 <= 224 and n0 a multiple
+// of 4 (the copy's row stride must be a multiple of 16 bytes).
+struct TmaOperator;
+bool tma_operator_supported(int n0, int n1, int n2);
+// nullptr when the mesh is not supported or a CUDA call fails; hx, hy, hz: element sizes
+TmaOperator* tma_operator_create(const LaunchCfg& c, const GridT<double>& g, const std::vector<double>& hx,
+                                 const std::vector<double>& hy, const std::vector<double>& hz, bool aniso,
+                                 const float* x, float* P, float* Q);
+void tma_operator_destroy(TmaOperator* t);
+int tma_operator_blocks(const TmaOperator* t);  // partial-sum slots of one launch
+const float* tma_operator_input(const TmaOperator* t);
+bool tma_operator_aniso(const TmaOperator* t);
+// P = k_xy dx dy dz / 48, Q = k_z dx dy / (16 dz) per element from the FP64 conductivities
+void launch_tma_coef(const LaunchCfg& c, const TmaOperator* t, const GridT<double>& g, const double* kxy,
+                     const double* kz);
+// Convective surface rows for the TMA operator: plane[k] = 0 when z-plane k holds none,
+// else 1 + the index of its node -> row map (map[(plane[k] - 1) n0 n1 + j n0 + i], -1: no
+// row), and the rows' CSR (ptr, col, val) as in SurfaceT
+struct TmaSurface {
+    const int* plane;
+    const int* map;
+    const int* ptr;
+    const int* col;
+    const float* val;
+};
+// y = A x (+ S x on surface rows) for the operator's input x (no Dirichlet replacement);
+// one partial of (x, y) per block at partials[block]; nothing runs unless *run is
+// SOLVE_RUNNING; a timed-out wait sets ctl's status words to SOLVE_DEVICE_TIMEOUT
+void launch_operator_tma(const LaunchCfg& c, const TmaOperator* t, float* y, double* partials, const int* run,
+                         SolveCtl* ctl, const TmaSurface& s);
+// ---- FP32 Jacobi-PCG on the TMA operator (fem3d_cg_fused.cu): per iteration the operator
+// (q = A p), an update kernel and a direction kernel, each reducing the previous launch's
+// partials in every block; control words alternate with the iteration parity q.
+struct TmaCg {
+    long long N;
+    float *x, *r, *p, *q;
+    const float* minv;
+    double* part;  // 2 x kMaxPartialBlocks: (p, A p) per operator block; (r, M^-1 r), (r, r) per update block
+    int upd_blocks, op_blocks;
+};
+// x = 0, p = M^-1 r; the last block sets the stop threshold and the status (as launch_cg_start)
+void launch_tmacg_start(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, double rtol, int ref_slot, int maxit,
+                        int stall_limit);
+// where the operator writes its partials, and the status word its launch of parity q checks
+double* tmacg_op_partials(const TmaCg& f);
+const int* tmacg_op_run(SolveCtl* ctl, int q);
+void launch_tmacg_update(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, int q);
+void launch_tmacg_direction(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, int q);
+// ctl->pq = the sum of nslots block partials (fixed order)
+void launch_partials_to_ctl(const LaunchCfg& c, const double* partials, int nslots, SolveCtl* ctl);
 // dshift: a diagonal added to the operator (lumped capacity); cmass: per-element corner
 // capacities c of a consistent capacity matrix c (M (x) M (x) M), M = [[2,1],[1,2]] / 3
 // CG step, first half: y[row] = S x on the surface rows and block partials of (x, S x) in

@@ -46,3 +46,59 @@ def test_mult_matches_oracle_matrix(kind, order, after_loop):
     scale = np.max(np.abs(ref))
     assert np.max(np.abs(y64 - ref)) <= 1e-12 * scale
     assert np.max(np.abs(y32 - ref)) <= 2e-5 * scale
+
+
+# Meshes the TMA-staged CG kernel takes (n0 a multiple of 4, at most 224): one to seven
+# warps along x, partial row tiles, several z-chunks, convective top faces (surface rows in
+# one plane) and side conditions (surface rows in every plane).
+@pytest.mark.parametrize("shape,kind,order", [
+    ((36, 33, 21), "aniso", "201"),
+    ((40, 23, 17), "iso", "012"),
+    ((128, 20, 30), "aniso", "201"),
+    ((200, 12, 10), "aniso", "120"),
+    ((8, 9, 7), "iso", "210"),
+])
+def test_cg_operator_matches_oracle_matrix(shape, kind, order):
+    if kind == "iso":
+        s = S.layered_c0(seed=23, n=shape)
+        s.convection = [("top", 50.0, 300.0)]
+    else:
+        s = S.layered_c1(seed=23, n=shape)
+        s.heatflux = [("left", -2e4)]
+        s.convection = s.convection + [("front", 20.0, 310.0)]
+    sv = TH.solver_for_structure(s, ordering=order, algorithm="gpu-mixed")
+    sv.compute(1)
+    T = sv._full_temperature()
+    p = O.from_structure(s, order=order)
+    A, F, node_id, n = O.assemble(p, T)
+    is_d, vf, vl = O.dirichlet_values(p, node_id, n)
+    A2, _ = O.apply_dirichlet(A, F, is_d, vf, vl)
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal(n)
+    x[is_d] = 0.0  # the CG direction vanishes on Dirichlet nodes
+    ref = A2 @ x
+    y, xax, staged = sv._fem.cg_operator(x)
+    assert staged, "the TMA-staged kernel should run on this mesh"
+    free = ~is_d
+    scale = np.max(np.abs(ref))
+    assert np.max(np.abs(y[free] - ref[free])) <= 2e-5 * scale
+    ref_xax = float(x @ ref)
+    assert abs(xax - ref_xax) <= 1e-5 * abs(ref_xax)
+
+
+def test_cg_operator_falls_back_on_unaligned_meshes():
+    s = S.layered_c1(seed=24, n=(35, 17, 12))  # 35 columns: row stride not a multiple of 16 bytes
+    sv = TH.solver_for_structure(s, ordering="201", algorithm="gpu-mixed")
+    sv.compute(1)
+    T = sv._full_temperature()
+    p = O.from_structure(s, order="201")
+    A, F, node_id, n = O.assemble(p, T)
+    is_d, vf, vl = O.dirichlet_values(p, node_id, n)
+    A2, _ = O.apply_dirichlet(A, F, is_d, vf, vl)
+    x = np.random.default_rng(10).standard_normal(n)
+    x[is_d] = 0.0
+    ref = A2 @ x
+    y, xax, staged = sv._fem.cg_operator(x)
+    assert not staged
+    free = ~is_d
+    assert np.max(np.abs(y[free] - ref[free])) <= 2e-5 * np.max(np.abs(ref))

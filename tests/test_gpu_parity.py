@@ -25,6 +25,10 @@ CASES = [
     ("c0-012", lambda: S.layered_c0(seed=4, n=(9, 9, 14)), "012"),
     ("c1", lambda: S.layered_c1(seed=5, n=(12, 10, 18)), "201"),
     ("c1-210", lambda: S.layered_c1(seed=6, n=(11, 13, 15)), "210"),
+    # x-widths the TMA-staged operator and its CG take (a multiple of 4): two warps along
+    # x, several row tiles and z-chunks
+    ("c1-wide", lambda: S.layered_c1(seed=7, n=(36, 14, 20)), "201"),
+    ("c0-wide", lambda: S.layered_c0(seed=9, n=(40, 12, 22)), "120"),
 ]
 
 

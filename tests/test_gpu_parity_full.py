@@ -1,0 +1,80 @@
+"""GPU solves at the benchmark configurations' full sizes against the reference path.
+
+* 40 x 40 x 60 (the CPU-runnable configuration, ``structures.layered_c0(seed=1)``; seed 0 of
+  this generator runs away thermally): the oracle's band Cholesky (LAPACK dpbtrf/dpbtrs, as
+  cholesky_matrix.hpp:95,107) over the full outer loop, run here; the GPU's mixed-precision
+  and FP64 solvers must agree to 1e-6 K with the same number of outer loops.
+* 128 x 128 x 200 (the benchmark case, ``structures.layered_c1()``): too large for the band
+  Cholesky (433 GB), so the reference answer is the reference's own NSPCG driven to
+  zeta = 1e-12, stored in ``tests/golden/static3d_layered_c1_128x128x200_nspcg.npz`` at 16384
+  seeded nodes, the plane through the hottest node and the vertical line through it
+  (``tests/golden/make_golden_c1.py``).  The regenerated inputs must hash to the fixture's.
+"""
+import json
+import pathlib
+import sys
+
+import numpy as np
+import pytest
+
+from oracle import fem3d as O
+from plask_gb300 import structures as S
+from plask_gb300 import thermal as TH
+
+HERE = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE / "golden"))
+
+pytestmark = pytest.mark.gpu
+
+TOL_T = 1e-6  # K
+C1_FIXTURE = HERE / "golden" / "static3d_layered_c1_128x128x200_nspcg.npz"
+
+
+@pytest.fixture(scope="module")
+def c0_oracle():
+    s = S.layered_c0(seed=1)
+    p = O.from_structure(s)  # the optimal order (largest axis major), as the reference's generator picks
+    To, tot, rec = O.compute(p)
+    return s, p.order, To, tot, rec
+
+
+@pytest.mark.parametrize("algorithm", ["gpu-mixed", "gpu-pcg"])
+def test_c0_full_size_matches_band_cholesky(c0_oracle, algorithm):
+    s, order, To, tot_o, rec = c0_oracle
+    assert To.shape == (60, 40, 40)
+    sv = TH.solver_for_structure(s, ordering=order, algorithm=algorithm)
+    tot = sv.compute()
+    T = sv._full_temperature()
+    assert sv.stats["loops"] == len(rec)
+    assert np.max(np.abs(T - To)) <= TOL_T
+    assert abs(tot - tot_o) <= TOL_T
+    assert sv.stats["last_rel_residual"] <= 1e-12
+
+
+def c1_golden():
+    d = np.load(C1_FIXTURE)
+    return json.loads(str(d["meta"])), d
+
+
+def c1_max_dT(T, meta, d):
+    """max |T - T_ref| over the fixture's nodes, plane and line (T in (k, j, i) layout)."""
+    k, j, i = meta["hot_node"]
+    return max(float(np.max(np.abs(T.ravel()[d["idx"]] - d["T_idx"]))),
+               float(np.max(np.abs(T[k] - d["plane"]))), float(np.max(np.abs(T[:, j, i] - d["line"]))))
+
+
+@pytest.mark.skipif(not C1_FIXTURE.exists(), reason="the 128x128x200 NSPCG fixture is not generated")
+def test_c1_full_size_matches_reference_nspcg():
+    from make_golden_c1 import input_digest
+
+    meta, d = c1_golden()
+    s = S.layered_c1()
+    assert input_digest(s) == meta["input_sha256"], "the generator no longer gives the fixture's inputs"
+    sv = TH.solver_for_structure(s, ordering="best", algorithm="gpu-mixed")
+    tot = sv.compute()
+    T = sv._full_temperature()
+    assert sv.stats["loops"] == len(meta["loops"])
+    assert abs(tot - meta["toterr"]) <= TOL_T
+    dT = c1_max_dT(T, meta, d)
+    assert dT <= TOL_T, f"max |dT| = {dT:.3e} K against the reference's NSPCG"
+    assert sv.stats["last_rel_residual"] <= 1e-12
