@@ -1263,7 +1263,7 @@ struct plgpu_fem3d {
     bool fused_ready() const { return !planar && tma != nullptr && tma_fresh && !dyn_active; }
     TmaCg fused_args() {
         return TmaCg{N, x32.as<float>(), r32v.as<float>(), p32.as<float>(), q32.as<float>(), minv32.as<float>(),
-                     cgpart.as<double>(), cfg.vec_blocks, tma_operator_blocks(tma)};
+                     cgpart.as<double>(), tmacg_blocks(cfg), tma_operator_blocks(tma)};
     }
     // x32 = the FP32 Jacobi-PCG solution of A x = r32v to inner_rtol: the TMA operator with
     // the surface rows, then the update and direction kernels

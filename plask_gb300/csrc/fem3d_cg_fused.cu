@@ -14,6 +14,7 @@
 // kernels of parity q read rz2[q] and status2[q], the direction kernel writes slot 1 - q.
 // The stopping test, the stagnation watch and the iteration cap are those of k_cg_update
 // (fem3d_kernels.cu), taken on the new residual after each update.
+#include <algorithm>
 #include <cstdint>
 
 #include "fem3d_device.cuh"
@@ -22,9 +23,15 @@
 
 namespace plgpu {
 
+// Block size of the update and direction kernels (overridable at compile time for tuning
+// sweeps); the grid is 1024 threads per SM (one wave), 64 registers per thread.
+#ifndef PLGPU_CG_THREADS
+#define PLGPU_CG_THREADS 256
+#endif
+constexpr int kCgThreads = PLGPU_CG_THREADS;
+
 namespace {
-// float4 groups in flight per thread; the update and direction kernels run 4 blocks of 256
-// threads per SM (the grid is 4 blocks per SM: one wave), 64 registers per thread
+// float4 groups in flight per thread
 constexpr int kUnroll = 2;
 constexpr size_t kPQ = 0;                          // (p, A p): one value per operator block
 constexpr size_t kRZ = (size_t)kMaxPartialBlocks;  // (r, M^-1 r) and (r, r) per update block
@@ -32,7 +39,7 @@ constexpr size_t kRZ = (size_t)kMaxPartialBlocks;  // (r, M^-1 r) and (r, r) per
 
 // x = 0, p = M^-1 r, rz = (r, M^-1 r), rr = (r, r); the last block sets the stop threshold
 // and the status (as k_cg_start) and the words of both parities
-__global__ void __launch_bounds__(256) k_tmacg_start(const TmaCg f, SolveCtl* __restrict__ ctl, double rtol,
+__global__ void __launch_bounds__(kCgThreads) k_tmacg_start(const TmaCg f, SolveCtl* __restrict__ ctl, double rtol,
                                                      int ref_slot, int maxit, int stall_limit) {
     float rz = 0.f, rr = 0.f;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < f.N;
@@ -87,24 +94,35 @@ __device__ __forceinline__ void tmacg_update_one(float& x, float& r, float p, fl
     rr += rn * rn;
 }
 
-__global__ void __launch_bounds__(256, 4) k_tmacg_update(const TmaCg f, SolveCtl* __restrict__ ctl, int q) {
+__global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_update(const TmaCg f, SolveCtl* __restrict__ ctl, int q) {
     if (ctl->status2[q] != SOLVE_RUNNING) return;
-    double pv[1];
-    reduce_partials<1, OpSum>(pv, f.part + kPQ, f.op_blocks);
-    const double pq = pv[0];
-    const double rz = ctl->rz2[q];
-    int st = SOLVE_RUNNING;
-    if (!isfinite(pq))
-        st = SOLVE_NONFINITE;
-    else if (!(pq > 0.0))
-        st = SOLVE_BREAKDOWN;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        ctl->ustatus = st;
-        ctl->pq = pq;
-        ctl->alpha = st == SOLVE_RUNNING ? rz / pq : 0.0;
+    // warp 0 reduces the operator's partials; lane 0 takes the decision for the block
+    __shared__ int sh_st;
+    __shared__ float sh_alpha;
+    if (threadIdx.x < 32) {
+        double pv[1];
+        warp0_reduce_partials<1>(pv, f.part + kPQ, f.op_blocks);
+        if (threadIdx.x == 0) {
+            const double pq = pv[0];
+            const double rz = ctl->rz2[q];
+            int st = SOLVE_RUNNING;
+            if (!isfinite(pq))
+                st = SOLVE_NONFINITE;
+            else if (!(pq > 0.0))
+                st = SOLVE_BREAKDOWN;
+            const double alpha = st == SOLVE_RUNNING ? rz / pq : 0.0;
+            sh_st = st;
+            sh_alpha = (float)alpha;
+            if (blockIdx.x == 0) {
+                ctl->ustatus = st;
+                ctl->pq = pq;
+                ctl->alpha = alpha;
+            }
+        }
     }
-    if (st != SOLVE_RUNNING) return;
-    const float alpha = (float)(rz / pq);
+    __syncthreads();
+    if (sh_st != SOLVE_RUNNING) return;
+    const float alpha = sh_alpha;
     float rzn = 0.f, rr = 0.f;
     const long long N4 = f.N >> 2, stride = (long long)gridDim.x * blockDim.x;
     const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -147,11 +165,11 @@ __global__ void __launch_bounds__(256, 4) k_tmacg_update(const TmaCg f, SolveCtl
         f.x[n] = xn;
         f.r[n] = rn;
     }
-    double v[2] = {(double)rzn, (double)rr};
-    write_partial<2, OpSum>(v, f.part + kRZ, blockIdx.x);
+    float v[2] = {rzn, rr};
+    write_partial_f32<2>(v, f.part + kRZ, blockIdx.x);
 }
 
-__global__ void __launch_bounds__(256, 4) k_tmacg_direction(const TmaCg f, SolveCtl* __restrict__ ctl, int q) {
+__global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_direction(const TmaCg f, SolveCtl* __restrict__ ctl, int q) {
     const int st0 = ctl->status2[q];
     if (st0 != SOLVE_RUNNING) {  // pass a final status on to the other parity
         if (blockIdx.x == 0 && threadIdx.x == 0) ctl->status2[1 - q] = st0;
@@ -162,18 +180,32 @@ __global__ void __launch_bounds__(256, 4) k_tmacg_direction(const TmaCg f, Solve
         if (blockIdx.x == 0 && threadIdx.x == 0) ctl->status2[1 - q] = ctl->status = ust;
         return;
     }
-    double v[2];
-    reduce_partials<2, OpSum>(v, f.part + kRZ, f.upd_blocks);
-    const double rzn = v[0], rrn = v[1];
-    const double rz = ctl->rz2[q];
-    const double m = ctl->plain ? rrn : rzn;
-    int st = SOLVE_RUNNING;
-    if (!isfinite(rrn) || !isfinite(rzn))
-        st = SOLVE_NONFINITE;
-    else if (m <= ctl->tol2)
-        st = SOLVE_CONVERGED;
+    // warp 0 reduces the update's partials; lane 0 takes the decision for the block
+    __shared__ int sh_st;
+    __shared__ float sh_beta;
+    __shared__ double sh_v[3];
+    if (threadIdx.x < 32) {
+        double v[2];
+        warp0_reduce_partials<2>(v, f.part + kRZ, f.upd_blocks);
+        if (threadIdx.x == 0) {
+            const double rzn = v[0], rrn = v[1];
+            const double m = ctl->plain ? rrn : rzn;
+            int st = SOLVE_RUNNING;
+            if (!isfinite(rrn) || !isfinite(rzn))
+                st = SOLVE_NONFINITE;
+            else if (m <= ctl->tol2)
+                st = SOLVE_CONVERGED;
+            sh_st = st;
+            sh_beta = (float)(rzn / ctl->rz2[q]);
+            sh_v[0] = rzn;
+            sh_v[1] = rrn;
+            sh_v[2] = m;
+        }
+    }
+    __syncthreads();
+    int st = sh_st;
     if (st == SOLVE_RUNNING) {
-        const float beta = (float)(rzn / rz);
+        const float beta = sh_beta;
         const long long N4 = f.N >> 2, stride = (long long)gridDim.x * blockDim.x;
         const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         float4* p4 = reinterpret_cast<float4*>(f.p);
@@ -205,6 +237,7 @@ __global__ void __launch_bounds__(256, 4) k_tmacg_direction(const TmaCg f, Solve
         for (long long n = (N4 << 2) + t0; n < f.N; n += stride) f.p[n] = f.minv[n] * f.r[n] + beta * f.p[n];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const double rzn = sh_v[0], rrn = sh_v[1], m = sh_v[2], rz = ctl->rz2[q];
         ctl->iter += 1;
         ctl->rz_old = rz;
         ctl->rz = rzn;
@@ -235,7 +268,7 @@ __global__ void __launch_bounds__(256) k_partials_to_ctl(const double* __restric
 
 void launch_tmacg_start(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, double rtol, int ref_slot, int maxit,
                         int stall_limit) {
-    launch_kernel(k_tmacg_start, dim3(f.upd_blocks), dim3(256), c.stream, f, ctl, rtol, ref_slot, maxit, stall_limit);
+    launch_kernel(k_tmacg_start, dim3(f.upd_blocks), dim3(kCgThreads), c.stream, f, ctl, rtol, ref_slot, maxit, stall_limit);
 }
 
 double* tmacg_op_partials(const TmaCg& f) { return f.part + kPQ; }
@@ -243,12 +276,14 @@ double* tmacg_op_partials(const TmaCg& f) { return f.part + kPQ; }
 const int* tmacg_op_run(SolveCtl* ctl, int q) { return &ctl->status2[q]; }
 
 void launch_tmacg_update(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, int q) {
-    launch_kernel(k_tmacg_update, dim3(f.upd_blocks), dim3(256), c.stream, f, ctl, q);
+    launch_kernel(k_tmacg_update, dim3(f.upd_blocks), dim3(kCgThreads), c.stream, f, ctl, q);
 }
 
 void launch_tmacg_direction(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, int q) {
-    launch_kernel(k_tmacg_direction, dim3(f.upd_blocks), dim3(256), c.stream, f, ctl, q);
+    launch_kernel(k_tmacg_direction, dim3(f.upd_blocks), dim3(kCgThreads), c.stream, f, ctl, q);
 }
+
+int tmacg_blocks(const LaunchCfg& c) { return std::max(1, c.sm_count * (1024 / kCgThreads)); }
 
 void launch_partials_to_ctl(const LaunchCfg& c, const double* partials, int nslots, SolveCtl* ctl) {
     launch_kernel(k_partials_to_ctl, dim3(1), dim3(256), c.stream, partials, nslots, ctl);

@@ -113,6 +113,8 @@ void launch_tmacg_start(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, doubl
 // where the operator writes its partials, and the status word its launch of parity q checks
 double* tmacg_op_partials(const TmaCg& f);
 const int* tmacg_op_run(SolveCtl* ctl, int q);
+// grid of the start, update and direction kernels (TmaCg::upd_blocks)
+int tmacg_blocks(const LaunchCfg& c);
 void launch_tmacg_update(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, int q);
 void launch_tmacg_direction(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, int q);
 // ctl->pq = the sum of nslots block partials (fixed order)

@@ -369,8 +369,8 @@ __global__ void __launch_bounds__(32 * WX, WX <= 4 ? (12 + WX - 1) / WX : 2)
 
     // (x, A x): this block's partial; the next kernel reduces the partials of all blocks
     const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    double v[1] = {(double)dot};
-    write_partial<1, OpSum>(v, a.partials, bid);
+    float v[1] = {dot};
+    write_partial_f32<1>(v, a.partials, bid);
 }
 
 // P = k_xy dx dy dz / 48, Q = k_z dx dy / (16 dz) per element (padded layout), from the

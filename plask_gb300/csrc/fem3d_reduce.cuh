@@ -95,4 +95,58 @@ __device__ __forceinline__ void reduce_partials(double (&v)[NV], const double* p
     block_reduce<NV, Op>(v);
 }
 
+// The two helpers below keep FP64 arithmetic (a slow pipe on this GPU) to a few
+// instructions per block.
+
+// This block's partials of NV FP32 per-thread values: each warp sums its lanes in FP32 (a
+// fixed butterfly), thread 0 adds the warps' sums in FP64 in warp order and writes
+// partials[i * kMaxPartialBlocks + slot].
+template <int NV>
+__device__ __forceinline__ void write_partial_f32(float (&v)[NV], double* partials, int slot) {
+    __shared__ float sh[NV][32];
+    const int t = linear_tid(), lane = t & 31, warp = t >> 5, nw = (block_threads() + 31) >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+        for (int o = 16; o; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) sh[i][warp] = v[i];
+    }
+    __syncthreads();
+    if (t == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double a = 0.0;
+            for (int w = 0; w < nw; ++w) a += (double)sh[i][w];
+            partials[(size_t)i * kMaxPartialBlocks + slot] = a;
+        }
+    }
+}
+
+// Sum of partial slots [0, nslots) of NV values, computed by warp 0 alone (lane l takes
+// slots l, l + 32, ... in increasing order, then a fixed butterfly), so every block that
+// calls it gets the same bits.  The result is valid in warp 0 only; `scalar` (lane 0 of
+// warp 0) derives what the block needs from it, and the block synchronises before reading.
+template <int NV>
+__device__ __forceinline__ void warp0_reduce_partials(double (&v)[NV], const double* partials, int nslots) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        const double* src = partials + (size_t)i * kMaxPartialBlocks;
+        const int lane = threadIdx.x & 31;
+        double a = 0.0;
+        for (int s0 = lane; s0 < nslots; s0 += 4 * 32) {
+            double buf[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int s = s0 + 32 * u;
+                buf[u] = s < nslots ? __ldcg(src + s) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) a += buf[u];
+        }
+        for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        v[i] = a;
+    }
+}
+
 }  // namespace plgpu
