@@ -5,19 +5,22 @@
 // the input planes staged in shared memory by the Tensor Memory Accelerator instead of
 // per-thread global loads.
 //
-// Work layout.  A block spans the whole mesh along x: warp w, lane m owns node column
-// c = 32 w + m and computes the element column c - 1 to its left.  Each thread covers RR
-// consecutive rows along y and marches a chunk of z-planes.  For every plane the block
-// holds in shared memory, written by cp.async.bulk.tensor:
-//   - the node tile of the input x: columns -4 .. 32 WX - 1, rows j0 - 1 .. j0 + RR;
+// Work layout.  A block spans the whole mesh along x: warp (wx, wy), lane m owns the node
+// columns c0 = 64 wx + 2 m and c0 + 1 and computes the two element columns to their left,
+// A = c0 - 1 and B = c0, with packed two-wide FP32 instructions (add/mul/fma.f32x2): the two
+// elements take the same arithmetic on different data.  Each thread covers RR consecutive
+// rows along y (warp row wy of the block) and marches a chunk of z-planes.  For every plane
+// the block holds in shared memory, written by cp.async.bulk.tensor, per pair of warps along
+// x (a region of 128 columns):
+//   - the node tile of the input x: columns 128 r - 4 .. 128 r + 127, rows j0 - 1 .. j0 + RR WY;
 //   - the element tile(s) of the pre-scaled conductances P (and Q when anisotropic) of the
-//     element layer above the plane: columns -4 .. 32 WX - 1, rows j0 - 1 .. j0 + RR - 1.
-// The tiles start at column -4 so that the copy's first x coordinate is 16-byte aligned;
-// rows, columns and planes outside the mesh arrive as zeros (the copy's out-of-bounds fill),
-// so elements outside the mesh contribute nothing and no load carries a bounds test.
-// NS stages form a ring: stage u % NS holds plane kstart + u; an mbarrier per stage counts
-// the bytes of its copies.  One block-wide barrier per plane releases the stage the block
-// has finished with, and thread 0 then issues the copies of the plane NS ahead.
+//     element layer above the plane, rows j0 - 1 .. j0 + RR WY - 1.
+// The tiles start at column 128 r - 4 so that the copy's first x coordinate is 16-byte
+// aligned; rows, columns and planes outside the mesh arrive as zeros (the copy's
+// out-of-bounds fill), so elements outside the mesh contribute nothing and no load carries
+// a bounds test.  NS stages form a ring: stage u % NS holds plane kstart + u; an mbarrier per
+// stage counts the bytes of its copies.  One block-wide barrier per plane releases the stage
+// the block has finished with, and thread 0 then issues the copies of the plane NS ahead.
 //
 // Element algebra (derivation in fem3d_operator.cu).  With the conductances pre-scaled per
 // element by k_tma_coef,
@@ -26,9 +29,10 @@
 //     l100 = 3X, l010 = 3Y, l001 = 3Z, l110 = X + Y, l101 = X + Z, l011 = Y + Z,
 //     l111 = (X + Y + Z) / 3.
 // Contributions to the two x-corners of an element are accumulated as (sum, difference)
-// pairs: the element's right corner (this lane's node) gets S + D, its left corner (the
-// previous lane's node) S - D, sent by one shuffle per output row; the last lane of a warp
-// takes it from the next warp through shared memory after the plane's barrier.
+// pairs: an element's right corner gets S + D, its left corner S - D.  Node c0 takes A's
+// right and B's left corner (both in the lane); node c0 + 1 takes B's right corner and the
+// left corner of the next lane's A, sent by one shuffle per output row; the last lane of a
+// warp takes it from the next warp along x through shared memory after the plane's barrier.
 //
 // Convective surface rows (therm3d.cpp:250-259: the face stiffness, kept as a small CSR
 // operator) are added in the same pass: a plane that holds surface rows has a node -> row
@@ -60,7 +64,7 @@ namespace {
 //   PLGPU_TMA_STAGES  planes in the shared-memory ring
 //   PLGPU_TMA_BLOCKS  resident blocks per SM the z-chunks are sized for (0: the cost model)
 #ifndef PLGPU_TMA_ROWS
-#define PLGPU_TMA_ROWS 8
+#define PLGPU_TMA_ROWS 2
 #endif
 #ifndef PLGPU_TMA_STAGES
 #define PLGPU_TMA_STAGES 4
@@ -68,26 +72,43 @@ namespace {
 #ifndef PLGPU_TMA_BLOCKS
 #define PLGPU_TMA_BLOCKS 0
 #endif
+//   PLGPU_TMA_MINB    blocks per SM the register budget is sized for
+#ifndef PLGPU_TMA_MINB
+#define PLGPU_TMA_MINB 5
+#endif
 constexpr int kTmaRows = PLGPU_TMA_ROWS;
 constexpr int kTmaStages = PLGPU_TMA_STAGES;
-constexpr int kTmaMaxWarpsX = 7;  // box width 32 * 7 + 4 = 228 <= 256
+constexpr int kTmaMaxWarpsX = 4;  // 64 columns per warp: meshes up to 256 nodes along x
 constexpr unsigned kSpinLimit = 1u << 22;
 
-__host__ __device__ constexpr int tma_pitch(int wx) { return 32 * wx + 4; }
+// warps along y of a block with wx warps along x (128 threads, 96 for wx = 3)
+__host__ __device__ constexpr int tma_wy(int wx) { return wx == 1 ? 4 : wx == 2 ? 2 : 1; }
+// columns of one copy: a region of 128 columns (64 for one warp) plus the 4 to its left
+__host__ __device__ constexpr int tma_box(int wx) { return wx == 1 ? 68 : 132; }
+__host__ __device__ constexpr int tma_regions(int wx) { return (wx + 1) / 2; }
 __host__ __device__ constexpr int align128(int b) { return (b + 127) & ~127; }
-__host__ __device__ constexpr int tma_x_bytes(int wx, int rr) { return align128((rr + 2) * tma_pitch(wx) * 4); }
-__host__ __device__ constexpr int tma_k_bytes(int wx, int rr) { return align128((rr + 1) * tma_pitch(wx) * 4); }
+__host__ __device__ constexpr int tma_x_rows(int wx, int rr) { return rr * tma_wy(wx) + 2; }
+__host__ __device__ constexpr int tma_k_rows(int wx, int rr) { return rr * tma_wy(wx) + 1; }
+__host__ __device__ constexpr int tma_x_tile(int wx, int rr) { return align128(tma_x_rows(wx, rr) * tma_box(wx) * 4); }
+__host__ __device__ constexpr int tma_k_tile(int wx, int rr) { return align128(tma_k_rows(wx, rr) * tma_box(wx) * 4); }
 __host__ __device__ constexpr int tma_stage_bytes(int wx, int rr, bool aniso) {
-    return tma_x_bytes(wx, rr) + tma_k_bytes(wx, rr) * (aniso ? 2 : 1);
+    return tma_regions(wx) * (tma_x_tile(wx, rr) + tma_k_tile(wx, rr) * (aniso ? 2 : 1));
 }
 // the bytes the copies of one stage deliver (the boxes, without the alignment padding)
 __host__ __device__ constexpr int tma_tx_bytes(int wx, int rr, bool aniso) {
-    return (rr + 2) * tma_pitch(wx) * 4 + (rr + 1) * tma_pitch(wx) * 4 * (aniso ? 2 : 1);
+    return tma_regions(wx) * tma_box(wx) * 4 * (tma_x_rows(wx, rr) + tma_k_rows(wx, rr) * (aniso ? 2 : 1));
 }
 __host__ __device__ constexpr int tma_smem_bytes(int wx, int rr, bool aniso, int ns) {
     // stages, then ns mbarriers, then the double-buffered exchange rows, plus 128 B to align
-    return ns * tma_stage_bytes(wx, rr, aniso) + ns * 8 + 2 * wx * rr * 4 + 128;
+    return ns * tma_stage_bytes(wx, rr, aniso) + ns * 8 + 2 * tma_wy(wx) * wx * rr * 4 + 128;
 }
+
+// packed two-wide FP32 arithmetic
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -139,36 +160,38 @@ struct TmaArgs {
     const float* az3;        // per element layer: 3 / dz^2 (isotropic only; 0 outside)
 };
 
-// (sum, difference) y-stage of one element row on one plane
+// (sum, difference) y-stage of one element row on one plane, for the lane's elements (A, B)
 template <int RR>
 struct YStage {
-    float ss[RR + 1], sd[RR + 1], ds[RR + 1], dd[RR + 1];
+    float2 ss[RR + 1], sd[RR + 1], ds[RR + 1], dd[RR + 1];
 };
 template <int RR>
 struct RowAcc {
-    float s[RR], d[RR];
+    float2 s[RR], d[RR];
 };
 
-// registers for at least 12 warps per SM up to 4 warps per block (at most 170 per thread),
-// for two blocks above
+// registers for PLGPU_TMA_MINB blocks per SM
 template <int WX, int RR, bool ANISO, int NS>
-__global__ void __launch_bounds__(32 * WX, WX <= 4 ? (12 + WX - 1) / WX : 2)
+__global__ void __launch_bounds__(32 * WX * tma_wy(WX), PLGPU_TMA_MINB)
     k_apply_tma(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap mp,
                 const __grid_constant__ CUtensorMap mq, const TmaArgs a) {
     if (*a.run != SOLVE_RUNNING) return;
-    constexpr int XW = tma_pitch(WX);
-    constexpr int XB = tma_x_bytes(WX, RR), KB = tma_k_bytes(WX, RR), SB = tma_stage_bytes(WX, RR, ANISO);
+    constexpr int WY = tma_wy(WX), NR = tma_regions(WX), BW = tma_box(WX);
+    constexpr int XT = tma_x_tile(WX, RR), KT = tma_k_tile(WX, RR), SB = tma_stage_bytes(WX, RR, ANISO);
     constexpr uint32_t TX = tma_tx_bytes(WX, RR, ANISO);
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = smem_raw + ((128 - (smem_u32(smem_raw) & 127)) & 127);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + NS * SB);
-    float* xch = reinterpret_cast<float*>(smem + NS * SB + NS * 8);  // [2][WX][RR]
+    float* xch = reinterpret_cast<float*>(smem + NS * SB + NS * 8);  // [2][WY][WX][RR]
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
-    const int c = 32 * warp + lane;  // node column
-    const int col = c + 4;           // its column in the tiles
-    const int j0 = blockIdx.y * RR;
+    const int wx = warp % WX, wy = warp / WX;
+    const int c0 = 64 * wx + 2 * lane;       // the lane's node columns c0, c0 + 1
+    const int reg = wx >> 1;                 // its region of 128 columns
+    const int cb = c0 + 4 - 128 * reg;       // column of c0 in the region's tiles (even)
+    const int j0 = blockIdx.y * (RR * WY);
+    const int jw = j0 + wy * RR;             // first output row of the warp
     const int k0 = blockIdx.z * a.zchunk;
     const int k1 = min(k0 + a.zchunk, a.n2);
     const int kstart = max(k0 - 1, 0);
@@ -178,14 +201,25 @@ __global__ void __launch_bounds__(32 * WX, WX <= 4 ? (12 + WX - 1) / WX : 2)
 
     auto stage_ptr = [&](int u) { return smem + (u % NS) * SB; };
     auto bar_of = [&](int u) { return smem_u32(&bars[u % NS]); };
+    // this warp's x rows (global rows jw - 1 ..) and element rows of the stage
+    auto xrows = [&](int u) { return reinterpret_cast<const float*>(stage_ptr(u) + reg * XT) + wy * RR * BW; };
+    auto prows = [&](int u) {
+        return reinterpret_cast<const float*>(stage_ptr(u) + NR * XT + reg * KT) + wy * RR * BW;
+    };
+    auto qrows = [&](int u) {
+        return reinterpret_cast<const float*>(stage_ptr(u) + NR * XT + NR * KT + reg * KT) + wy * RR * BW;
+    };
     auto issue = [&](int u) {  // copies of plane kstart + u into stage u % NS
         const uint32_t bar = bar_of(u);
-        const uint32_t dst = smem_u32(stage_ptr(u));
+        const uint32_t base = smem_u32(stage_ptr(u));
         const int p = kstart + u;
         mbar_expect_tx(bar, TX);
-        tma_load_3d(dst, &mx, bar, -4, j0 - 1, p);
-        tma_load_3d(dst + XB, &mp, bar, -4, j0 - 1, p);
-        if (ANISO) tma_load_3d(dst + XB + KB, &mq, bar, -4, j0 - 1, p);
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+            tma_load_3d(base + r * XT, &mx, bar, 128 * r - 4, j0 - 1, p);
+            tma_load_3d(base + NR * XT + r * KT, &mp, bar, 128 * r - 4, j0 - 1, p);
+            if (ANISO) tma_load_3d(base + NR * XT + NR * KT + r * KT, &mq, bar, 128 * r - 4, j0 - 1, p);
+        }
     };
 
     if (tid == 0) {
@@ -195,11 +229,11 @@ __global__ void __launch_bounds__(32 * WX, WX <= 4 ? (12 + WX - 1) / WX : 2)
     }
     __syncthreads();
 
-    // per-thread geometry: 1/dx^2 of the lane's element column, 1/dy^2 of its element rows
-    const float axc = a.ax[c];
+    // per-thread geometry: 1/dx^2 of the lane's element columns, 1/dy^2 of its element rows
+    const float2 AX = *reinterpret_cast<const float2*>(a.ax + c0);
     float ay[RR + 1];
 #pragma unroll
-    for (int e = 0; e <= RR; ++e) ay[e] = a.ay[j0 + e];  // element row j0 - 1 + e
+    for (int e = 0; e <= RR; ++e) ay[e] = a.ay[jw + e];  // element row jw - 1 + e
 
     bool failed = false;
     // bookkeeping for the bounded drain after a failed wait (the same in every thread):
@@ -209,27 +243,30 @@ __global__ void __launch_bounds__(32 * WX, WX <= 4 ? (12 + WX - 1) / WX : 2)
 
     YStage<RR> ya, yb;
     RowAcc<RR> acca, accb;
-    float xra[RR], xrb[RR];
-    float dot = 0.f;
+    float2 xra[RR], xrb[RR];
+    float2 dot = make_float2(0.f, 0.f);
 
-    // x-stage and y-stage of the plane in stage u; raw x of the output rows
-    auto plane_stage = [&](int u, YStage<RR>& ys, float(&xr)[RR]) {
-        const float* xs = reinterpret_cast<const float*>(stage_ptr(u));
-        float sp, dp;
+    // x-stage and y-stage of the plane in stage u; raw x of the output nodes
+    auto plane_stage = [&](int u, YStage<RR>& ys, float2(&xr)[RR]) {
+        const float* xs = xrows(u);
+        float2 sp, dp;
         {
-            const float x0 = xs[col - 1], x1 = xs[col];
-            sp = x0 + x1;
-            dp = x1 - x0;
+            const float2 xr2 = *reinterpret_cast<const float2*>(xs + cb);
+            const float2 xl2 = make_float2(xs[cb - 1], xr2.x);
+            sp = add2(xl2, xr2);
+            dp = sub2(xr2, xl2);
         }
 #pragma unroll
         for (int e = 0; e <= RR; ++e) {
-            const float x0 = xs[(e + 1) * XW + col - 1], x1 = xs[(e + 1) * XW + col];
-            const float s = x0 + x1, d = x1 - x0;
-            if (e < RR) xr[e] = x1;
-            ys.ss[e] = sp + s;
-            ys.sd[e] = s - sp;
-            ys.ds[e] = dp + d;
-            ys.dd[e] = d - dp;
+            const float* row = xs + (e + 1) * BW;
+            const float2 xr2 = *reinterpret_cast<const float2*>(row + cb);
+            const float2 xl2 = make_float2(row[cb - 1], xr2.x);
+            const float2 s = add2(xl2, xr2), d = sub2(xr2, xl2);
+            if (e < RR) xr[e] = xr2;
+            ys.ss[e] = add2(sp, s);
+            ys.sd[e] = sub2(s, sp);
+            ys.ds[e] = add2(dp, d);
+            ys.dd[e] = sub2(d, dp);
             sp = s;
             dp = d;
         }
@@ -237,7 +274,7 @@ __global__ void __launch_bounds__(32 * WX, WX <= 4 ? (12 + WX - 1) / WX : 2)
 
     // one element layer u (planes kstart + u and kstart + u + 1): lo = plane u, hi = plane u + 1
     auto layer = [&](int u, const YStage<RR>& lo, YStage<RR>& hi, RowAcc<RR>& accLo, RowAcc<RR>& accHi,
-                     const float(&xrLo)[RR], float(&xrHi)[RR]) {
+                     const float2(&xrLo)[RR], float2(&xrHi)[RR]) {
         // plane u + 1 landed?
         bool ok = true;
         if (u + 1 >= waited) {
@@ -246,52 +283,53 @@ __global__ void __launch_bounds__(32 * WX, WX <= 4 ? (12 + WX - 1) / WX : 2)
         }
         if (ok) {
             plane_stage(u + 1, hi, xrHi);
-            const float* kp = reinterpret_cast<const float*>(stage_ptr(u) + XB);
-            const float* kq = reinterpret_cast<const float*>(stage_ptr(u) + XB + KB);
+            const float* kp = prows(u);
+            const float* kq = qrows(u);
             const int k = kstart + u;
-            const float az3 = ANISO ? 0.f : a.az3[k];
+            const float2 az3 = splat(ANISO ? 0.f : a.az3[k]);
+            const float2 third = splat(1.f / 3.f), three = splat(3.f);
 #pragma unroll
             for (int e = 0; e <= RR; ++e) {
-                const float P = kp[e * XW + col - 1];
-                const float X = P * axc, Y = P * ay[e];
-                float Zt, l001;
+                const float2 P = make_float2(kp[e * BW + cb - 1], kp[e * BW + cb]);
+                const float2 X = mul2(P, AX), Y = mul2(P, splat(ay[e]));
+                float2 l001, Zt;
                 if (ANISO) {
-                    l001 = kq[e * XW + col - 1];
-                    Zt = l001 * (1.f / 3.f);
+                    l001 = make_float2(kq[e * BW + cb - 1], kq[e * BW + cb]);
+                    Zt = mul2(l001, third);
                 } else {
-                    l001 = P * az3;
-                    Zt = l001 * (1.f / 3.f);
+                    l001 = mul2(P, az3);
+                    Zt = mul2(l001, third);
                 }
-                const float l100 = 3.f * X, l010 = 3.f * Y;
-                const float l110 = X + Y, l101 = X + Zt, l011 = Y + Zt;
-                const float l111 = (l110 + Zt) * (1.f / 3.f);
-                const float m001 = (hi.ss[e] - lo.ss[e]) * l001;
-                const float m010 = (lo.sd[e] + hi.sd[e]) * l010, m011 = (hi.sd[e] - lo.sd[e]) * l011;
-                const float m100 = (lo.ds[e] + hi.ds[e]) * l100, m101 = (hi.ds[e] - lo.ds[e]) * l101;
-                const float m110 = (lo.dd[e] + hi.dd[e]) * l110, m111 = (hi.dd[e] - lo.dd[e]) * l111;
-                const float tsd0 = m010 - m011, tsd1 = m010 + m011;
-                const float tds0 = m100 - m101, tds1 = m100 + m101;
-                const float tdd0 = m110 - m111, tdd1 = m110 + m111;
-                // element row e spans tile node rows e and e + 1 = output rows e - 1 and e
+                const float2 l100 = mul2(X, three), l010 = mul2(Y, three);
+                const float2 l110 = add2(X, Y), l101 = add2(X, Zt), l011 = add2(Y, Zt);
+                const float2 l111 = mul2(add2(l110, Zt), third);
+                const float2 m001 = mul2(sub2(hi.ss[e], lo.ss[e]), l001);
+                const float2 m010 = mul2(add2(lo.sd[e], hi.sd[e]), l010), m011 = mul2(sub2(hi.sd[e], lo.sd[e]), l011);
+                const float2 m100 = mul2(add2(lo.ds[e], hi.ds[e]), l100), m101 = mul2(sub2(hi.ds[e], lo.ds[e]), l101);
+                const float2 m110 = mul2(add2(lo.dd[e], hi.dd[e]), l110), m111 = mul2(sub2(hi.dd[e], lo.dd[e]), l111);
+                const float2 tsd0 = sub2(m010, m011), tsd1 = add2(m010, m011);
+                const float2 tds0 = sub2(m100, m101), tds1 = add2(m100, m101);
+                const float2 tdd0 = sub2(m110, m111), tdd1 = add2(m110, m111);
+                // element row e spans the warp's node rows e and e + 1 = output rows e - 1 and e
                 if (e >= 1) {
-                    accLo.s[e - 1] += -m001 - tsd0;
-                    accLo.d[e - 1] += tds0 - tdd0;
-                    accHi.s[e - 1] += m001 - tsd1;
-                    accHi.d[e - 1] += tds1 - tdd1;
+                    accLo.s[e - 1] = sub2(accLo.s[e - 1], add2(m001, tsd0));
+                    accLo.d[e - 1] = add2(accLo.d[e - 1], sub2(tds0, tdd0));
+                    accHi.s[e - 1] = add2(accHi.s[e - 1], sub2(m001, tsd1));
+                    accHi.d[e - 1] = add2(accHi.d[e - 1], sub2(tds1, tdd1));
                 }
                 if (e < RR) {
-                    accLo.s[e] += tsd0 - m001;
-                    accLo.d[e] += tds0 + tdd0;
-                    accHi.s[e] += m001 + tsd1;
-                    accHi.d[e] += tds1 + tdd1;
+                    accLo.s[e] = add2(accLo.s[e], sub2(tsd0, m001));
+                    accLo.d[e] = add2(accLo.d[e], add2(tds0, tdd0));
+                    accHi.s[e] = add2(accHi.s[e], add2(m001, tsd1));
+                    accHi.d[e] = add2(accHi.d[e], add2(tds1, tdd1));
                 }
             }
         }
         // the left-corner sums of this warp's first lane go to the previous warp's last lane
-        float* xb = xch + (u & 1) * WX * RR;
+        float* xb = xch + ((u & 1) * WY + wy) * WX * RR;
         if (lane == 0) {
 #pragma unroll
-            for (int r = 0; r < RR; ++r) xb[warp * RR + r] = accLo.s[r] - accLo.d[r];
+            for (int r = 0; r < RR; ++r) xb[wx * RR + r] = accLo.s[r].x - accLo.d[r].x;
         }
         if (__syncthreads_or(ok ? 0 : 1)) {
             failed = true;
@@ -310,27 +348,36 @@ __global__ void __launch_bounds__(32 * WX, WX <= 4 ? (12 + WX - 1) / WX : 2)
             const long long pb = s2 * k;
 #pragma unroll
             for (int r = 0; r < RR; ++r) {
-                float recv = __shfl_down_sync(0xffffffffu, accLo.s[r] - accLo.d[r], 1);
-                if (lane == 31) recv = (warp + 1 < WX) ? xb[(warp + 1) * RR + r] : 0.f;
-                float out = accLo.s[r] + accLo.d[r] + recv;
-                const int row = j0 + r;
-                if (c < a.n0 && row < a.n1) {
-                    const long long n = pb + (long long)row * a.n0 + c;
+                const float2 right = add2(accLo.s[r], accLo.d[r]), left = sub2(accLo.s[r], accLo.d[r]);
+                float recv = __shfl_down_sync(0xffffffffu, left.x, 1);
+                if (lane == 31) recv = (wx + 1 < WX) ? xb[(wx + 1) * RR + r] : 0.f;
+                float2 out = make_float2(right.x + left.y, right.y + recv);
+                const int row = jw + r;
+                if (c0 < a.n0 && row < a.n1) {  // n0 is even: c0 + 1 < n0 too
+                    const long long n = pb + (long long)row * a.n0 + c0;
                     if (sp != 0) {
-                        const int sr = a.s.map[(long long)(sp - 1) * s2 + (long long)row * a.n0 + c];
-                        if (sr >= 0) {
-                            float acc = 0.f;
-                            for (int q = a.s.ptr[sr]; q < a.s.ptr[sr + 1]; ++q) acc += a.s.val[q] * a.x[a.s.col[q]];
-                            out += acc;
+                        const long long mb = (long long)(sp - 1) * s2 + (long long)row * a.n0 + c0;
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const int sr = a.s.map[mb + h];
+                            if (sr >= 0) {
+                                float acc = 0.f;
+                                for (int q = a.s.ptr[sr]; q < a.s.ptr[sr + 1]; ++q)
+                                    acc += a.s.val[q] * a.x[a.s.col[q]];
+                                if (h == 0)
+                                    out.x += acc;
+                                else
+                                    out.y += acc;
+                            }
                         }
                     }
-                    dot += xrLo[r] * out;
-                    a.y[n] = out;
+                    dot = fma2(xrLo[r], out, dot);
+                    *reinterpret_cast<float2*>(a.y + n) = out;
                 }
             }
         }
 #pragma unroll
-        for (int r = 0; r < RR; ++r) accLo.s[r] = accLo.d[r] = 0.f;
+        for (int r = 0; r < RR; ++r) accLo.s[r] = accLo.d[r] = make_float2(0.f, 0.f);
     };
 
     // prologue: plane 0 of the chunk
@@ -343,7 +390,7 @@ __global__ void __launch_bounds__(32 * WX, WX <= 4 ? (12 + WX - 1) / WX : 2)
         failed = __syncthreads_or(ok ? 0 : 1) != 0;
     }
 #pragma unroll
-    for (int r = 0; r < RR; ++r) acca.s[r] = acca.d[r] = accb.s[r] = accb.d[r] = 0.f;
+    for (int r = 0; r < RR; ++r) acca.s[r] = acca.d[r] = accb.s[r] = accb.d[r] = make_float2(0.f, 0.f);
 
     int u = 0;
     if (!failed) {
@@ -369,7 +416,7 @@ __global__ void __launch_bounds__(32 * WX, WX <= 4 ? (12 + WX - 1) / WX : 2)
 
     // (x, A x): this block's partial; the next kernel reduces the partials of all blocks
     const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    float v[1] = {dot};
+    float v[1] = {dot.x + dot.y};
     write_partial_f32<1>(v, a.partials, bid);
 }
 
@@ -436,10 +483,7 @@ void* kernel_for(int wx, bool aniso) {
         case 1: return aniso ? kernel_of<1, true>() : kernel_of<1, false>();
         case 2: return aniso ? kernel_of<2, true>() : kernel_of<2, false>();
         case 3: return aniso ? kernel_of<3, true>() : kernel_of<3, false>();
-        case 4: return aniso ? kernel_of<4, true>() : kernel_of<4, false>();
-        case 5: return aniso ? kernel_of<5, true>() : kernel_of<5, false>();
-        case 6: return aniso ? kernel_of<6, true>() : kernel_of<6, false>();
-        default: return aniso ? kernel_of<7, true>() : kernel_of<7, false>();
+        default: return aniso ? kernel_of<4, true>() : kernel_of<4, false>();
     }
 }
 
@@ -447,7 +491,7 @@ void* kernel_for(int wx, bool aniso) {
 
 struct TmaOperator {
     CUtensorMap mx, mp, mq;
-    int n0 = 0, n1 = 0, n2 = 0, wx = 0;
+    int n0 = 0, n1 = 0, n2 = 0, wx = 0, threads = 0;
     bool aniso = false;
     const float* x = nullptr;
     float* P = nullptr;
@@ -466,7 +510,7 @@ struct TmaOperator {
 };
 
 bool tma_operator_supported(int n0, int n1, int n2) {
-    return n0 >= 2 && n0 <= 32 * kTmaMaxWarpsX && (n0 % 4) == 0 && n1 >= 2 && n2 >= 2 && encode_fn() != nullptr;
+    return n0 >= 2 && n0 <= 64 * kTmaMaxWarpsX && (n0 % 4) == 0 && n1 >= 2 && n2 >= 2 && encode_fn() != nullptr;
 }
 
 TmaOperator* tma_operator_create(const LaunchCfg& c, const GridT<double>& g, const std::vector<double>& hx,
@@ -478,19 +522,20 @@ TmaOperator* tma_operator_create(const LaunchCfg& c, const GridT<double>& g, con
     t->n0 = n0;
     t->n1 = n1;
     t->n2 = n2;
-    t->wx = (n0 + 31) / 32;
+    t->wx = (n0 + 63) / 64;
+    t->threads = 32 * t->wx * tma_wy(t->wx);
     t->aniso = aniso;
     t->x = x;
     t->P = P;
     t->Q = Q;
-    const int pitch = tma_pitch(t->wx);
-    if (!encode_3d(&t->mx, x, n0, n1, n2, pitch, kTmaRows + 2)) return nullptr;
-    if (!encode_3d(&t->mp, P, n0, n1, n2, pitch, kTmaRows + 1)) return nullptr;
-    if (!encode_3d(&t->mq, aniso ? Q : P, n0, n1, n2, pitch, kTmaRows + 1)) return nullptr;
+    const int box = tma_box(t->wx), rows = kTmaRows * tma_wy(t->wx);
+    if (!encode_3d(&t->mx, x, n0, n1, n2, box, rows + 2)) return nullptr;
+    if (!encode_3d(&t->mp, P, n0, n1, n2, box, rows + 1)) return nullptr;
+    if (!encode_3d(&t->mq, aniso ? Q : P, n0, n1, n2, box, rows + 1)) return nullptr;
 
     // geometry factors (host-computed from the FP64 axes)
-    const int gy = (n1 + kTmaRows - 1) / kTmaRows;
-    std::vector<float> ax((size_t)32 * t->wx, 0.f), ay((size_t)gy * kTmaRows + 2, 0.f), az((size_t)n2, 0.f);
+    const int gy = (n1 + rows - 1) / rows;
+    std::vector<float> ax((size_t)64 * t->wx, 0.f), ay((size_t)gy * rows + 2, 0.f), az((size_t)n2, 0.f);
     for (int cc = 1; cc < n0; ++cc) ax[cc] = (float)(1.0 / (hx[cc - 1] * hx[cc - 1]));
     for (int j = 0; j < n1 - 1; ++j) ay[(size_t)j + 1] = (float)(1.0 / (hy[j] * hy[j]));
     for (int k = 0; k < n2 - 1; ++k) az[k] = (float)(3.0 / (hz[k] * hz[k]));
@@ -507,7 +552,7 @@ TmaOperator* tma_operator_create(const LaunchCfg& c, const GridT<double>& g, con
     void* k = kernel_for(t->wx, aniso);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, t->smem) != cudaSuccess) return nullptr;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 32 * t->wx, t->smem) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, t->threads, t->smem) != cudaSuccess || per_sm < 1)
         return nullptr;
     const int sms = std::max(1, c.sm_count / std::max(1, c.op_share));
     if (PLGPU_TMA_BLOCKS > 0) per_sm = std::min(per_sm, PLGPU_TMA_BLOCKS);
@@ -550,7 +595,8 @@ void launch_tma_coef(const LaunchCfg& c, const TmaOperator* t, const GridT<doubl
 
 template <int WX, bool ANISO>
 static void launch_tma_one(const LaunchCfg& c, const TmaOperator* t, const TmaArgs& a) {
-    k_apply_tma<WX, kTmaRows, ANISO, kTmaStages><<<t->grid, 32 * WX, t->smem, c.stream>>>(t->mx, t->mp, t->mq, a);
+    k_apply_tma<WX, kTmaRows, ANISO, kTmaStages><<<t->grid, 32 * WX * tma_wy(WX), t->smem, c.stream>>>(t->mx, t->mp,
+                                                                                                   t->mq, a);
     count_launch();
 }
 
@@ -569,9 +615,6 @@ void launch_operator_tma(const LaunchCfg& c, const TmaOperator* t, float* y, dou
         PLGPU_TMA_CASE(2)
         PLGPU_TMA_CASE(3)
         PLGPU_TMA_CASE(4)
-        PLGPU_TMA_CASE(5)
-        PLGPU_TMA_CASE(6)
-        PLGPU_TMA_CASE(7)
         default: break;
     }
 #undef PLGPU_TMA_CASE
