@@ -15,8 +15,16 @@ e2e      the same through the C ABI with pinned host buffers: upload of the
 plain    the plain FP64 Jacobi-PCG solver on the same case, for comparison;
 roofline the operator kernel (matrix-free stiffness apply, FP32) timed with
          CUDA events over 20 launches with L2 flushed before each launch;
+parity   max |dT| of the final field against the reference's own NSPCG solution
+         (zeta 1e-12, tests/golden/static3d_layered_c1_128x128x200_nspcg.npz) at
+         16384 seeded nodes, the plane and the vertical line through the hottest
+         node, and the FP64 relative residuals of both;
 cpu_baseline  the reference's default iterative algorithm (IC + CG) restated
-         on the host (oracle), timed on a bounded sample and extrapolated.
+         on the host (oracle), timed on a bounded sample of the 128x128x200 case
+         and extrapolated with the reference NSPCG's own iteration counts; beside
+         it the 40x40x60 configuration solved in full on the host, with the band
+         Cholesky (all cores) and with IC-CG (one core), and the extrapolation
+         model's prediction for that solve.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
     python bench.py --workload sweep [--sweep-count 256]   # batched sweep line (not the default)
@@ -197,27 +205,29 @@ def baseline_problem(size):
     return O.from_structure(S.layered_c1(n=size), empty_elements="include")
 
 
+def c1_iteration_record(size):
+    """(outer loops, IC-CG iterations, note) of the reference's iterative solve at zeta 1e-12."""
+    char_path = ROOT / "oracle" / "c1_iterations.json"
+    if char_path.exists() and tuple(size) == (128, 128, 200):
+        ch = json.loads(char_path.read_text())
+        # the reference's own NSPCG first (5641 iterations); the IC(0) port converges in fewer
+        key = next((k for k in ("nspcg:1e-12", "port:1e-12") if k in ch), None)
+        if key:
+            lp = ch[key]["loops"]
+            iters = sum(x["iterations"] for x in lp)
+            return len(lp), iters, (f"{len(lp)} outer loops and {iters} IC-CG iterations in total at zeta 1e-12 "
+                                    f"({key}, oracle/c1_iterations.json)")
+    return 5, 5 * 1000, "assumed 5 outer loops of 1000 iterations (reference maxit)"
+
+
 def cpu_baseline(size, cg_iterations, prob=None):
     from oracle import baseline as B
 
     if prob is None:
         prob = baseline_problem(size)
     r = B.sample(prob, cg_iterations=cg_iterations)
-    char_path = ROOT / "oracle" / "c1_iterations.json"
-    loops, iters, note = None, None, ""
-    if char_path.exists() and tuple(size) == (128, 128, 200):
-        ch = json.loads(char_path.read_text())
-        key = next((k for k in ("port:1e-12", "nspcg:1e-12") if k in ch), None)
-        if key:
-            lp = ch[key]["loops"]
-            loops = len(lp)
-            iters = sum(x["iterations"] for x in lp)
-            note = f"{loops} outer loops and {iters} IC-CG iterations in total at zeta 1e-12 ({key}, oracle/c1_iterations.json)"
-    if loops is None:
-        loops, iters = 5, 5 * 1000
-        note = "assumed 5 outer loops of 1000 iterations (reference maxit)"
-    refactors = (loops + 9) // 10
-    est = loops * r["assembly_s"] + refactors * r["factor_s"] + iters * r["per_iteration_s"]
+    loops, iters, note = c1_iteration_record(size)
+    est = B.predict(r, loops, iters)
     return {
         "value": 1.0 / est,
         "unit": UNIT,
@@ -229,6 +239,66 @@ def cpu_baseline(size, cg_iterations, prob=None):
                    f"to {est:.0f} s per solve (NSPCG is single-threaded in the reference)"),
         "seconds_per_solve": est,
     }
+
+
+def cpu_c0_measured():
+    """The 40x40x60 configuration (layered_c0, seed 1) solved in full on the host, both reference
+    algorithms, with the extrapolation model's prediction of the iterative solve beside it."""
+    import numpy as np
+
+    from oracle import baseline as B
+    from oracle import fem3d as O
+    from plask_gb300 import structures as S
+
+    s = S.layered_c0(seed=1)
+    p_it = O.from_structure(s, empty_elements="include")
+    it = B.full_solve_iterative(p_it)
+    sm = B.sample(p_it, cg_iterations=50)
+    pred = B.predict(sm, it["loops"], it["iterations"])
+    ch = B.full_solve_cholesky(O.from_structure(s))
+    return {
+        "workload": "layered-40x40x60 (seed 1), full outer loop to maxerr 0.05 K",
+        "cpu": _cpu_model(), "nproc": os.cpu_count(),
+        "measured_c0_s": {"cholesky": ch["wall_s"], "iterative": it["wall_s"]},
+        "cores": {"cholesky": os.cpu_count(), "iterative": 1},
+        "iterative_loops": it["loops"], "iterative_iterations": it["iterations"],
+        "cholesky_loops": ch["loops"],
+        "predicted_c0_s": pred,
+        "prediction_over_measured": pred / it["wall_s"],
+        "max_dT_iterative_vs_cholesky_K": float(np.max(np.abs(it["T"] - ch["T"]))),
+    }
+
+
+def _cpu_model():
+    try:
+        for line in pathlib.Path("/proc/cpuinfo").read_text().splitlines():
+            low = line.lower()
+            if low.startswith("model name") or low.startswith("cpu part"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
+def reference_parity(T, rel_residual):
+    """max |dT| of a canonical (n2, n1, n0) field against the reference NSPCG golden field."""
+    import numpy as np
+
+    path = ROOT / "tests" / "golden" / "static3d_layered_c1_128x128x200_nspcg.npz"
+    if not path.exists() or T.shape != (200, 128, 128):
+        return None
+    d = np.load(path)
+    meta = json.loads(str(d["meta"]))
+    k, j, i = meta["hot_node"]
+    dT = max(float(np.max(np.abs(T.ravel()[d["idx"]] - d["T_idx"]))), float(np.max(np.abs(T[k] - d["plane"]))),
+             float(np.max(np.abs(T[:, j, i] - d["line"]))))
+    return {"reference": "NSPCG (ic + cg from the reference's extlib/nspcg) at zeta 1e-12, 5 outer loops",
+            "fixture": "tests/golden/static3d_layered_c1_128x128x200_nspcg.npz",
+            "compared_nodes": int(d["idx"].size + d["plane"].size + d["line"].size),
+            "max_dT_vs_reference_K": dT, "rel_residual_fp64": rel_residual,
+            "reference_rel_residual_fp64": meta["rel_residual"], "reference_max_t_K": meta["max_t"]}
 
 
 def run_reference(args):
@@ -247,12 +317,18 @@ def run_reference(args):
         times.append(time.perf_counter() - t0)
         vals.append(last["value"])
     v = statistics.median(vals)
+    c0 = None
+    if not args.no_cpu:
+        try:
+            c0 = cpu_c0_measured()
+        except Exception as e:  # reported, not required
+            c0 = {"failed": str(e)}
     out = {
         "metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded layered generator)",
         "config": {"workload": WORKLOAD, "nodes": int(size[0] * size[1] * size[2]), "l2": "host run, n/a"},
-        "cpu_baseline": {k: last[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_baseline": dict({k: last[k] for k in ("value", "unit", "cores", "kind", "sample")}, c0_measured=c0),
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -393,6 +469,7 @@ def main():
     solves = dist.sum(len(times))
     value = solves / t_total
     T_mixed = fem.temperature()
+    parity = reference_parity(sv._full_temperature(), stats[-1]["last_rel_residual"])
 
     # end to end through the C ABI: pinned host inputs, results read back every step
     mat_h = torch.from_numpy(to_mesh_order(s.mat, sv.mesh.ordering).astype(np.int32)).pin_memory()
@@ -449,7 +526,8 @@ def main():
     peak, peak_kind = measured_peaks()
     achieved = by / (ms * 1e-3) / 1e9
     tr = profiled_traffic()
-    roofline = {"kernel": "k_apply (FP32 matrix-free stiffness apply, CG mode)", "bound": "hbm",
+    roofline = {"kernel": "k_apply_tma (FP32 matrix-free stiffness apply of the inner CG: TMA-staged planes, "
+                          "packed f32x2 arithmetic)", "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"{peak_kind} hbm_gbs", "bytes_per_launch": by, "ms_per_launch": ms,
                 "traffic": (tr or {}).get("bytes_per_launch"),
@@ -462,6 +540,10 @@ def main():
             cpu = cpu_baseline(size, args.cpu_iterations)
         except Exception as e:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {e}"}
+        try:
+            cpu["c0_measured"] = cpu_c0_measured()
+        except Exception as e:
+            cpu["c0_measured"] = {"failed": str(e)}
 
     last = stats[-1]
     out = {
@@ -475,6 +557,7 @@ def main():
                   "refinements": last["refinements"], "rel_residual": last["last_rel_residual"],
                   "max_t_K": last["max_t"], "toterr_K": last["toterr"]},
         "plain_fp64": plain,
+        "parity": parity,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": 1e3 * statistics.mean(e2e_times)},
         "gpu_launches": int(sum(st["kernel_launches"] for st in stats)),

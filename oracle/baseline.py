@@ -137,3 +137,43 @@ def sample(prob, cg_iterations=30, solver="port", zeta=1e-12):
         raise ValueError(solver)
     return {"assembly_s": t1 - t0, "factor_s": t2 - t1, "cg_s": t3 - t2, "cg_iterations": iters,
             "per_iteration_s": (t3 - t2) / max(iters, 1), "nodes": int(b.size)}
+
+
+def full_solve_iterative(prob, zeta=1e-12, maxit=5000, max_loops=30):
+    """The whole outer k(T) loop of the reference's ``iterative`` algorithm with the IC(0)-PCG
+    restatement on one core (therm3d.cpp:281-340 around iterative_matrix.hpp:141-339), timed.
+
+    Returns wall seconds, outer loops, IC-CG iterations summed over the loops and the field."""
+    numbering = O.masked_numbering(prob)
+    th = O.element_thickness(prob)
+    T = np.full(prob.shape, float(prob.inittemp))
+    sv = IcCg(maxit=maxit, zeta=zeta)
+    loops, iters = 0, 0
+    t0 = time.perf_counter()
+    while True:
+        coef, b, offsets = assemble_diagonal(prob, T, th, numbering)
+        x = sv.solve(coef, offsets, b, O.from_full(numbering[0], numbering[1], T))
+        Tn = O.to_full(prob, numbering[0], x)
+        err = float(np.max(np.abs(Tn - T)))
+        T = Tn
+        loops += 1
+        iters += sv.iters
+        if not ((sv.status != 0 or err > prob.maxerr) and loops < max_loops):
+            break
+    return {"wall_s": time.perf_counter() - t0, "loops": loops, "iterations": iters, "T": T}
+
+
+def full_solve_cholesky(prob):
+    """The whole outer loop of the reference's ``cholesky`` algorithm: the oracle's assembly and
+    LAPACK dpbtrf/dpbtrs (cholesky_matrix.hpp:95,107) with the BLAS library's threads, timed."""
+    t0 = time.perf_counter()
+    T, toterr, rec = O.compute(prob)
+    return {"wall_s": time.perf_counter() - t0, "loops": len(rec), "T": T}
+
+
+def predict(sample_result, loops, iterations, nfact=10):
+    """Seconds of a full iterative solve from a bounded sample: per loop an assembly, one IC
+    factorisation per nfact solves (iterative_matrix.hpp:149-150), per iteration the sampled cost."""
+    refactors = (loops + nfact - 1) // nfact
+    return (loops * sample_result["assembly_s"] + refactors * sample_result["factor_s"]
+            + iterations * sample_result["per_iteration_s"])
