@@ -111,6 +111,18 @@ const char* plgpu_fem3d_last_error(const plgpu_fem3d* h);
 int plgpu_fem3d_set_materials(plgpu_fem3d* h, int n_mat, const double* k300, const double* p,
                               const double* kz_ratio, const double* hexp, const uint8_t* empty);
 
+/* Tabulated k(T) of one material, replacing the power law of
+   plgpu_fem3d_set_materials for it: the reference calls the material's
+   virtual Material::thermk(T, h) (plask/material/material.hpp:691) per
+   element (therm3d.cpp:208-213, 366-370, 421-435); a caller binds any such
+   material by sampling it at n_points temperatures T[i] (strictly increasing,
+   K) into k_xy[i] and k_z[i] (W/(m K); k_z NULL: isotropic).  Between points k
+   is linear in T, beyond the first and the last point it is held constant; the
+   material's h^hexp factor still applies.  n_points = 0 removes the table.
+   Call after plgpu_fem3d_set_materials, which clears all tables. */
+int plgpu_fem3d_set_material_table(plgpu_fem3d* h, int material, int n_points, const double* T,
+                                   const double* k_xy, const double* k_z);
+
 /* Material id and heat density of every element, in mesh element order.
    Replaces geometry->getMaterial(midpoint) (therm3d.cpp:205) and the inHeat
    receiver sampled at element midpoints (therm3d.cpp:179).  heat may be NULL (no source).

@@ -65,6 +65,9 @@ class Materials:
     kz_ratio: np.ndarray | None = None
     hexp: np.ndarray | None = None
     empty: np.ndarray | None = None
+    # tabulated k(T): {material id: (T, k_xy, k_z or None)}, replacing the power law of that
+    # material (piecewise linear in T, constant beyond the ends; h**hexp still applies)
+    tables: dict | None = None
 
     def __post_init__(self):
         self.k300 = np.asarray(self.k300, dtype=np.float64)
@@ -76,11 +79,46 @@ class Materials:
 
     def thermk(self, m, T, h):
         """(k_xy, k_z) of material ids ``m`` at temperature ``T`` and thickness ``h``."""
+        m = np.asarray(m)
         kxy = self.k300[m] * (300.0 / T) ** self.p[m]
         he = self.hexp[m]
         if np.any(he != 0):
             kxy = kxy * np.where(he != 0, h ** he, 1.0)
-        return kxy, kxy * self.kz_ratio[m]
+        kz = kxy * self.kz_ratio[m]
+        if self.tables:
+            Tb = np.broadcast_to(np.asarray(T, np.float64), m.shape)
+            hb = np.broadcast_to(np.asarray(h, np.float64), m.shape) if h is not None else None
+            kxy, kz = np.array(kxy, np.float64, copy=True), np.array(kz, np.float64, copy=True)
+            for mid, tab in self.tables.items():
+                sel = m == mid
+                if not np.any(sel):
+                    continue
+                a, c = table_k(tab, Tb[sel])
+                if self.hexp[mid] != 0:
+                    f = hb[sel] ** self.hexp[mid]
+                    a, c = a * f, c * f
+                kxy[sel], kz[sel] = a, c
+        return kxy, kz
+
+
+def table_k(tab, T):
+    """(k_xy, k_z) of a tabulated material at temperatures T: linear between the points,
+    constant beyond the first and the last (the GPU's mat_thermk evaluates the same)."""
+    t = np.asarray(tab[0], np.float64)
+    a = np.asarray(tab[1], np.float64)
+    c = a if len(tab) < 3 or tab[2] is None else np.asarray(tab[2], np.float64)
+    T = np.asarray(T, np.float64)
+    hi = np.clip(np.searchsorted(t, T, side="right"), 1, max(len(t) - 1, 1))
+    lo = hi - 1
+    if len(t) == 1:
+        return np.full(T.shape, a[0]), np.full(T.shape, c[0])
+    w = (T - t[lo]) / (t[hi] - t[lo])
+    ka = a[lo] + w * (a[hi] - a[lo])
+    kc = c[lo] + w * (c[hi] - c[lo])
+    below, above = ~(T > t[0]), T >= t[-1]
+    ka = np.where(below, a[0], np.where(above, a[-1], ka))
+    kc = np.where(below, c[0], np.where(above, c[-1], kc))
+    return ka, kc
 
 
 @dataclasses.dataclass
@@ -546,7 +584,7 @@ def from_structure(s, order=None, empty_elements="exclude"):
     shape = tuple(len(a) for a in s.axes[::-1])
     if order is None:
         order = optimal_order(len(s.axes[0]), len(s.axes[1]), len(s.axes[2]))
-    mats = Materials(s.k300, s.p, s.kz_ratio, s.hexp, s.empty)
+    mats = Materials(s.k300, s.p, s.kz_ratio, s.hexp, s.empty, getattr(s, "ktables", None))
     return Problem(
         axes=tuple(np.asarray(a, np.float64) for a in s.axes), mat=np.asarray(s.mat), materials=mats,
         heat=np.asarray(s.heat, np.float64),

@@ -98,6 +98,7 @@ SIGNATURES = {
     "plgpu_fem3d_set_preconditioner": (C.c_int, [_h, _h]),
     "plgpu_fem3d_mult": (C.c_int, [_h, C.c_int, _dp, _dp]),
     "plgpu_fem3d_mult_noalloc": (C.c_int, [_h, C.c_int, _dp, _dp]),
+    "plgpu_fem3d_set_material_table": (C.c_int, [_h, C.c_int, C.c_int, _dp, _dp, _dp]),
     "plgpu_fem3d_cg_operator": (C.c_int, [_h, _dp, _dp, _dp, C.POINTER(C.c_int)]),
     # include/plgpu_elec3d.h
     "plgpu_elec3d_create": (C.c_int, [_dp, C.c_int, _dp, C.c_int, _dp, C.c_int, C.c_int, C.POINTER(_h)]),
@@ -243,6 +244,15 @@ class Fem3D:
         self._check(self._lib.plgpu_fem3d_set_materials(self._h, len(k300), _ptr(k300, C.c_double), _ptr(p, C.c_double),
                                                         _ptr(kz, C.c_double), _ptr(he, C.c_double),
                                                         _ptr(em, C.c_uint8)))
+
+    def set_material_table(self, material, T, k_xy, k_z=None):
+        """Tabulated k(T) of one material (piecewise linear, constant beyond the ends)."""
+        t, kx, kz = _f64(T), _f64(k_xy), _f64(k_z)
+        n = 0 if t is None else len(t)
+        if n and (len(kx) != n or (kz is not None and len(kz) != n)):
+            raise BadInput(-1, "table arrays must have the same length")
+        self._check(self._lib.plgpu_fem3d_set_material_table(self._h, int(material), n, _ptr(t, C.c_double),
+                                                             _ptr(kx, C.c_double), _ptr(kz, C.c_double)))
 
     def set_elements(self, material, heat=None, leaf_height=None):
         m = np.ascontiguousarray(material, dtype=np.int32).ravel()

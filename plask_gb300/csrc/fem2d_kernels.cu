@@ -187,10 +187,7 @@ __global__ void __launch_bounds__(256) k_coef2d(int n0, int n1, const double* __
             const int m = mat[e];
             if (!tab.excluded[m]) {
                 const double t = quad_mean(T, e, n0);
-                double kk = tab.k300[m] * pow(300.0 / t, tab.p[m]);
-                if (tab.hexp[m] != 0.0) kk *= pow(th[e], tab.hexp[m]);
-                kx = kk;
-                ky = kk * tab.kz_ratio[m];
+                mat_thermk(tab, m, t, th[e], kx, ky);
             }
         }
         k64[e] = kx;
@@ -313,9 +310,8 @@ __global__ void __launch_bounds__(256) k_flux2d(const GridT<double> g, const dou
         }
         const double ll = T[e], lr = T[e + 1], ul = T[e + n0], ur = T[e + 1 + n0];
         const double temp = 0.25 * (ll + lr + ul + ur);
-        double kk = tab.k300[m] * pow(300.0 / temp, tab.p[m]);
-        if (tab.hexp[m] != 0.0) kk *= pow(hleaf[e], tab.hexp[m]);
-        const double kx = kk, ky = kk * tab.kz_ratio[m];
+        double kx, ky;
+        mat_thermk(tab, m, temp, hleaf[e], kx, ky);
         out[2 * t] = -0.5e6 * kx * (-ll + lr - ul + ur) / g.h0[i];
         out[2 * t + 1] = -0.5e6 * ky * (-ll - lr + ul + ur) / g.h1[j];
     }
@@ -334,10 +330,10 @@ __global__ void __launch_bounds__(256) k_conductivity2d(int n0, int n1, const do
             continue;
         }
         const double temp = quad_mean(T, e, n0);
-        double kk = tab.k300[m] * pow(300.0 / temp, tab.p[m]);
-        if (tab.hexp[m] != 0.0) kk *= pow(th[e], tab.hexp[m]);
+        double kk, kv;
+        mat_thermk(tab, m, temp, th[e], kk, kv);
         out[2 * t] = kk;
-        out[2 * t + 1] = kk * tab.kz_ratio[m];
+        out[2 * t + 1] = kv;
     }
 }
 

@@ -189,6 +189,10 @@ struct plgpu_fem3d {
     bool aniso = false;
     DevBuf d_k300, d_p, d_kzr, d_hexp, d_excl;
     MatTable tab{};
+    // tabulated k(T) per material (empty: the power law)
+    std::vector<std::vector<double>> ktab_T, ktab_xy, ktab_z;
+    DevBuf d_toff, d_tn, d_tT, d_txy, d_tz;
+    bool any_ktab = false;
 
     // elements (canonical padded layout)
     std::vector<int32_t> host_mat;  // mesh element order
@@ -479,6 +483,10 @@ struct plgpu_fem3d {
             if (!(k300[m] >= 0.0) || !std::isfinite(k300[m])) throw ArgError("k300 must be finite and >= 0");
             if (kzr[m] != 1.0) aniso = true;
         }
+        ktab_T.assign(nm, {});
+        ktab_xy.assign(nm, {});
+        ktab_z.assign(nm, {});
+        any_ktab = false;
         upload(d_k300, k300, stream);
         upload(d_p, pexp, stream);
         upload(d_kzr, kzr, stream);
@@ -489,6 +497,62 @@ struct plgpu_fem3d {
         }
         invalidate_graphs();
         invalidate_solution();
+    }
+
+    // A tabulated k(T) for material m (n points; n = 0 removes it), in place of the power law
+    void set_material_table(int m, int npts, const double* Tp, const double* kxy, const double* kz) {
+        if (n_mat == 0) throw StateError("set the material table first");
+        if (m < 0 || m >= n_mat) throw ArgError("material id out of range");
+        if (npts < 0) throw ArgError("negative point count");
+        if (npts > 0 && (!Tp || !kxy)) throw ArgError("the table needs temperatures and k_xy");
+        for (int i = 0; i < npts; ++i) {
+            if (!std::isfinite(Tp[i]) || !(Tp[i] > 0.0)) throw ArgError("table temperatures must be finite and > 0");
+            if (i > 0 && !(Tp[i] > Tp[i - 1])) throw ArgError("table temperatures must be strictly increasing");
+            if (!std::isfinite(kxy[i]) || kxy[i] < 0.0 || (kz && (!std::isfinite(kz[i]) || kz[i] < 0.0)))
+                throw ArgError("table conductivities must be finite and >= 0");
+        }
+        ktab_T[m].assign(Tp, Tp + npts);
+        ktab_xy[m].assign(kxy, kxy + npts);
+        ktab_z[m].assign(kz ? kz : kxy, (kz ? kz : kxy) + npts);
+        // flattened device copy of all tables
+        std::vector<int> off((size_t)n_mat, -1), cnt((size_t)n_mat, 0);
+        std::vector<double> tT, txy, tz;
+        any_ktab = false;
+        bool tab_aniso = false;
+        for (int q = 0; q < n_mat; ++q) {
+            if (ktab_T[q].empty()) continue;
+            any_ktab = true;
+            off[q] = (int)tT.size();
+            cnt[q] = (int)ktab_T[q].size();
+            tT.insert(tT.end(), ktab_T[q].begin(), ktab_T[q].end());
+            txy.insert(txy.end(), ktab_xy[q].begin(), ktab_xy[q].end());
+            tz.insert(tz.end(), ktab_z[q].begin(), ktab_z[q].end());
+            for (size_t i = 0; i < ktab_T[q].size(); ++i) tab_aniso |= ktab_z[q][i] != ktab_xy[q][i];
+        }
+        if (any_ktab) {
+            upload(d_toff, off, stream);
+            upload(d_tn, cnt, stream);
+            upload(d_tT, tT, stream);
+            upload(d_txy, txy, stream);
+            upload(d_tz, tz, stream);
+        }
+        bool an = tab_aniso;
+        for (int q = 0; q < n_mat; ++q) an |= ktab_T[q].empty() && kzr[q] != 1.0;
+        if (an && !aniso) {
+            kz64.alloc((size_t)N * 8);
+            kz32.alloc((size_t)N * 4);
+        }
+        aniso = aniso || an;
+        bind_tables();
+        invalidate_graphs();
+        invalidate_solution();
+    }
+    void bind_tables() {
+        tab.tab_off = any_ktab ? d_toff.as<int>() : nullptr;
+        tab.tab_n = any_ktab ? d_tn.as<int>() : nullptr;
+        tab.tab_T = any_ktab ? d_tT.as<double>() : nullptr;
+        tab.tab_kxy = any_ktab ? d_txy.as<double>() : nullptr;
+        tab.tab_kz = any_ktab ? d_tz.as<double>() : nullptr;
     }
 
     void set_elements(const int32_t* mat, const double* heat, const double* leaf) {
@@ -563,6 +627,7 @@ struct plgpu_fem3d {
         upload(d_excl, ex, stream);
         tab = MatTable{d_k300.as<double>(), d_p.as<double>(), d_kzr.as<double>(), d_hexp.as<double>(),
                        d_excl.as<uint8_t>()};
+        bind_tables();
 
         // masked numbering: nodes touched by an active element, in mesh order
         masked = false;
@@ -2645,6 +2710,11 @@ const char* plgpu_fem3d_last_error(const plgpu_fem3d* h) { return h ? h->err.c_s
 int plgpu_fem3d_set_materials(plgpu_fem3d* h, int n_mat, const double* k300, const double* p, const double* kz_ratio,
                               const double* hexp, const uint8_t* empty) {
     return guarded(h, [&] { h->set_materials(n_mat, k300, p, kz_ratio, hexp, empty); });
+}
+
+int plgpu_fem3d_set_material_table(plgpu_fem3d* h, int material, int n_points, const double* T, const double* k_xy,
+                                   const double* k_z) {
+    return guarded(h, [&] { h->set_material_table(material, n_points, T, k_xy, k_z); });
 }
 
 int plgpu_fem3d_set_elements(plgpu_fem3d* h, const int32_t* material, const double* heat, const double* leaf_height) {

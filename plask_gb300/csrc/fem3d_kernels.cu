@@ -481,10 +481,10 @@ __global__ void __launch_bounds__(256) k_coef(int n0, int n1, int n2, const doub
                 t += T[e + s1 + s2];
                 t += T[e + 1 + s1 + s2];
                 t *= 0.125;
-                double kk = tab.k300[m] * pow(300.0 / t, tab.p[m]);
-                if (tab.hexp[m] != 0.0) kk *= pow(th[e], tab.hexp[m]);
+                double kk, kv;
+                mat_thermk(tab, m, t, th[e], kk, kv);
                 kxy = kk * 1e-6;
-                kz = (kk * tab.kz_ratio[m]) * 1e-6;
+                kz = kv * 1e-6;
             }
         }
         k64[e] = kxy;
@@ -639,9 +639,8 @@ __global__ void __launch_bounds__(256) k_flux(const GridT<double> g, const doubl
         const double lll = T[e], ull = T[e + 1], lul = T[e + s1], uul = T[e + 1 + s1];
         const double llu = T[e + s2], ulu = T[e + 1 + s2], luu = T[e + s1 + s2], uuu = T[e + 1 + s1 + s2];
         const double temp = 0.125 * (lll + llu + lul + luu + ull + ulu + uul + uuu);
-        double kk = tab.k300[m] * pow(300.0 / temp, tab.p[m]);
-        if (tab.hexp[m] != 0.0) kk *= pow(hleaf[e], tab.hexp[m]);
-        const double kxy = kk, kz = kk * tab.kz_ratio[m];
+        double kxy, kz;
+        mat_thermk(tab, m, temp, hleaf[e], kxy, kz);
         out[3 * t] = -0.25e6 * kxy * (-lll - llu - lul - luu + ull + ulu + uul + uuu) / g.h0[i];
         out[3 * t + 1] = -0.25e6 * kxy * (-lll - llu + lul + luu - ull - ulu + uul + uuu) / g.h1[j];
         out[3 * t + 2] = -0.25e6 * kz * (-lll + llu - lul + luu - ull + ulu - uul + uuu) / g.h2[k];
@@ -667,10 +666,10 @@ __global__ void __launch_bounds__(256) k_conductivity(int n0, int n1, int n2, co
         }
         const double temp = 0.125 * (T[e] + T[e + 1] + T[e + s1] + T[e + 1 + s1] + T[e + s2] + T[e + 1 + s2] +
                                      T[e + s1 + s2] + T[e + 1 + s1 + s2]);
-        double kk = tab.k300[m] * pow(300.0 / temp, tab.p[m]);
-        if (tab.hexp[m] != 0.0) kk *= pow(th[e], tab.hexp[m]);
+        double kk, kv;
+        mat_thermk(tab, m, temp, th[e], kk, kv);
         out[2 * t] = kk;
-        out[2 * t + 1] = kk * tab.kz_ratio[m];
+        out[2 * t + 1] = kv;
     }
 }
 

@@ -33,7 +33,65 @@ struct MatTable {
     const double* kz_ratio;
     const double* hexp;
     const uint8_t* excluded;  // element of this material is dropped from the system
+    // tabulated k(T) (plgpu_fem3d_set_material_table): for material m with tab_off[m] >= 0,
+    // tab_n[m] points (tab_T, tab_kxy, tab_kz)[tab_off[m] ...] replace k300 (300/T)^p and kz_ratio;
+    // tab_off == nullptr when no material has a table
+    const int* tab_off;
+    const int* tab_n;
+    const double* tab_T;
+    const double* tab_kxy;
+    const double* tab_kz;
 };
+
+#ifdef __CUDACC__
+// k_xy, k_z [W/(m K)] of material m at temperature T and layer-run thickness h, as the
+// reference's Material::thermk(T, h) (plask/material/material.hpp:691) for the materials
+// this solver models: the power law k300 (300/T)^p, k_z = kz_ratio k_xy, or the material's
+// table, piecewise linear in T between its points and constant beyond the first and the
+// last (a monotone interpolation: it never leaves the range of two neighbouring points);
+// either times h^hexp when hexp != 0.
+__device__ __forceinline__ void mat_thermk(const MatTable& tab, int m, double T, double h, double& kxy,
+                                           double& kz) {
+    double kk, kv;
+    const int off = tab.tab_off != nullptr ? tab.tab_off[m] : -1;
+    if (off >= 0) {
+        const int n = tab.tab_n[m];
+        const double* t = tab.tab_T + off;
+        const double* a = tab.tab_kxy + off;
+        const double* c = tab.tab_kz + off;
+        if (!(T > t[0])) {  // also a NaN temperature
+            kk = a[0];
+            kv = c[0];
+        } else if (T >= t[n - 1]) {
+            kk = a[n - 1];
+            kv = c[n - 1];
+        } else {
+            int lo = 0, hi = n - 1;  // t[lo] < T < t[hi]
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (t[mid] <= T)
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            const double w = (T - t[lo]) / (t[hi] - t[lo]);
+            kk = a[lo] + w * (a[hi] - a[lo]);
+            kv = c[lo] + w * (c[hi] - c[lo]);
+        }
+        if (tab.hexp[m] != 0.0) {
+            const double f = pow(h, tab.hexp[m]);
+            kk *= f;
+            kv *= f;
+        }
+    } else {
+        kk = tab.k300[m] * pow(300.0 / T, tab.p[m]);
+        if (tab.hexp[m] != 0.0) kk *= pow(h, tab.hexp[m]);
+        kv = kk * tab.kz_ratio[m];
+    }
+    kxy = kk;
+    kz = kv;
+}
+#endif
 
 struct LaunchCfg {
     cudaStream_t stream;

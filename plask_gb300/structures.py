@@ -38,6 +38,7 @@ class Structure:
     * ``temperature``/``heatflux``/``convection``/``radiation``: boundary
       conditions as (side, values...) with side one of
       "bottom", "top", "back", "front", "left", "right"
+    * ``ktables``: tabulated k(T) replacing the power law of some materials
     """
 
     axes: tuple
@@ -55,6 +56,8 @@ class Structure:
     maxerr: float = 0.05
     inittemp: float = 300.0
     name: str = ""
+    # tabulated k(T) of some materials: {material id: (T, k_xy, k_z or None)}
+    ktables: dict | None = None
 
     @property
     def shape(self):

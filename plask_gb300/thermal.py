@@ -40,6 +40,9 @@ class MaterialTable:
     empty: np.ndarray | None = None
     cp: np.ndarray | None = None     # heat capacity J/(kg K), for Dynamic3D
     dens: np.ndarray | None = None   # density kg/m^3, for Dynamic3D
+    # tabulated k(T) replacing the power law of some materials: {material id: (T, k_xy, k_z or None)},
+    # linear in T between the points, constant beyond the ends (the h**hexp factor still applies)
+    tables: dict | None = None
 
     def __post_init__(self):
         self.k300 = np.asarray(self.k300, np.float64)
@@ -49,11 +52,42 @@ class MaterialTable:
         self.hexp = np.zeros(n) if self.hexp is None else np.asarray(self.hexp, np.float64)
         self.empty = np.zeros(n, bool) if self.empty is None else np.asarray(self.empty, bool)
 
+    def tabulate(self, m, thermk, T):
+        """Replace material m's power law by a table sampled from ``thermk(T) -> (k_xy, k_z)``
+        (the way a caller binds a material's Material::thermk, plask/material/material.hpp:691)
+        at the strictly increasing temperatures T."""
+        T = np.asarray(T, np.float64)
+        kxy, kz = zip(*(thermk(float(t)) for t in T))
+        if self.tables is None:
+            self.tables = {}
+        self.tables[int(m)] = (T, np.asarray(kxy, np.float64), np.asarray(kz, np.float64))
+
     def thermk(self, m, T, h=None):
+        m = np.asarray(m)
         kxy = self.k300[m] * (300.0 / np.asarray(T)) ** self.p[m]
         if h is not None and np.any(self.hexp[m] != 0):
             kxy = kxy * np.asarray(h) ** self.hexp[m]
-        return kxy, kxy * self.kz_ratio[m]
+        kz = kxy * self.kz_ratio[m]
+        if self.tables:
+            Tb = np.broadcast_to(np.asarray(T, np.float64), m.shape)
+            kxy, kz = np.array(kxy, np.float64, copy=True), np.array(kz, np.float64, copy=True)
+            for mid, tab in self.tables.items():
+                sel = m == mid
+                if not np.any(sel):
+                    continue
+                t, a = np.asarray(tab[0], np.float64), np.asarray(tab[1], np.float64)
+                c = a if len(tab) < 3 or tab[2] is None else np.asarray(tab[2], np.float64)
+                ka, kc = np.interp(Tb[sel], t, a), np.interp(Tb[sel], t, c)
+                if h is not None and self.hexp[mid] != 0:
+                    f = np.broadcast_to(np.asarray(h, np.float64), m.shape)[sel] ** self.hexp[mid]
+                    ka, kc = ka * f, kc * f
+                kxy[sel], kz[sel] = ka, kc
+        return kxy, kz
+
+    def apply_tables(self, fem):
+        """Send the tables to a native handle (after its set_materials)."""
+        for mid, tab in (self.tables or {}).items():
+            fem.set_material_table(int(mid), tab[0], tab[1], None if len(tab) < 3 else tab[2])
 
 
 class StructureGeometry:
@@ -86,7 +120,8 @@ class StructureGeometry:
 
     @classmethod
     def from_structure(cls, s):
-        return cls(MaterialTable(s.k300, s.p, s.kz_ratio, s.hexp, s.empty), mat=s.mat)
+        return cls(MaterialTable(s.k300, s.p, s.kz_ratio, s.hexp, s.empty, tables=getattr(s, "ktables", None)),
+                   mat=s.mat)
 
 
 class BoundaryConditions:
@@ -707,6 +742,7 @@ class Static3D:
         if self._elements_dirty:
             mt = self._geometry.materials
             fem.set_materials(mt.k300, mt.p, mt.kz_ratio, mt.hexp, mt.empty)
+            mt.apply_tables(fem)
             mat = self._geometry.material_ids(self._mesh)
             leaf = self._geometry.leaf_height(self._mesh)
             order = self._mesh.ordering

@@ -55,7 +55,8 @@ class StructureGeometry2D:
 
     @classmethod
     def from_structure(cls, s):
-        return cls(MaterialTable(s.k300, s.p, s.kz_ratio, s.hexp, s.empty), mat=s.mat)
+        return cls(MaterialTable(s.k300, s.p, s.kz_ratio, s.hexp, s.empty, tables=getattr(s, "ktables", None)),
+                   mat=s.mat)
 
 
 class Receiver2D:
@@ -234,6 +235,7 @@ class Static2D:
         if self._elements_dirty:
             mt = self._geometry.materials
             fem.set_materials(mt.k300, mt.p, mt.kz_ratio, mt.hexp, mt.empty)
+            mt.apply_tables(fem)
             mat = self._geometry.material_ids(self._mesh)
             leaf = self._geometry.leaf_height(self._mesh)
             fem.set_elements(to_mesh_order2d(mat, order), to_mesh_order2d(self._inHeat(self._mesh), order),

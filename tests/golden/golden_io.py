@@ -90,5 +90,10 @@ def load(name):
     return data, meta
 
 
+# fixtures that store answers at a subset of nodes of a regenerated structure instead of the
+# inputs (make_golden_c1.py); replayed by their own tests, not by the generic replay
+SUBSET_FIXTURES = ("static3d_layered_c1_128x128x200_nspcg",)
+
+
 def names():
-    return sorted(p.stem for p in HERE.glob("*.npz"))
+    return sorted(p.stem for p in HERE.glob("*.npz") if p.stem not in SUBSET_FIXTURES)

@@ -2,6 +2,7 @@
 
     python tests/golden/make_golden_c1.py           (about forty minutes on one core)
     python tests/golden/make_golden_c1.py 40,36,50  (a dry run on a smaller mesh, writes nothing)
+    python tests/golden/make_golden_c1.py --refresh-inputs  (rewrite the stored input summary only)
 
 The benchmark's case (``structures.layered_c1()``: seed 1000, 128 x 128 x 200 nodes,
 anisotropic layers, convective top, Dirichlet bottom) solved by the reference's own
@@ -13,9 +14,9 @@ reference's 14-diagonal storage (iterative_matrix.hpp:373-393).
 At this size the band Cholesky of the ``cholesky`` algorithm needs 433 GB and cannot run,
 so the tight NSPCG solve is the reference answer.  The whole field (26 MB) is not stored:
 the fixture keeps
-  * a SHA-256 of the generated inputs (axes, element materials and heat, material table,
-    boundary conditions), so that a test regenerating the structure knows it has the
-    problem the answers belong to;
+  * a summary of the generated inputs (``input_summary``: axes, material table, a SHA-256 of
+    the element materials, heat statistics, boundary conditions), so that a test regenerating
+    the structure knows it has the problem the answers belong to;
   * the temperatures of 16384 seeded random nodes, of the whole plane through the hottest
     node and of the vertical line through it;
   * per outer loop: NSPCG iterations, err, max T, wall time and the FP64 relative residual
@@ -47,18 +48,32 @@ OUT = HERE / "static3d_layered_c1_128x128x200_nspcg.npz"
 N_RANDOM = 16384
 
 
-def input_digest(s):
-    """SHA-256 over the solver inputs of a generated structure."""
-    h = hashlib.sha256()
-    for a in s.axes:
-        h.update(np.ascontiguousarray(a, np.float64).tobytes())
-    h.update(np.ascontiguousarray(s.mat, np.int32).tobytes())
-    h.update(np.ascontiguousarray(s.heat, np.float64).tobytes())
-    for f in ("k300", "p", "kz_ratio", "hexp"):
-        h.update(np.ascontiguousarray(getattr(s, f), np.float64).tobytes())
-    h.update(np.ascontiguousarray(s.empty, np.uint8).tobytes())
-    h.update(json.dumps([s.temperature, s.heatflux, s.convection, s.radiation, s.maxerr, s.inittemp]).encode())
-    return h.hexdigest()
+def input_summary(s):
+    """The solver inputs of a generated structure, in a form that survives the last-bit
+    differences of libm between machines: the axes and the material table in full, a SHA-256
+    of the (integer) element materials, the heat's nonzero count, sum and extremes, and the
+    boundary conditions."""
+    heat = np.asarray(s.heat, np.float64)
+    return {"axes": [np.asarray(a, np.float64).tolist() for a in s.axes],
+            "materials": {f: np.asarray(getattr(s, f), np.float64).tolist() for f in ("k300", "p", "kz_ratio", "hexp")},
+            "empty": np.asarray(s.empty, bool).tolist(),
+            "mat_sha256": hashlib.sha256(np.ascontiguousarray(s.mat, np.int32).tobytes()).hexdigest(),
+            "heat": {"nonzero": int(np.count_nonzero(heat)), "sum": float(heat.sum()), "min": float(heat.min()),
+                     "max": float(heat.max())},
+            "bc": json.loads(json.dumps([s.temperature, s.heatflux, s.convection, s.radiation, s.maxerr,
+                                         s.inittemp]))}
+
+
+def inputs_match(s, summary, rtol=1e-12):
+    """Whether a regenerated structure has the inputs a fixture's answers belong to."""
+    now = input_summary(s)
+    close = lambda a, b: np.allclose(np.asarray(a, np.float64), np.asarray(b, np.float64), rtol=rtol, atol=0)
+    return (all(close(a, b) for a, b in zip(now["axes"], summary["axes"]))
+            and all(close(now["materials"][f], summary["materials"][f]) for f in now["materials"])
+            and now["empty"] == summary["empty"] and now["mat_sha256"] == summary["mat_sha256"]
+            and now["heat"]["nonzero"] == summary["heat"]["nonzero"]
+            and all(close(now["heat"][f], summary["heat"][f]) for f in ("sum", "min", "max"))
+            and now["bc"] == summary["bc"])
 
 
 def sample_nodes(shape, rng):
@@ -72,7 +87,7 @@ def main(size=None):
     if not NS.available():
         raise SystemExit("oracle/_ref/libnspcg_ref.so is not built: make -C oracle ref (needs the reference tree)")
     s = S.layered_c1() if size is None else S.layered_c1(n=size)
-    digest = input_digest(s)
+    summary = input_summary(s)
     prob = O.from_structure(s, empty_elements="include")
     numbering = O.masked_numbering(prob)
     node_id, n_active = numbering
@@ -105,7 +120,7 @@ def main(size=None):
     k_hot, j_hot, i_hot = np.unravel_index(int(np.argmax(Tf)), prob.shape)
     plane = np.ascontiguousarray(T[k_hot])
     line = np.ascontiguousarray(T[:, j_hot, i_hot])
-    meta = {"generator": "structures.layered_c1(seed=1000, n=(128, 128, 200))", "input_sha256": digest,
+    meta = {"generator": "structures.layered_c1(seed=1000, n=(128, 128, 200))", "inputs": summary,
             "solver": "NSPCG ic + cg from extlib/nspcg, zeta 1e-12, maxit 5000, nfact 10", "order": prob.order,
             "loops": loops, "toterr": toterr, "rel_residual": loops[-1]["rel_residual"],
             "max_t": float(Tf.max()), "hot_node": [int(k_hot), int(j_hot), int(i_hot)], "wall_s": wall,
@@ -120,5 +135,18 @@ def main(size=None):
     CH.OUT.write_text(json.dumps(res, indent=1))
 
 
+def refresh_inputs():
+    """Rewrite the input summary of the existing fixture (the answers are kept)."""
+    d = dict(np.load(OUT))
+    meta = json.loads(str(d["meta"]))
+    meta.pop("input_sha256", None)
+    meta["inputs"] = input_summary(S.layered_c1())
+    d["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(OUT, **d)
+
+
 if __name__ == "__main__":
-    main(tuple(int(v) for v in sys.argv[1].split(",")) if len(sys.argv) > 1 else None)
+    if len(sys.argv) > 1 and sys.argv[1] == "--refresh-inputs":
+        refresh_inputs()
+    else:
+        main(tuple(int(v) for v in sys.argv[1].split(",")) if len(sys.argv) > 1 else None)

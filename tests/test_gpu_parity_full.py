@@ -8,7 +8,7 @@
   Cholesky (433 GB), so the reference answer is the reference's own NSPCG driven to
   zeta = 1e-12, stored in ``tests/golden/static3d_layered_c1_128x128x200_nspcg.npz`` at 16384
   seeded nodes, the plane through the hottest node and the vertical line through it
-  (``tests/golden/make_golden_c1.py``).  The regenerated inputs must hash to the fixture's.
+  (``tests/golden/make_golden_c1.py``).  The regenerated inputs must match the fixture's input summary.
 """
 import json
 import pathlib
@@ -65,11 +65,11 @@ def c1_max_dT(T, meta, d):
 
 @pytest.mark.skipif(not C1_FIXTURE.exists(), reason="the 128x128x200 NSPCG fixture is not generated")
 def test_c1_full_size_matches_reference_nspcg():
-    from make_golden_c1 import input_digest
+    from make_golden_c1 import inputs_match
 
     meta, d = c1_golden()
     s = S.layered_c1()
-    assert input_digest(s) == meta["input_sha256"], "the generator no longer gives the fixture's inputs"
+    assert inputs_match(s, meta["inputs"]), "the generator no longer gives the fixture's inputs"
     sv = TH.solver_for_structure(s, ordering="best", algorithm="gpu-mixed")
     tot = sv.compute()
     T = sv._full_temperature()
