@@ -64,6 +64,10 @@ def parse():
     ap.add_argument("--cpu-iterations", type=int, default=10, help="CG iterations in the CPU baseline sample")
     ap.add_argument("--size", default="128,128,200")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-coupled", action="store_true", help="skip the coupled thermo-electric record")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the batched-sweep record")
+    ap.add_argument("--sweep-record-count", type=int, default=64)
+    ap.add_argument("--sweep-record-sequential", type=int, default=8)
     ap.add_argument("--workload", default="layered", choices=["layered", "sweep"])
     ap.add_argument("--sweep-count", type=int, default=256)
     ap.add_argument("--sweep-loops", type=int, default=30, help="outer-loop cap of every sweep solve")
@@ -339,6 +343,99 @@ def run_reference(args):
 # GPU arm
 
 
+def coupled_record():
+    """The coupled thermo-electric loop (thermoelectric.py:181-219) at 200x200x120
+    (structures.shockley_c4(seed=4000)): electrical compute(tfreq), its Joule heat to the
+    thermal solver on the device, thermal compute(1), until both errors are within maxerr;
+    each call timed (host clock around synchronised calls)."""
+    import numpy as np
+    import torch
+
+    from plask_gb300 import electrical as EL
+    from plask_gb300 import structures as S
+    from plask_gb300 import thermal as TH
+
+    s = S.shockley_c4(seed=4000)
+    te = EL.ThermoElectric3D()
+    te.thermal = TH.solver_for_structure(s.thermal, ordering="best", algorithm="gpu-mixed")
+    te.electrical = EL.solver_for_structure(s, ordering="best", algorithm="gpu-mixed")
+    te.reconnect()
+    te.invalidate()
+    te.initialize()
+    torch.cuda.synchronize()
+    rounds = []
+    verr, terr = 2.0 * te.electrical.maxerr, 2.0 * te.thermal.maxerr
+    t_start = time.perf_counter()
+    while terr > te.thermal.maxerr or verr > te.electrical.maxerr:
+        t0 = time.perf_counter()
+        verr = te.electrical.compute(te.tfreq)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        te._move_heat()
+        terr = te.thermal.compute(1)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        es, ts = te.electrical.stats, te.thermal.stats
+        rounds.append({"electrical_s": t1 - t0, "electrical_loops": es.get("loops"),
+                       "electrical_cg_iterations": es.get("inner_iterations"), "verr_pct": verr,
+                       "thermal_s": t2 - t1, "thermal_cg_iterations": ts.get("inner_iterations"), "terr_K": terr})
+        if len(rounds) >= 30:
+            break
+    wall = time.perf_counter() - t_start
+    n = [len(a) for a in s.axes]
+    return {"workload": f"coupled thermo-electric loop, shockley_c4 seed 4000, {n[0]}x{n[1]}x{n[2]} nodes, "
+                        f"{max(v for _, v in s.voltage):.3f} V on a 6 um top contact, maxerr 0.05 K / 0.1 %",
+            "seconds": wall, "rounds": len(rounds), "per_round": rounds,
+            "electrical_s": sum(r["electrical_s"] for r in rounds), "thermal_s": sum(r["thermal_s"] for r in rounds),
+            "total_current_mA": float(te.get_total_current()), "max_t_K": float(te.thermal.stats.get("max_t", np.nan)),
+            "electrical_operator": "k_apply_tma" if n[0] % 4 == 0 and n[0] <= 256 else "k_apply_shared"}
+
+
+def sweep_record(count, sequential, algorithm="gpu-mixed", loops=30):
+    """A subset of the batched sweep (uneven layered structures, 32..96 nodes per axis): the
+    autotuner on the first 16, all ``count`` solved batched, the first ``sequential`` one at a
+    time (the reference's way), and their agreement."""
+    import numpy as np
+    import torch
+
+    from plask_gb300 import _native
+    from plask_gb300 import structures as S
+    from plask_gb300 import thermal as TH
+
+    structs = S.sweep_c3(count=count)
+    svs = []
+    for st in structs:
+        sv = TH.solver_for_structure(st, ordering="best", algorithm=algorithm)
+        sv.initialize()
+        svs.append(sv)
+    fems = [sv._fem for sv in svs]
+    nodes = int(sum(np.prod(st.shape) for st in structs))
+    seq = fems[:sequential]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for f in seq:
+        f.compute(loops)
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    T_seq = [f.temperature() for f in seq]
+    threads, share, trials = _native.batch_tune(fems[: min(16, len(fems))], loops=loops, max_threads=32)
+    for f in fems:
+        f.set_grid_share(share)
+        f.invalidate()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _native.batch_compute(fems, loops=loops, threads=threads)
+    torch.cuda.synchronize()
+    t_bat = time.perf_counter() - t0
+    dT = max(float(np.max(np.abs(fems[k].temperature() - T_seq[k]))) for k in range(len(seq)))
+    return {"workload": f"{count} structures of the uneven-size sweep (seed 3000: 32..96 nodes per axis, "
+                        f"{nodes} nodes in total, 1e15..1e16 W/m^3, at most {loops} outer loops)",
+            "batched_solves_per_s": count / t_bat, "batched_seconds": t_bat, "threads": threads, "grid_share": share,
+            "one_at_a_time_solves_per_s": sequential / t_seq, "one_at_a_time_sample": sequential,
+            "speedup": (count / t_bat) / (sequential / t_seq),
+            "max_dT_batched_vs_one_at_a_time_K": dT}
+
+
 def run_sweep(args):
     """Batched sweep: one-at-a-time vs concurrent solves of the uneven-size sweep."""
     # more hardware work queues than the default 8, so that up to 32 solver streams
@@ -411,6 +508,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    # more hardware work queues than the default 8 for the batched sweep's solver streams
+    # (read when the CUDA context is created)
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     if args.workload == "sweep":
         return run_sweep(args)
     dist = Dist()
@@ -534,6 +634,18 @@ def main():
                 "l2_resident_ms_per_launch": ms_l2,
                 "fp64_ms_per_launch": ms64, "fp64_achieved_gbs": by64 / (ms64 * 1e-3) / 1e9}
 
+    coupled = sweep = None
+    if dist.rank == 0 and not args.no_coupled:
+        try:
+            coupled = coupled_record()
+        except Exception as e:  # reported, not required
+            coupled = {"failed": str(e)}
+    if dist.rank == 0 and not args.no_sweep:
+        try:
+            sweep = sweep_record(args.sweep_record_count, args.sweep_record_sequential, args.algorithm)
+        except Exception as e:
+            sweep = {"failed": str(e)}
+
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
         try:
@@ -562,6 +674,8 @@ def main():
                 "ms_per_step": 1e3 * statistics.mean(e2e_times)},
         "gpu_launches": int(sum(st["kernel_launches"] for st in stats)),
         "roofline": roofline,
+        "coupled": coupled,
+        "sweep": sweep,
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
