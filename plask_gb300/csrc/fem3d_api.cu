@@ -1071,7 +1071,9 @@ struct plgpu_fem3d {
 
     // The pre-scaled conductances of the TMA operator from the current FP64 ones; called after
     // every write of k64 / kz64 outside a stream capture.  The first call on a mesh the kernel
-    // supports (n0 <= 224 and a multiple of 4) creates the operator.
+    // takes (tma_operator_supported) creates the operator.  Environment: PLGPU_NO_TMA=1 keeps
+    // the register-march kernels everywhere; PLGPU_TMA_ALWAYS=1 takes the TMA kernel on every
+    // mesh it can run, also where it fills less than 80 % of its columns (tests use it).
     void refresh_tma() {
         tma_fresh = false;
         if (planar) return;
@@ -1083,7 +1085,9 @@ struct plgpu_fem3d {
         }
         if (!tma_tried) {
             tma_tried = true;
-            if (std::getenv("PLGPU_NO_TMA") == nullptr && tma_operator_supported(n[0], n[1], n[2])) {
+            const char* always = std::getenv("PLGPU_TMA_ALWAYS");
+            if (std::getenv("PLGPU_NO_TMA") == nullptr &&
+                tma_operator_supported(n[0], n[1], n[2], always != nullptr && always[0] == '1')) {
                 if (!tmaP.p) tmaP.alloc((size_t)N * 4);
                 if (aniso && !tmaQ.p) tmaQ.alloc((size_t)N * 4);
                 if (!cgpart.p) cgpart.alloc(sizeof(double) * 3 * kMaxPartialBlocks);

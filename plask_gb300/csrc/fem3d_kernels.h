@@ -125,10 +125,10 @@ void launch_operator(const LaunchCfg& c, const GridT<double>& g, const double* z
                      const double* rhs, double* partials, int mode, SolveCtl* ctl, const uint32_t* smask = nullptr,
                      int sslots = 0, const double* dshift = nullptr, const double* cmass = nullptr);
 // TMA-staged FP32 operator of the inner CG (fem3d_operator_tma.cu) on one fixed input
-// vector x (the tensor map is encoded for it), for meshes with n0 <= 224 and n0 a multiple
-// of 4 (the copy's row stride must be a multiple of 16 bytes).
+// vector x (the tensor map is encoded for it), for meshes with n0 a multiple of 4, at most
+// 256, that fill at least 80 % of the kernel's 64-column warp spans.
 struct TmaOperator;
-bool tma_operator_supported(int n0, int n1, int n2);
+bool tma_operator_supported(int n0, int n1, int n2, bool any_fill = false);
 // nullptr when the mesh is not supported or a CUDA call fails; hx, hy, hz: element sizes
 TmaOperator* tma_operator_create(const LaunchCfg& c, const GridT<double>& g, const std::vector<double>& hx,
                                  const std::vector<double>& hy, const std::vector<double>& hz, bool aniso,

@@ -33,7 +33,7 @@ import time
 import numpy as np
 
 from . import _native
-from .mesh import RectangularMesh3D, to_mesh_order
+from .mesh import RectangularMesh3D, to_mesh_order, wrap_symmetric
 from .thermal import BadInput, BoundaryConditions, ComputationError, IterativeParams, Provider, Static3D
 from .thermal import (_check_interpolation, _element_axis, _nearest_axis, _points, _trilinear,
                       masked_element_interpolate, masked_interpolate, spline_interpolate)
@@ -492,16 +492,9 @@ class Shockley3D:
         ``symmetric`` flags) a negative coordinate reads at its absolute value.  Returns the
         wrapped points and, per mirrored axis, the mask of reflected points."""
         sym = tuple(getattr(self._geometry, "symmetric", ())) if self._geometry is not None else ()
-        flips = {}
         if not any(sym):
-            return pts, flips
-        w = pts.copy()
-        for d, on in enumerate(sym):
-            if on:
-                flips[d] = w[:, d] < 0.0
-                w[:, d] = np.abs(w[:, d])
-                w[w[:, d] == 0.0, d] = 1e-12
-        return w, flips
+            return pts, {}
+        return wrap_symmetric(pts, sym, [float(a[0]) for a in self._mesh.axes])
 
     def _get_voltage(self, dst_mesh, interpolation="linear"):
         """Potential on a destination mesh (electr3d.cpp:507-515): trilinear or the nearest

@@ -334,3 +334,29 @@ class RectangularMesh2D:
     def side(name):
         return {"left": RectangularMesh2D.Left, "right": RectangularMesh2D.Right,
                 "bottom": RectangularMesh2D.Bottom, "top": RectangularMesh2D.Top}[name]()
+
+
+def wrap_symmetric(pts, sym, lows):
+    """Points as a provider reads them along axes where the geometry mirrors at 0
+    (InterpolationFlags::wrap, plask/mesh/interpolation.hpp:232-250, non-periodic branch):
+    a coordinate 0 becomes 1e-12, then, when the geometry lies on the positive side of the
+    axis (its lower bound ``lows[d]`` >= 0), every coordinate reads at its absolute value,
+    otherwise at minus it.  Returns the wrapped points and, per mirrored axis, the mask of
+    points on the other side, whose vector components along that axis change sign
+    (InterpolationFlags::postprocess, interpolation.hpp:272-287)."""
+    flips = {}
+    if not any(sym):
+        return pts, flips
+    w = np.array(pts, dtype=np.float64, copy=True)
+    for d, on in enumerate(sym):
+        if not on:
+            continue
+        x0 = w[:, d].copy()  # postprocess reflects on the coordinate as given
+        x = np.where(x0 == 0.0, 1e-12, x0)
+        if lows[d] >= 0.0:
+            flips[d] = x0 < 0.0
+            w[:, d] = np.abs(x)
+        else:
+            flips[d] = x0 > 0.0
+            w[:, d] = -np.abs(x)
+    return w, flips

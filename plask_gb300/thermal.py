@@ -21,7 +21,7 @@ import logging
 import numpy as np
 
 from . import _native
-from .mesh import RectangularMesh3D, to_mesh_order
+from .mesh import RectangularMesh3D, to_mesh_order, wrap_symmetric
 
 log = logging.getLogger("plask_gb300.thermal")
 
@@ -851,16 +851,9 @@ class Static3D:
         negative coordinate reads at its absolute value.  Returns the wrapped points and, per
         mirrored axis, the mask of reflected points."""
         sym = tuple(getattr(self._geometry, "symmetric", ())) if self._geometry is not None else ()
-        flips = {}
         if not any(sym):
-            return pts, flips
-        w = pts.copy()
-        for d, on in enumerate(sym):
-            if on:
-                flips[d] = w[:, d] < 0.0
-                w[:, d] = np.abs(w[:, d])
-                w[w[:, d] == 0.0, d] = 1e-12
-        return w, flips
+            return pts, {}
+        return wrap_symmetric(pts, sym, [float(a[0]) for a in self._mesh.axes])
 
     def _get_temperatures(self, dst_mesh, interpolation="linear"):
         """Temperatures on a destination mesh (therm3d.cpp:387-395): trilinear or the nearest

@@ -18,7 +18,7 @@ import logging
 import numpy as np
 
 from . import _native
-from .mesh import RectangularMesh2D, mesh_index2d, to_mesh_order2d
+from .mesh import RectangularMesh2D, mesh_index2d, to_mesh_order2d, wrap_symmetric
 from .thermal import (BadInput, BoundaryConditions, IterativeParams, MaterialTable, Provider, _check_interpolation,
                       _element_axis, _nearest_axis, conductivity_elements, load_state, masked_element_interpolate,
                       masked_interpolate, save_state, spline_interpolate)
@@ -338,16 +338,9 @@ class Static2D:
         sym = sym[:2]
         if self._geometry_kind == "cylindrical":
             sym[0] = True
-        flips = {}
         if not any(sym):
-            return pts, flips
-        w = pts.copy()
-        for d, on in enumerate(sym):
-            if on:
-                flips[d] = w[:, d] < 0.0
-                w[:, d] = np.abs(w[:, d])
-                w[w[:, d] == 0.0, d] = 1e-12
-        return w, flips
+            return pts, {}
+        return wrap_symmetric(pts, sym, [float(a[0]) for a in self._mesh.axes])
 
     def _get_temperatures(self, dst_mesh, interpolation="linear"):
         """Temperatures on a destination mesh or points (therm2d.cpp:544-553): bilinear or the

@@ -27,6 +27,9 @@ Fixtures:
 * ``thermoelectric3d_19x19x28``: the ThermoElectric3D loop (thermoelectric.py:181-219):
   electrical compute(6), its Joule heat to the thermal problem, thermal compute(1),
   until both errors are within maxerr, ORDER_012.
+* ``thermoelectric3d_betaT_19x19x28``: the same loop with a temperature-dependent junction
+  beta(T) = 18 (300/T)^1.5, each round's element temperatures fed back into the electrical
+  problem (the thermal -> electrical direction of the coupling).
 """
 from __future__ import annotations
 
@@ -209,6 +212,45 @@ def thermoelectric3d():
     G.save("thermoelectric3d_19x19x28", arr, meta)
 
 
+def element_mean(T):
+    """Element-average temperatures (the 8-node mean) of a canonical node field."""
+    return 0.125 * (T[:-1, :-1, :-1] + T[:-1, :-1, 1:] + T[:-1, 1:, :-1] + T[:-1, 1:, 1:]
+                    + T[1:, :-1, :-1] + T[1:, :-1, 1:] + T[1:, 1:, :-1] + T[1:, 1:, 1:])
+
+
+BETA_T = (18.0, 1.5)  # beta(T) = 18 (300/T)^1.5 1/V
+
+
+def beta_of_t(b0, bp):
+    return lambda T: b0 * (300.0 / T) ** bp
+
+
+def thermoelectric3d_beta_t():
+    """The ThermoElectric3D loop with a temperature-dependent junction beta(T): each round the
+    electrical problem reads the element temperatures of the last thermal solve, as the
+    reference's electrical solver reads its inTemperature receiver (thermoelectric.py:209-211,
+    electr3d.cpp:203-237)."""
+    s = S.shockley_c4(seed=4005, n=(19, 19, 28), voltage=2.2)
+    order, tfreq = "012", 6
+    packed_beta = list(s.beta)
+    s.beta = [beta_of_t(*BETA_T)]
+    p = E.from_structure(s, order=order)
+    tp = O.from_structure(s.thermal, order=order)
+    state, T, rounds = {}, None, []
+    ve, tt = 2 * s.maxerr, 2 * tp.maxerr
+    while tt > tp.maxerr or ve > s.maxerr:
+        p.temperature = np.full(tuple(n - 1 for n in tp.shape), tp.inittemp) if T is None else element_mean(T)
+        V, conds, ve, _ = E.compute(p, loops=tfreq, state=state)
+        tp.heat = E.heat(p, V, conds)
+        T, tt, _ = O.compute(tp, loops=1, T=T)
+        rounds.append([ve, tt])
+    s.beta = packed_beta
+    arr, meta = G.pack_elec(s)
+    arr.update(T_cholesky=T, V_cholesky=V)
+    meta.update(kind="thermoelectric3d", order=order, tfreq=tfreq, rounds=rounds, beta_T=list(BETA_T))
+    G.save("thermoelectric3d_betaT_19x19x28", arr, meta)
+
+
 def main():
     if not N.available():
         raise SystemExit("oracle/_ref/libnspcg_ref.so is not built: make -C oracle ref (needs the reference tree)")
@@ -221,6 +263,7 @@ def main():
     dynamiccyl()
     shockley3d()
     thermoelectric3d()
+    thermoelectric3d_beta_t()
     for n in G.names():
         print(n, (HERE / f"{n}.npz").stat().st_size, "bytes")
 

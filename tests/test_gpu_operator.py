@@ -48,17 +48,24 @@ def test_mult_matches_oracle_matrix(kind, order, after_loop):
     assert np.max(np.abs(y32 - ref)) <= 2e-5 * scale
 
 
-# Meshes the TMA-staged CG kernel takes (n0 a multiple of 4, at most 224): one to seven
-# warps along x, partial row tiles, several z-chunks, convective top faces (surface rows in
-# one plane) and side conditions (surface rows in every plane).
-@pytest.mark.parametrize("shape,kind,order", [
-    ((36, 33, 21), "aniso", "201"),
-    ((40, 23, 17), "iso", "012"),
-    ((128, 20, 30), "aniso", "201"),
-    ((200, 12, 10), "aniso", "120"),
-    ((8, 9, 7), "iso", "210"),
+# Meshes the TMA-staged CG kernel takes: one to four warps along x (64, 128, 192 and 248
+# columns: one or two copy regions), partial row tiles, several z-chunks, convective top
+# faces (surface rows in one plane) and side conditions (surface rows in every plane); and,
+# with PLGPU_TMA_ALWAYS=1, widths it fills only partly (36, 40, 200 and 8 columns), which
+# the solver leaves to the register-march kernel by default.
+@pytest.mark.parametrize("shape,kind,order,always", [
+    ((64, 20, 13), "aniso", "201", False),
+    ((128, 20, 30), "aniso", "201", False),
+    ((192, 9, 8), "iso", "012", False),
+    ((248, 6, 7), "aniso", "120", False),
+    ((36, 33, 21), "aniso", "201", True),
+    ((40, 23, 17), "iso", "012", True),
+    ((200, 12, 10), "aniso", "120", True),
+    ((8, 9, 7), "iso", "210", True),
 ])
-def test_cg_operator_matches_oracle_matrix(shape, kind, order):
+def test_cg_operator_matches_oracle_matrix(shape, kind, order, always, monkeypatch):
+    if always:
+        monkeypatch.setenv("PLGPU_TMA_ALWAYS", "1")
     if kind == "iso":
         s = S.layered_c0(seed=23, n=shape)
         s.convection = [("top", 50.0, 300.0)]
@@ -86,8 +93,9 @@ def test_cg_operator_matches_oracle_matrix(shape, kind, order):
     assert abs(xax - ref_xax) <= 1e-5 * abs(ref_xax)
 
 
-def test_cg_operator_falls_back_on_unaligned_meshes():
-    s = S.layered_c1(seed=24, n=(35, 17, 12))  # 35 columns: row stride not a multiple of 16 bytes
+@pytest.mark.parametrize("n0", [35, 200])  # a row stride that is no multiple of 16 bytes; 78 % of the columns
+def test_cg_operator_falls_back_on_unaligned_or_underfilled_meshes(n0):
+    s = S.layered_c1(seed=24, n=(n0, 17, 12))
     sv = TH.solver_for_structure(s, ordering="201", algorithm="gpu-mixed")
     sv.compute(1)
     T = sv._full_temperature()

@@ -25,10 +25,10 @@ CASES = [
     ("c0-012", lambda: S.layered_c0(seed=4, n=(9, 9, 14)), "012"),
     ("c1", lambda: S.layered_c1(seed=5, n=(12, 10, 18)), "201"),
     ("c1-210", lambda: S.layered_c1(seed=6, n=(11, 13, 15)), "210"),
-    # x-widths the TMA-staged operator and its CG take (a multiple of 4): two warps along
-    # x, several row tiles and z-chunks
-    ("c1-wide", lambda: S.layered_c1(seed=7, n=(36, 14, 20)), "201"),
-    ("c0-wide", lambda: S.layered_c0(seed=9, n=(40, 12, 22)), "120"),
+    # x-widths the TMA-staged operator and its CG take: one and two warps along x,
+    # several row tiles and z-chunks
+    ("c1-wide", lambda: S.layered_c1(seed=7, n=(64, 14, 20)), "201"),
+    ("c0-wide", lambda: S.layered_c0(seed=9, n=(128, 10, 12)), "120"),
 ]
 
 
@@ -103,9 +103,13 @@ def _mesa_with_faces(seed, n):
     return s
 
 
-@pytest.mark.parametrize("algorithm", ["gpu-mixed", "gpu-pcg"])
+@pytest.mark.parametrize("algorithm,always", [("gpu-mixed", False), ("gpu-pcg", False), ("gpu-mixed", True)])
 @pytest.mark.parametrize("order", ["201", "012"])
-def test_masked_mesh_with_face_conditions_matches_oracle(order, algorithm):
+def test_masked_mesh_with_face_conditions_matches_oracle(order, algorithm, always, monkeypatch):
+    # always: the TMA operator and its CG on this 12-column mesh too (surface rows on the
+    # top, right and front faces, masked-out nodes)
+    if always:
+        monkeypatch.setenv("PLGPU_TMA_ALWAYS", "1")
     """Full compute() with a masked mesh and heat-flux, convective and radiative faces in
     the reference's placement (face terms on element corners 0-3, radiation reading the
     temperatures of global nodes 0-7), against the oracle."""

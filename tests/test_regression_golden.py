@@ -26,6 +26,22 @@ TOL_V = 1e-9  # V
 FIXTURES = G.names()
 
 
+def _element_mean(T):
+    """Element-average temperatures (the 8-node mean) of a canonical node field."""
+    return 0.125 * (T[:-1, :-1, :-1] + T[:-1, :-1, 1:] + T[:-1, 1:, :-1] + T[:-1, 1:, 1:]
+                    + T[1:, :-1, :-1] + T[1:, :-1, 1:] + T[1:, 1:, :-1] + T[1:, 1:, 1:])
+
+
+def _elec_structure(data, meta):
+    """An electrical fixture's structure; a stored beta(T) = b0 (300/T)^bp becomes the callable
+    the solvers evaluate at the element temperatures (electr_python.cpp:104-111)."""
+    s = G.unpack_elec(data, meta)
+    if meta.get("beta_T"):
+        b0, bp = meta["beta_T"]
+        s.beta = [lambda T, b0=b0, bp=bp: b0 * (300.0 / T) ** bp for _ in s.beta]
+    return s
+
+
 def _problem2d(s, meta):
     mats = O.Materials(s.k300, s.p, s.kz_ratio, s.hexp, s.empty)
     mesh = RectangularMesh2D(*s.axes, ordering=meta["order"])
@@ -89,12 +105,14 @@ def test_oracle_replays_fixture(name):
         assert _same_nan(T, data["T_direct"]) and _maxdiff(T, data["T_direct"]) <= 1e-9
         assert steps == meta["steps"] and elaps == pytest.approx(meta["elapsed"], abs=1e-12)
     elif kind == "thermoelectric3d":
-        s = G.unpack_elec(data, meta)
+        s = _elec_structure(data, meta)
         p = E.from_structure(s, order=meta["order"])
         tp = O.from_structure(s.thermal, order=meta["order"])
         state, T, n = {}, None, 0
         ve, tt = 2 * s.maxerr, 2 * tp.maxerr
         while tt > tp.maxerr or ve > s.maxerr:
+            # the electrical problem reads the last thermal solve's element temperatures
+            p.temperature = np.full(tuple(k - 1 for k in tp.shape), tp.inittemp) if T is None else _element_mean(T)
             V, conds, ve, _ = E.compute(p, loops=meta["tfreq"], state=state)
             tp.heat = E.heat(p, V, conds)
             T, tt, _ = O.compute(tp, loops=1, T=T)
@@ -227,12 +245,13 @@ def test_gpu_shockley3d_matches_fixture():
 
 
 @pytest.mark.gpu
-def test_gpu_thermoelectric3d_matches_fixture():
+@pytest.mark.parametrize("name", ["thermoelectric3d_19x19x28", "thermoelectric3d_betaT_19x19x28"])
+def test_gpu_thermoelectric3d_matches_fixture(name):
     from plask_gb300 import electrical as EL
     from plask_gb300 import thermal as TH
 
-    data, meta = G.load("thermoelectric3d_19x19x28")
-    s = G.unpack_elec(data, meta)
+    data, meta = G.load(name)
+    s = _elec_structure(data, meta)
     te = EL.ThermoElectric3D()
     te.thermal = TH.solver_for_structure(s.thermal, ordering=meta["order"], algorithm="gpu-mixed")
     te.electrical = EL.solver_for_structure(s, ordering=meta["order"], algorithm="gpu-mixed")
