@@ -213,6 +213,78 @@ def layered_c1(seed=1000, n=(128, 128, 200), power=1e16, n_layers=12):
                      name=f"layered-aniso-{n[0]}x{n[1]}x{n[2]}-s{seed}")
 
 
+def learned_c2(seed=2000, n=None, oxide_factor=1e-2):
+    """Structures of the learned preconditioner's configuration: 8..40 random layers on the
+    150 um substrate (thickness log-uniform in 0.05..3 um, k300 log-uniform in 1..150 W/mK,
+    p in 0.5..1.5, k_z / k_xy in 0.5..1), a cylindrical mesa of radius 5..30 um about
+    x = y = 0 etched through the upper part of the layers (EMPTY outside it: a masked mesh),
+    an annular oxide aperture inside the mesa -- one layer whose material between the
+    aperture radius and the mesa radius has ``oxide_factor`` times its host's conductivity
+    (the reference's HollowCylinder, plask/geometry/cylinder.hpp:95), a contrast of up to
+    1e3 against the other layers -- and 1..3 Gaussian heat blobs in the aperture, their total
+    power scaled to a temperature rise of the order of 40 K.  Grids
+    of 96..160 nodes per axis (``n`` overrides), multiples of 4; bottom at 300 K, the other
+    faces adiabatic, the quarter device mirrored in x and y."""
+    rng = np.random.default_rng(seed)
+    if n is None:
+        n = tuple(int(4 * round(rng.uniform(96, 160) / 4)) for _ in range(3))
+    n_layers = min(int(rng.integers(8, 41)), _fit_layers(n, 40))
+    thick = np.exp(rng.uniform(math.log(0.05), math.log(3.0), n_layers))
+    x0 = graded_axis(n[0])
+    x1 = graded_axis(n[1])
+    z, layer_of = vertical_axis(thick, n[2])
+    n_lay = n_layers + 1  # substrate + layers
+    k300 = np.exp(rng.uniform(math.log(1.0), math.log(150.0), n_lay))
+    pexp = rng.uniform(0.5, 1.5, n_lay)
+    kz = rng.uniform(0.5, 1.0, n_lay)
+    mesa_r = rng.uniform(5.0, 30.0)
+    first_etched = int(rng.integers(max(1, n_layers // 2), n_layers)) + 1  # layer ids first_etched..n_layers
+    ox_layer = int(rng.integers(first_etched, n_layers + 1))
+    ap_r = rng.uniform(0.2, 0.7) * mesa_r
+    ox_id, empty_id = n_lay, n_lay + 1
+    k300 = np.append(k300, [k300[ox_layer] * oxide_factor, 0.026])
+    pexp = np.append(pexp, [pexp[ox_layer], 0.0])
+    kz = np.append(kz, [kz[ox_layer], 1.0])
+    empty = np.zeros(n_lay + 2, bool)
+    empty[empty_id] = True
+    xm = 0.5 * (x0[1:] + x0[:-1])
+    ym = 0.5 * (x1[1:] + x1[:-1])
+    zm = 0.5 * (z[1:] + z[:-1])
+    r = np.sqrt(xm[None, :] ** 2 + ym[:, None] ** 2)  # (n1 - 1, n0 - 1)
+    mat = np.broadcast_to(layer_of[:, None, None], (n[2] - 1, n[1] - 1, n[0] - 1)).astype(np.int32).copy()
+    etched = layer_of >= first_etched
+    mat[etched] = np.where(r > mesa_r, empty_id, mat[etched])
+    ox = layer_of == ox_layer
+    mat[ox] = np.where((r > ap_r) & (r <= mesa_r), ox_id, mat[ox])
+    # heat: 1..3 Gaussian blobs near the aperture layer, inside the aperture
+    heat = np.zeros(mat.shape)
+    z_ox = 0.5 * (z[np.flatnonzero(ox)[0]] + z[np.flatnonzero(ox)[-1] + 1])
+    for _ in range(int(rng.integers(1, 4))):
+        ang = rng.uniform(0.0, 0.5 * math.pi)
+        rad = rng.uniform(0.0, 0.8) * ap_r
+        cx, cy = rad * math.cos(ang), rad * math.sin(ang)
+        cz = z_ox + rng.uniform(-1.0, 1.0)
+        sxy, sz = rng.uniform(1.0, 4.0), rng.uniform(0.2, 1.0)
+        peak = rng.uniform(0.5, 2.0)  # relative weights; the total is scaled below
+        g = np.exp(-((xm[None, None, :] - cx) ** 2 + (ym[None, :, None] - cy) ** 2) / (2 * sxy ** 2)
+                   - (zm[:, None, None] - cz) ** 2 / (2 * sz ** 2))
+        heat += peak * g
+    heat[mat == empty_id] = 0.0
+    # total power of the quarter device scaled so that the heat would raise a half-space of the
+    # weaker of the substrate and the blobs' host layer by about 40 K at 300 K through a 4 um
+    # disc (dT = P / (pi k r) for the full disc: P_quarter = dT pi k r / 4), which keeps the
+    # k(T) loop away from thermal runaway whatever the drawn conductivities
+    vol = (np.diff(z)[:, None, None] * np.diff(x1)[None, :, None] * np.diff(x0)[None, None, :]) * 1e-18
+    k_weak = min(k300[0], k300[ox_layer])
+    target = 40.0 * math.pi * k_weak * 4e-6 / 4.0
+    total = float((heat * vol).sum())
+    if total > 0:
+        heat *= target / total
+    return Structure(axes=(x0, x1, z), mat=np.ascontiguousarray(mat), k300=k300, p=pexp, kz_ratio=kz,
+                     hexp=np.zeros(k300.size), empty=empty, heat=heat, temperature=[("bottom", 300.0)],
+                     name=f"learned_c2-{seed}")
+
+
 def sweep_c3(seed=3000, count=256, lo=32, hi=96, power=(1e15, 1e16)):
     """Batched sweep: ``count`` layered structures with per-axis node counts
     uniform in [lo, hi] and source power uniform in ``power`` W/m^3.
