@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-coupled", action="store_true", help="skip the coupled thermo-electric record")
     ap.add_argument("--no-sweep", action="store_true", help="skip the batched-sweep record")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner record")
+    ap.add_argument("--learned-weights", default=None, help="weights file of the learned record (default: shipped)")
+    ap.add_argument("--learned-seed", type=int, default=2001)
     ap.add_argument("--sweep-record-count", type=int, default=64)
     ap.add_argument("--sweep-record-sequential", type=int, default=8)
     ap.add_argument("--workload", default="layered", choices=["layered", "sweep"])
@@ -436,6 +439,53 @@ def sweep_record(count, sequential, algorithm="gpu-mixed", loops=30):
             "max_dT_batched_vs_one_at_a_time_K": dT}
 
 
+def learned_record(weights=None, seed=2001):
+    """The learned preconditioner on a structure of its own family (structures.learned_c2,
+    not one of the training seeds): the learned flexible CG inside the mixed-precision
+    refinement (gpu-learned), the Jacobi-PCG mixed solve (gpu-mixed) and plain FP64
+    Jacobi-PCG (gpu-pcg), each a full compute() from 300 K (device time of the second of
+    two runs), with CG iterations, fallbacks to Jacobi-PCG and max |dT| against the plain
+    FP64 answer."""
+    import numpy as np
+
+    from plask_gb300 import learned as LN
+    from plask_gb300 import structures as S
+    from plask_gb300 import thermal as TH
+
+    path = pathlib.Path(weights) if weights else LN.WEIGHTS_C2
+    net = LN.load_c2(path)
+    s = S.learned_c2(seed=seed)
+
+    def run(algo, reps):
+        for _ in range(reps):
+            sv = TH.solver_for_structure(s, algorithm=algo)
+            if algo == "gpu-learned":
+                sv.preconditioner = net
+            sv.compute()
+        st = sv.stats
+        rec = {"s_per_solve": st["total_ms"] / 1e3, "solves_per_s": 1e3 / st["total_ms"], "outer_loops": st["loops"],
+               "cg_iterations": st["inner_iterations"], "us_per_iteration": 1e3 * st["total_ms"] / st["inner_iterations"]}
+        if algo == "gpu-learned":
+            rec["fallbacks"] = st.get("fallbacks")
+        return rec, sv._full_temperature()
+
+    plain, T_plain = run("gpu-pcg", 1)
+    mixed, T_mixed = run("gpu-mixed", 2)
+    learned, T_learned = run("gpu-learned", 2)
+    mixed["max_dT_vs_plain_fp64_K"] = float(np.nanmax(np.abs(T_mixed - T_plain)))
+    learned["max_dT_vs_plain_fp64_K"] = float(np.nanmax(np.abs(T_learned - T_plain)))
+    learned["max_dT_vs_jacobi_mixed_K"] = float(np.nanmax(np.abs(T_learned - T_mixed)))
+    n = [len(a) for a in s.axes]
+    return {"workload": f"learned_c2 seed {seed}: {n[0]}x{n[1]}x{n[2]} nodes, {len(s.k300)} materials, etched mesa, "
+                        f"oxide aperture at 1e-2, Gaussian heat blobs; bottom 300 K, maxerr {s.maxerr} K",
+            "weights": f"{path.name}: 4-level U-Net trained on {len(LN.TRAIN_SEEDS) * LN.STEPS_PER_STRUCTURE} "
+                       f"residual->error pairs from {len(LN.TRAIN_SEEDS)} learned_c2 structures",
+            "learned": learned, "jacobi_mixed": mixed, "plain_fp64": plain,
+            "learned_speedup_vs_plain_fp64": plain["s_per_solve"] / learned["s_per_solve"],
+            "jacobi_mixed_speedup_vs_plain_fp64": plain["s_per_solve"] / mixed["s_per_solve"],
+            "learned_speedup_vs_jacobi_mixed": mixed["s_per_solve"] / learned["s_per_solve"]}
+
+
 def run_sweep(args):
     """Batched sweep: one-at-a-time vs concurrent solves of the uneven-size sweep."""
     # more hardware work queues than the default 8, so that up to 32 solver streams
@@ -634,7 +684,12 @@ def main():
                 "l2_resident_ms_per_launch": ms_l2,
                 "fp64_ms_per_launch": ms64, "fp64_achieved_gbs": by64 / (ms64 * 1e-3) / 1e9}
 
-    coupled = sweep = None
+    coupled = sweep = learned = None
+    if dist.rank == 0 and not args.no_learned:
+        try:
+            learned = learned_record(args.learned_weights, args.learned_seed)
+        except Exception as e:  # reported, not required
+            learned = {"failed": str(e)}
     if dist.rank == 0 and not args.no_coupled:
         try:
             coupled = coupled_record()
@@ -674,6 +729,7 @@ def main():
                 "ms_per_step": 1e3 * statistics.mean(e2e_times)},
         "gpu_launches": int(sum(st["kernel_launches"] for st in stats)),
         "roofline": roofline,
+        "learned": learned,
         "coupled": coupled,
         "sweep": sweep,
         "clocks": clocks,

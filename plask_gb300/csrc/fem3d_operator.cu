@@ -555,14 +555,23 @@ static void op_grid(const LaunchCfg& c, int n0, int n1, int n2, bool fp64, dim3&
     const int gx = (n0 + 29) / 30;
     const int gy = (n1 + rows * kWarps - 1) / (rows * kWarps);
     // z-chunks: fill whole waves of resident blocks (4 per SM in FP32, 2 in FP64),
-    // each chunk at least 8 planes (one extra element layer is recomputed per chunk)
+    // each chunk at least 8 planes (one extra element layer is recomputed per chunk).
+    // A mesh whose columns cannot fill one wave with 8-plane chunks takes shorter
+    // chunks (down to 4 planes) up to one wave, and then every chunk it has.
     const int resident = max(1, c.sm_count * (fp64 ? 2 : 4) / max(1, c.op_share));
-    const int maxchunks = max(1, (n2 + 7) / 8);
+    const int columns = gx * gy;
+    int maxchunks = max(1, (n2 + 7) / 8);
+    if ((long long)columns * maxchunks < resident)
+        maxchunks = max(maxchunks, min((n2 + 3) / 4, (resident + columns - 1) / columns));
     int chunks = 1;
-    for (int waves = 1; waves <= 8; ++waves) {
-        const int want = (waves * resident) / (gx * gy);
-        if (want >= 1 && want <= maxchunks) chunks = want;
-        if (want > maxchunks) break;
+    if ((long long)columns * maxchunks <= resident) {
+        chunks = maxchunks;
+    } else {
+        for (int waves = 1; waves <= 8; ++waves) {
+            const int want = (waves * resident) / columns;
+            if (want > maxchunks) break;
+            if (want >= 1) chunks = want;
+        }
     }
     while ((long long)gx * gy * chunks > kMaxPartialBlocks - 256) --chunks;
     zchunk = (n2 + chunks - 1) / chunks;

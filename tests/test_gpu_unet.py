@@ -103,17 +103,46 @@ def test_training_lowers_the_loss_and_weights_round_trip(tmp_path):
         other.load(bad)
 
 
-def test_learned_solve_matches_and_reports_its_gain():
-    """The learned solve reaches the Jacobi-PCG answer (max |dT| <= 1e-6 K, same
-    outer loops).  Its gain in inner iterations is printed, and it may not lose more
-    than 15 % against Jacobi-PCG: the network trained here (a few hundred steps on
-    one structure) does not yet remove iterations on this layered case."""
-    s = S.layered_c1(seed=43, n=(64, 64, 56))
-    order = "201"
-    net = _native.UNet(seed=4)
-    trainer = TH.solver_for_structure(s, ordering=order, algorithm="gpu-learned")
-    trainer.initialize()
-    net.train(trainer._fem, steps=400, lr=2e-3, seed=6, smooth=(20, 300), pairs="cg")
+def _active_nodes(s):
+    """Canonical (n2, n1, n0) mask of the nodes touched by a non-EMPTY element."""
+    act = ~np.asarray(s.empty)[s.mat]
+    out = np.zeros(s.shape, bool)
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                out[dz:dz + act.shape[0], dy:dy + act.shape[1], dx:dx + act.shape[2]] |= act
+    return out
+
+
+def test_shipped_network_gain_on_config2():
+    """The shipped network (plask_gb300.learned: 20 000 residual -> error pairs from ten
+    learned_c2 structures, seeds 2100..2109) on a held-out structure of its family
+    (seed 2002, 96x96x96 nodes).
+
+    Gain per application, asserted: on smooth errors the trained network's correction
+    leaves at most 60 % of the A-norm error that the untrained network's leaves (the
+    loss is one minus the squared A-cosine between the correction and the error).
+
+    The solve: the learned flexible CG reaches the Jacobi-PCG answer (max |dT| <= 1e-6 K,
+    same outer loops).  It does not cut the CG iterations on this family -- the network
+    captures most of a Jacobi-smoothed error's energy but only a few per cent of what
+    Jacobi-PCG leaves after a few hundred iterations -- so the iteration counts are
+    printed and bounded (at most 15 % above Jacobi-PCG), not claimed as a gain."""
+    from plask_gb300 import learned as LN
+
+    s = S.learned_c2(seed=2002, n=(96, 96, 96))
+    order = "210"  # mesh order == canonical order
+    net = LN.load_c2()
+    fresh = _native.UNet(seed=11)
+    sv = TH.solver_for_structure(s, ordering=order, algorithm="gpu-learned")
+    sv.initialize()
+    mask = _active_nodes(s)
+    mask[0] = False  # the Dirichlet bottom
+    val = [(_smooth_error(s.shape, 300 + k) * mask).ravel() for k in range(4)]
+    trained = float(np.mean([net.loss_grad(sv._fem, e)[0] for e in val]))
+    untrained = float(np.mean([fresh.loss_grad(sv._fem, e)[0] for e in val]))
+    print("validation loss: trained", trained, "untrained", untrained)
+    assert trained <= 0.6 * untrained
 
     base = TH.solver_for_structure(s, ordering=order, algorithm="gpu-mixed")
     base.compute()
@@ -124,5 +153,5 @@ def test_learned_solve_matches_and_reports_its_gain():
     print("jacobi iterations", base.stats["inner_iterations"], "learned", learned.stats["inner_iterations"],
           "fallbacks", learned.stats["fallbacks"], "ms", base.stats["total_ms"], learned.stats["total_ms"])
     assert learned.stats["loops"] == base.stats["loops"]
-    assert np.max(np.abs(T1 - T0)) <= 1e-6
+    assert np.nanmax(np.abs(T1 - T0)) <= 1e-6
     assert learned.stats["inner_iterations"] <= 1.15 * base.stats["inner_iterations"]
