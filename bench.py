@@ -444,7 +444,9 @@ def learned_record(weights=None, seed=2001):
     not one of the training seeds): the learned flexible CG inside the mixed-precision
     refinement (gpu-learned), the Jacobi-PCG mixed solve (gpu-mixed) and plain FP64
     Jacobi-PCG (gpu-pcg), each a full compute() from 300 K (device time of the second of
-    two runs), with CG iterations, fallbacks to Jacobi-PCG and max |dT| against the plain
+    two runs), with CG iterations (those of the learned flexible CG and those of the
+    Jacobi-PCG that finishes a correction after a fallback), the device time of one network
+    forward pass and of one preconditioner application, and max |dT| against the plain
     FP64 answer."""
     import numpy as np
 
@@ -467,6 +469,11 @@ def learned_record(weights=None, seed=2001):
                "cg_iterations": st["inner_iterations"], "us_per_iteration": 1e3 * st["total_ms"] / st["inner_iterations"]}
         if algo == "gpu-learned":
             rec["fallbacks"] = st.get("fallbacks")
+            rec["learned_fcg_iterations"] = st.get("learned_iterations")
+            rec["jacobi_fallback_iterations"] = st["inner_iterations"] - st.get("learned_iterations", 0)
+            fwd, app = net.time_apply(sv._fem, reps=20)
+            rec["network_forward_us"] = 1e3 * fwd
+            rec["preconditioner_apply_us"] = 1e3 * app
         return rec, sv._full_temperature()
 
     plain, T_plain = run("gpu-pcg", 1)

@@ -90,6 +90,8 @@ typedef struct plgpu_stats {
     double solve_ms;        /* device time of the linear solves [ms] */
     double total_ms;        /* device time of the whole call [ms] */
     long long kernel_launches; /* CUDA kernels this library launched during the call */
+    int learned_iterations; /* inner iterations of the flexible CG with the learned preconditioner
+                               (the rest of inner_iterations: Jacobi-PCG, after fallbacks) */
 } plgpu_stats;
 
 /* Create a solver on a rectilinear mesh.  Replaces mesh setup and

@@ -63,6 +63,11 @@ int plgpu_unet_loss_grad(plgpu_unet* net, plgpu_fem3d* fem, const double* e, dou
 /* Apply the preconditioner to a residual (full node arrays, mesh order). */
 int plgpu_unet_apply(plgpu_unet* net, plgpu_fem3d* fem, const double* r, double* z);
 
+/* Device time [ms] of one network forward pass and of one whole preconditioner
+   application (forward, A v, two dot products, combination) on the handle's mesh,
+   averaged over reps after one untimed pass (CUDA events on the solver's stream). */
+int plgpu_unet_time_apply(plgpu_unet* net, plgpu_fem3d* fem, int reps, double* forward_ms, double* apply_ms);
+
 /* Attach the network to a solver handle (NULL detaches); used by PLGPU_ALGO_GPU_LEARNED.
    The handle keeps a pointer: the network must outlive the attachment. */
 int plgpu_fem3d_set_preconditioner(plgpu_fem3d* fem, plgpu_unet* net);

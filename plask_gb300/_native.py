@@ -42,6 +42,7 @@ class Stats(C.Structure):
         ("solve_ms", C.c_double),
         ("total_ms", C.c_double),
         ("kernel_launches", C.c_longlong),
+        ("learned_iterations", C.c_int),
     ]
 
     def as_dict(self):
@@ -95,6 +96,7 @@ SIGNATURES = {
                                    C.POINTER(C.c_float)]),
     "plgpu_unet_loss_grad": (C.c_int, [_h, _h, _dp, _dp, C.POINTER(C.c_float), _dp, _dp]),
     "plgpu_unet_apply": (C.c_int, [_h, _h, _dp, _dp]),
+    "plgpu_unet_time_apply": (C.c_int, [_h, _h, C.c_int, _dp, _dp]),
     "plgpu_fem3d_set_preconditioner": (C.c_int, [_h, _h]),
     "plgpu_fem3d_mult": (C.c_int, [_h, C.c_int, _dp, _dp]),
     "plgpu_fem3d_mult_noalloc": (C.c_int, [_h, C.c_int, _dp, _dp]),
@@ -691,6 +693,12 @@ class UNet:
         z = np.empty_like(r)
         self._check(self._lib.plgpu_unet_apply(self._h, fem._h, _ptr(r, C.c_double), _ptr(z, C.c_double)), fem)
         return z
+
+    def time_apply(self, fem, reps=20):
+        """(forward ms, whole preconditioner application ms), device time on ``fem``'s mesh."""
+        a, b = C.c_double(0.0), C.c_double(0.0)
+        self._check(self._lib.plgpu_unet_time_apply(self._h, fem._h, int(reps), C.byref(a), C.byref(b)), fem)
+        return a.value, b.value
 
 
 def attach_preconditioner(fem, net):

@@ -262,6 +262,7 @@ struct plgpu_fem3d {
     std::unique_ptr<UNetWork> uw;
     DevBuf z32, t32, v32, av32, dscal, dpart;  // z, training scratch, network direction v and A v, scalars
     int fallbacks = 0;
+    long long learned_iters = 0;  // CG iterations run with the learned preconditioner
 
     bool initialized = false;
     int loopno = 0;
@@ -1612,6 +1613,43 @@ struct plgpu_fem3d {
         f32_to_host(z32.as<float>(), z);
     }
 
+    // Device time (CUDA events on the solver's stream, averaged over reps after one untimed
+    // pass) of one network forward pass (input scaling, the U-Net, the head) and of one whole
+    // preconditioner application (forward, A v, (v, r), (v, A v), z = M^-1 r + c v), on a
+    // residual of ones at the current temperature's matrix.
+    void time_net(plgpu_unet* net, int reps, double* fwd_ms, double* pre_ms) {
+        if (reps <= 0) throw ArgError("reps must be positive");
+        prepare_matrix();
+        std::vector<double> ones((size_t)N, 1.0);
+        host_to_f32(ones.data(), r32v.as<float>());
+        double* sc = dscal.as<double>();
+        launch_rmr(cfg, N, r32v.as<float>(), minv32.as<float>(), dpart.as<double>(), sc);
+        const UNetModel& M = net->model;
+        float tf = 0.f, tp = 0.f;
+        for (int k = -1; k < reps; ++k) {
+            float a = 0.f, b2 = 0.f;
+            ck(cudaEventRecord(ev2, stream), "event");
+            launch_unet_input(cfg, N, r32v.as<float>(), minv32.as<float>(), sc, uw->feat);
+            HeadArgs h = unet_head_args(M, *uw, r32v.as<float>(), minv32.as<float>(), sc, v32.as<float>());
+            unet_forward(cfg, M, *uw, &h);
+            ck(cudaEventRecord(ev3, stream), "event");
+            ck(cudaEventSynchronize(ev3), "sync");
+            ck(cudaEventElapsedTime(&a, ev2, ev3), "elapsed");
+            ck(cudaEventRecord(ev2, stream), "event");
+            precond(M, r32v.as<float>(), z32.as<float>(), sc);
+            ck(cudaEventRecord(ev3, stream), "event");
+            ck(cudaEventSynchronize(ev3), "sync");
+            ck(cudaEventElapsedTime(&b2, ev2, ev3), "elapsed");
+            if (k >= 0) {
+                tf += a;
+                tp += b2;
+            }
+        }
+        ck(cudaGetLastError(), "launch");
+        *fwd_ms = tf / reps;
+        *pre_ms = tp / reps;
+    }
+
     // Inner FP32 solve with flexible CG and the network; Jacobi-PCG takes over from the
     // current iterate when the flexible CG stagnates or breaks down.
     void fcg_inner(int& st, int& it, int cap) {
@@ -1635,6 +1673,7 @@ struct plgpu_fem3d {
             }
         };
         run_chunks(2, 4, 16, enqueue, st, it, cap);
+        learned_iters += it;
         if (st == SOLVE_STAGNATED || st == SOLVE_BREAKDOWN || (st == SOLVE_MAXIT && it < cap)) {
             ++fallbacks;
             int st2 = 0, it2 = 0;
@@ -1655,6 +1694,7 @@ struct plgpu_fem3d {
         if (bc_dirty) materialize_bc();
         const long long launches0 = thread_launch_count();
         const int fallbacks0 = fallbacks;
+        const long long learned0 = learned_iters;
         ck(cudaEventRecord(ev0, stream), "event");
         if (heat_dirty) build_static_load();
         log(3, "Running thermal calculations");
@@ -1731,6 +1771,7 @@ struct plgpu_fem3d {
             st->refinements = total_ref;
             st->converged = converged ? 1 : 0;
             st->fallbacks = fallbacks - fallbacks0;
+            st->learned_iterations = (int)(learned_iters - learned0);
             st->err = err;
             st->toterr = toterr;
             st->max_t = maxT;
@@ -1843,6 +1884,7 @@ struct plgpu_fem3d {
         upload(d_dens, dens_tab, stream);
         const long long launches0 = thread_launch_count();
         const int fallbacks0 = fallbacks;
+        const long long learned0 = learned_iters;
         ck(cudaEventRecord(ev0, stream), "event");
         if (heat_dirty) build_static_load();
         invalidate_graphs();  // captured solves carry the operator without the capacity shift
@@ -1941,6 +1983,7 @@ struct plgpu_fem3d {
             st->refinements = total_ref;
             st->converged = converged ? 1 : 0;
             st->fallbacks = fallbacks - fallbacks0;
+            st->learned_iterations = (int)(learned_iters - learned0);
             st->err = 0.0;
             st->toterr = 0.0;
             st->max_t = maxT;
@@ -2430,6 +2473,7 @@ struct plgpu_elec3d : plgpu_fem3d {
         upload_info();
         const long long launches0 = thread_launch_count();
         const int fallbacks0 = fallbacks;
+        const long long learned0 = learned_iters;
         ck(cudaEventRecord(ev0, stream), "event");
         if (heat_dirty) build_static_load();  // zero load: no sources in the electrical problem
         log(3, "Running electrical calculations");
@@ -2508,6 +2552,7 @@ struct plgpu_elec3d : plgpu_fem3d {
             st->refinements = total_ref;
             st->converged = converged ? 1 : 0;
             st->fallbacks = fallbacks - fallbacks0;
+            st->learned_iterations = (int)(learned_iters - learned0);
             st->err = err;
             st->toterr = toterr;
             st->max_t = mcur;
@@ -2994,6 +3039,15 @@ int plgpu_unet_apply(plgpu_unet* net, plgpu_fem3d* fem, const double* r, double*
         if (!r || !z) throw ArgError("null argument");
         if (fem->planar) throw ArgError("the learned preconditioner is 3D only");
         fem->apply_net(net, r, z);
+    });
+}
+
+int plgpu_unet_time_apply(plgpu_unet* net, plgpu_fem3d* fem, int reps, double* forward_ms, double* apply_ms) {
+    if (!net) return PLGPU_ERR_ARG;
+    return guarded(fem, [&] {
+        if (!forward_ms || !apply_ms) throw ArgError("null argument");
+        if (fem->planar) throw ArgError("the learned preconditioner is 3D only");
+        fem->time_net(net, reps, forward_ms, apply_ms);
     });
 }
 
