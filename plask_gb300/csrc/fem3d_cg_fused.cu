@@ -4,9 +4,10 @@
 // the reference's solveMatrix, cholesky_matrix.hpp:90-111 / iterative_matrix.hpp:141-339).
 // An iteration is three kernels:
 //     operator  (k_apply_tma):        q = A p (convective surface rows included), partials of (p, q)
-//     update    (k_tmacg_update):     alpha = rz / (p, q),  x += alpha p,  r -= alpha q,
+//     update    (k_tmacg_update):     alpha = rz / (p, q),  r -= alpha q,
 //                                     partials of (r, M^-1 r), (r, r)
-//     direction (k_tmacg_direction):  rz' = (r, M^-1 r),  beta = rz' / rz,  p = M^-1 r + beta p
+//     direction (k_tmacg_direction):  x += alpha p,  rz' = (r, M^-1 r),  beta = rz' / rz,
+//                                     p = M^-1 r + beta p
 // No kernel waits for its own blocks: every block of the update and direction kernels
 // reduces the previous launch's partials itself, in the same fixed order (so all blocks
 // see the same bits and take the same decision), and block 0 records the scalars.  The
@@ -84,9 +85,7 @@ __global__ void __launch_bounds__(kCgThreads) k_tmacg_start(const TmaCg f, Solve
     }
 }
 
-__device__ __forceinline__ void tmacg_update_one(float& x, float& r, float p, float q, float m, float alpha, float& rz,
-                                                 float& rr) {
-    x += alpha * p;
+__device__ __forceinline__ void tmacg_update_one(float& r, float q, float m, float alpha, float& rz, float& rr) {
     // Dirichlet rows (M^-1 = 0) keep r = 0: the operator leaves A p there
     const float rn = m != 0.f ? r - alpha * q : 0.f;
     r = rn;
@@ -94,8 +93,29 @@ __device__ __forceinline__ void tmacg_update_one(float& x, float& r, float p, fl
     rr += rn * rn;
 }
 
+// r -= alpha q and the partials of (r, M^-1 r), (r, r).  The solution update x += alpha p
+// waits for the direction kernel, which reads p anyway.  The first trip's loads do not
+// depend on alpha and are issued before warp 0 reduces the operator's partials.
 __global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_update(const TmaCg f, SolveCtl* __restrict__ ctl, int q) {
     if (ctl->status2[q] != SOLVE_RUNNING) return;
+    const long long N4 = f.N >> 2, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    float4* r4 = reinterpret_cast<float4*>(f.r);
+    const float4* q4 = reinterpret_cast<const float4*>(f.q);
+    const float4* m4 = reinterpret_cast<const float4*>(f.minv);
+    float4 qn[kUnroll], mn[kUnroll], rn[kUnroll];
+    auto load = [&](long long v0) {
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const long long v = v0 + u * stride;
+            if (v < N4) {
+                qn[u] = q4[v];
+                mn[u] = m4[v];
+                rn[u] = r4[v];
+            }
+        }
+    };
+    load(t0);
     // warp 0 reduces the operator's partials; lane 0 takes the decision for the block
     __shared__ int sh_st;
     __shared__ float sh_alpha;
@@ -124,51 +144,34 @@ __global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_update(
     if (sh_st != SOLVE_RUNNING) return;
     const float alpha = sh_alpha;
     float rzn = 0.f, rr = 0.f;
-    const long long N4 = f.N >> 2, stride = (long long)gridDim.x * blockDim.x;
-    const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    float4* x4 = reinterpret_cast<float4*>(f.x);
-    float4* r4 = reinterpret_cast<float4*>(f.r);
-    const float4* p4 = reinterpret_cast<const float4*>(f.p);
-    const float4* q4 = reinterpret_cast<const float4*>(f.q);
-    const float4* m4 = reinterpret_cast<const float4*>(f.minv);
     // kUnroll groups per trip, all loads issued first; each thread visits its groups in
     // increasing order (a fixed summation order)
     for (long long v0 = t0; v0 < N4; v0 += kUnroll * stride) {
-        float4 pn[kUnroll], qn[kUnroll], mn[kUnroll], xn[kUnroll], rn[kUnroll];
+        if (v0 != t0) load(v0);
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u) {
             const long long v = v0 + u * stride;
             if (v < N4) {
-                pn[u] = p4[v];
-                qn[u] = q4[v];
-                mn[u] = m4[v];
-                xn[u] = x4[v];
-                rn[u] = r4[v];
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
-            const long long v = v0 + u * stride;
-            if (v < N4) {
-                tmacg_update_one(xn[u].x, rn[u].x, pn[u].x, qn[u].x, mn[u].x, alpha, rzn, rr);
-                tmacg_update_one(xn[u].y, rn[u].y, pn[u].y, qn[u].y, mn[u].y, alpha, rzn, rr);
-                tmacg_update_one(xn[u].z, rn[u].z, pn[u].z, qn[u].z, mn[u].z, alpha, rzn, rr);
-                tmacg_update_one(xn[u].w, rn[u].w, pn[u].w, qn[u].w, mn[u].w, alpha, rzn, rr);
-                x4[v] = xn[u];
+                tmacg_update_one(rn[u].x, qn[u].x, mn[u].x, alpha, rzn, rr);
+                tmacg_update_one(rn[u].y, qn[u].y, mn[u].y, alpha, rzn, rr);
+                tmacg_update_one(rn[u].z, qn[u].z, mn[u].z, alpha, rzn, rr);
+                tmacg_update_one(rn[u].w, qn[u].w, mn[u].w, alpha, rzn, rr);
                 r4[v] = rn[u];
             }
         }
     }
     for (long long n = (N4 << 2) + t0; n < f.N; n += stride) {
-        float xn = f.x[n], rn = f.r[n];
-        tmacg_update_one(xn, rn, f.p[n], f.q[n], f.minv[n], alpha, rzn, rr);
-        f.x[n] = xn;
-        f.r[n] = rn;
+        float r1 = f.r[n];
+        tmacg_update_one(r1, f.q[n], f.minv[n], alpha, rzn, rr);
+        f.r[n] = r1;
     }
     float v[2] = {rzn, rr};
     write_partial_f32<2>(v, f.part + kRZ, blockIdx.x);
 }
 
+// x += alpha p with the step of this iteration's update, then rz' = (r, M^-1 r),
+// beta = rz' / rz and p = M^-1 r + beta p unless the solve has stopped.  The first trip's
+// loads are issued before warp 0 reduces the update's partials.
 __global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_direction(const TmaCg f, SolveCtl* __restrict__ ctl, int q) {
     const int st0 = ctl->status2[q];
     if (st0 != SOLVE_RUNNING) {  // pass a final status on to the other parity
@@ -176,13 +179,33 @@ __global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_directi
         return;
     }
     const int ust = ctl->ustatus;
-    if (ust != SOLVE_RUNNING) {
+    if (ust != SOLVE_RUNNING) {  // the update found no valid step: x stays
         if (blockIdx.x == 0 && threadIdx.x == 0) ctl->status2[1 - q] = ctl->status = ust;
         return;
     }
+    const long long N4 = f.N >> 2, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    float4* p4 = reinterpret_cast<float4*>(f.p);
+    float4* x4 = reinterpret_cast<float4*>(f.x);
+    const float4* r4 = reinterpret_cast<const float4*>(f.r);
+    const float4* m4 = reinterpret_cast<const float4*>(f.minv);
+    float4 rn[kUnroll], mn[kUnroll], pn[kUnroll], xn[kUnroll];
+    auto load = [&](long long v0) {
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const long long vv = v0 + u * stride;
+            if (vv < N4) {
+                pn[u] = p4[vv];
+                xn[u] = x4[vv];
+                rn[u] = r4[vv];
+                mn[u] = m4[vv];
+            }
+        }
+    };
+    load(t0);
     // warp 0 reduces the update's partials; lane 0 takes the decision for the block
     __shared__ int sh_st;
-    __shared__ float sh_beta;
+    __shared__ float sh_beta, sh_alpha;
     __shared__ double sh_v[3];
     if (threadIdx.x < 32) {
         double v[2];
@@ -197,6 +220,7 @@ __global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_directi
                 st = SOLVE_CONVERGED;
             sh_st = st;
             sh_beta = (float)(rzn / ctl->rz2[q]);
+            sh_alpha = (float)ctl->alpha;
             sh_v[0] = rzn;
             sh_v[1] = rrn;
             sh_v[2] = m;
@@ -204,28 +228,20 @@ __global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_directi
     }
     __syncthreads();
     int st = sh_st;
-    if (st == SOLVE_RUNNING) {
-        const float beta = sh_beta;
-        const long long N4 = f.N >> 2, stride = (long long)gridDim.x * blockDim.x;
-        const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-        float4* p4 = reinterpret_cast<float4*>(f.p);
-        const float4* r4 = reinterpret_cast<const float4*>(f.r);
-        const float4* m4 = reinterpret_cast<const float4*>(f.minv);
-        for (long long v0 = t0; v0 < N4; v0 += kUnroll * stride) {
-            float4 rn[kUnroll], mn[kUnroll], pn[kUnroll];
+    const bool more = st == SOLVE_RUNNING;
+    const float beta = sh_beta, alpha = sh_alpha;
+    for (long long v0 = t0; v0 < N4; v0 += kUnroll * stride) {
+        if (v0 != t0) load(v0);
 #pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                const long long vv = v0 + u * stride;
-                if (vv < N4) {
-                    rn[u] = r4[vv];
-                    mn[u] = m4[vv];
-                    pn[u] = p4[vv];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                const long long vv = v0 + u * stride;
-                if (vv < N4) {
+        for (int u = 0; u < kUnroll; ++u) {
+            const long long vv = v0 + u * stride;
+            if (vv < N4) {
+                xn[u].x += alpha * pn[u].x;
+                xn[u].y += alpha * pn[u].y;
+                xn[u].z += alpha * pn[u].z;
+                xn[u].w += alpha * pn[u].w;
+                x4[vv] = xn[u];
+                if (more) {
                     pn[u].x = mn[u].x * rn[u].x + beta * pn[u].x;
                     pn[u].y = mn[u].y * rn[u].y + beta * pn[u].y;
                     pn[u].z = mn[u].z * rn[u].z + beta * pn[u].z;
@@ -234,7 +250,11 @@ __global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_directi
                 }
             }
         }
-        for (long long n = (N4 << 2) + t0; n < f.N; n += stride) f.p[n] = f.minv[n] * f.r[n] + beta * f.p[n];
+    }
+    for (long long n = (N4 << 2) + t0; n < f.N; n += stride) {
+        const float pn1 = f.p[n];
+        f.x[n] += alpha * pn1;
+        if (more) f.p[n] = f.minv[n] * f.r[n] + beta * pn1;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const double rzn = sh_v[0], rrn = sh_v[1], m = sh_v[2], rz = ctl->rz2[q];
