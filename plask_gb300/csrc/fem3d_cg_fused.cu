@@ -97,6 +97,8 @@ __device__ __forceinline__ void tmacg_update_one(float& r, float q, float m, flo
 // waits for the direction kernel, which reads p anyway.  The first trip's loads do not
 // depend on alpha and are issued before warp 0 reduces the operator's partials.
 __global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_update(const TmaCg f, SolveCtl* __restrict__ ctl, int q) {
+    pdl_trigger_at(1);
+    pdl_wait();
     if (ctl->status2[q] != SOLVE_RUNNING) return;
     const long long N4 = f.N >> 2, stride = (long long)gridDim.x * blockDim.x;
     const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -165,6 +167,7 @@ __global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_update(
         tmacg_update_one(r1, f.q[n], f.minv[n], alpha, rzn, rr);
         f.r[n] = r1;
     }
+    pdl_trigger_at(2);
     float v[2] = {rzn, rr};
     write_partial_f32<2>(v, f.part + kRZ, blockIdx.x);
 }
@@ -173,6 +176,8 @@ __global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_update(
 // beta = rz' / rz and p = M^-1 r + beta p unless the solve has stopped.  The first trip's
 // loads are issued before warp 0 reduces the update's partials.
 __global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_direction(const TmaCg f, SolveCtl* __restrict__ ctl, int q) {
+    pdl_trigger_at(1);
+    pdl_wait();
     const int st0 = ctl->status2[q];
     if (st0 != SOLVE_RUNNING) {  // pass a final status on to the other parity
         if (blockIdx.x == 0 && threadIdx.x == 0) ctl->status2[1 - q] = st0;
@@ -256,6 +261,7 @@ __global__ void __launch_bounds__(kCgThreads, 1024 / kCgThreads) k_tmacg_directi
         f.x[n] += alpha * pn1;
         if (more) f.p[n] = f.minv[n] * f.r[n] + beta * pn1;
     }
+    pdl_trigger_at(2);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const double rzn = sh_v[0], rrn = sh_v[1], m = sh_v[2], rz = ctl->rz2[q];
         ctl->iter += 1;
@@ -296,11 +302,11 @@ double* tmacg_op_partials(const TmaCg& f) { return f.part + kPQ; }
 const int* tmacg_op_run(SolveCtl* ctl, int q) { return &ctl->status2[q]; }
 
 void launch_tmacg_update(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, int q) {
-    launch_kernel(k_tmacg_update, dim3(f.upd_blocks), dim3(kCgThreads), c.stream, f, ctl, q);
+    launch_kernel_pdl(k_tmacg_update, dim3(f.upd_blocks), dim3(kCgThreads), 0, c.stream, f, ctl, q);
 }
 
 void launch_tmacg_direction(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, int q) {
-    launch_kernel(k_tmacg_direction, dim3(f.upd_blocks), dim3(kCgThreads), c.stream, f, ctl, q);
+    launch_kernel_pdl(k_tmacg_direction, dim3(f.upd_blocks), dim3(kCgThreads), 0, c.stream, f, ctl, q);
 }
 
 int tmacg_blocks(const LaunchCfg& c) { return std::max(1, c.sm_count * (1024 / kCgThreads)); }

@@ -70,4 +70,21 @@ struct SurfaceT {
 
 constexpr int kMaxPartialBlocks = 4096;
 
+#ifdef __CUDACC__
+// Programmatic dependent launch (launch_kernel_pdl): pdl_trigger lets the next kernel of the
+// stream be scheduled while this one runs; pdl_wait blocks until the previous kernel has
+// completed and its writes are visible.  Both are no-ops in a kernel launched normally.
+// Where the kernels of the fused CG let the next one be scheduled (overridable at compile
+// time for tuning): 0 = only when their blocks exit, 1 = at their start, 2 = after their
+// main loop.
+#ifndef PLGPU_PDL_TRIGGER
+#define PLGPU_PDL_TRIGGER 0
+#endif
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger_at(int where) {
+    if (where == PLGPU_PDL_TRIGGER) pdl_trigger();
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+#endif
+
 }  // namespace plgpu

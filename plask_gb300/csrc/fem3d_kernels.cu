@@ -16,6 +16,7 @@
 // and the last block to arrive sums the partials in a fixed order.
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cfloat>
 #include <cstdint>
 
@@ -726,6 +727,11 @@ static std::atomic<long long> g_launches{0};
 static thread_local long long t_launches = 0;  // a handle runs on one host thread at a time
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 long long thread_launch_count() { return t_launches; }
+bool pdl_enabled() {
+    static const bool on = std::getenv("PLGPU_NO_PDL") == nullptr;
+    return on;
+}
+
 void count_launch() {
     g_launches.fetch_add(1, std::memory_order_relaxed);
     ++t_launches;

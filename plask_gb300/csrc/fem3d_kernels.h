@@ -26,6 +26,28 @@ inline void launch_kernel(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStr
     count_launch();
 }
 
+// Programmatic dependent launch of the kernels of the fused CG iteration: a kernel
+// launched this way may be scheduled while the previous kernel of the stream drains; it
+// calls pdl_wait() (fem3d_device.cuh) before it reads anything the previous kernels
+// wrote.  Off when the environment sets PLGPU_NO_PDL.
+bool pdl_enabled();
+template <typename... KArgs, typename... Args>
+inline void launch_kernel_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                              Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);  // errors surface in cudaGetLastError
+    count_launch();
+}
+
 // Material table in device memory (one entry per material id).
 struct MatTable {
     const double* k300;

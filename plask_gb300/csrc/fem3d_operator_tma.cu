@@ -175,6 +175,8 @@ template <int WX, int RR, bool ANISO, int NS>
 __global__ void __launch_bounds__(32 * WX * tma_wy(WX), PLGPU_TMA_MINB)
     k_apply_tma(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap mp,
                 const __grid_constant__ CUtensorMap mq, const TmaArgs a) {
+    pdl_trigger_at(1);
+    pdl_wait();  // the input vector and the run word come from the previous kernels
     if (*a.run != SOLVE_RUNNING) return;
     constexpr int WY = tma_wy(WX), NR = tma_regions(WX), BW = tma_box(WX);
     constexpr int XT = tma_x_tile(WX, RR), KT = tma_k_tile(WX, RR), SB = tma_stage_bytes(WX, RR, ANISO);
@@ -403,6 +405,7 @@ __global__ void __launch_bounds__(32 * WX * tma_wy(WX), PLGPU_TMA_MINB)
         if (!failed && u < nlayers) layer(u, ya, yb, acca, accb, xra, xrb);
     }
 
+    pdl_trigger_at(2);
     if (failed) {
         // report, then wait (bounded) for the copies this block still has in flight
         if (tid == 0) {
@@ -603,9 +606,8 @@ void launch_tma_coef(const LaunchCfg& c, const TmaOperator* t, const GridT<doubl
 
 template <int WX, bool ANISO>
 static void launch_tma_one(const LaunchCfg& c, const TmaOperator* t, const TmaArgs& a) {
-    k_apply_tma<WX, kTmaRows, ANISO, kTmaStages><<<t->grid, 32 * WX * tma_wy(WX), t->smem, c.stream>>>(t->mx, t->mp,
-                                                                                                   t->mq, a);
-    count_launch();
+    launch_kernel_pdl(k_apply_tma<WX, kTmaRows, ANISO, kTmaStages>, t->grid, dim3(32 * WX * tma_wy(WX)), t->smem,
+                      c.stream, t->mx, t->mp, t->mq, a);
 }
 
 void launch_operator_tma(const LaunchCfg& c, const TmaOperator* t, float* y, double* partials, const int* run,
