@@ -67,14 +67,14 @@ namespace {
 #define PLGPU_TMA_ROWS 2
 #endif
 #ifndef PLGPU_TMA_STAGES
-#define PLGPU_TMA_STAGES 4
+#define PLGPU_TMA_STAGES 3
 #endif
 #ifndef PLGPU_TMA_BLOCKS
 #define PLGPU_TMA_BLOCKS 0
 #endif
 //   PLGPU_TMA_MINB    blocks per SM the register budget is sized for
 #ifndef PLGPU_TMA_MINB
-#define PLGPU_TMA_MINB 5
+#define PLGPU_TMA_MINB 4
 #endif
 constexpr int kTmaRows = PLGPU_TMA_ROWS;
 constexpr int kTmaStages = PLGPU_TMA_STAGES;
@@ -345,36 +345,54 @@ __global__ void __launch_bounds__(32 * WX * tma_wy(WX), PLGPU_TMA_MINB)
         // plane kstart + u is complete
         const int k = kstart + u;
         if (k >= k0) {
-            // planes holding convective surface rows have a node -> row map
-            const int sp = a.s.plane != nullptr ? a.s.plane[k] : 0;
             const long long pb = s2 * k;
+            float2 out[RR];
 #pragma unroll
             for (int r = 0; r < RR; ++r) {
                 const float2 right = add2(accLo.s[r], accLo.d[r]), left = sub2(accLo.s[r], accLo.d[r]);
                 float recv = __shfl_down_sync(0xffffffffu, left.x, 1);
                 if (lane == 31) recv = (wx + 1 < WX) ? xb[(wx + 1) * RR + r] : 0.f;
-                float2 out = make_float2(right.x + left.y, right.y + recv);
+                out[r] = make_float2(right.x + left.y, right.y + recv);
+            }
+            // planes holding convective surface rows have a node -> row map; the rows of the
+            // thread's 2 RR nodes are gathered together (independent loads in each round)
+            const int sp = a.s.plane != nullptr ? a.s.plane[k] : 0;
+            if (sp != 0) {
+                int beg[2 * RR], cnt[2 * RR];
+                int most = 0;
+#pragma unroll
+                for (int r = 0; r < RR; ++r) {
+                    const int row = jw + r;
+                    const bool in = c0 < a.n0 && row < a.n1;
+                    const long long mb = (long long)(sp - 1) * s2 + (long long)row * a.n0 + c0;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int sr = in ? a.s.map[mb + h] : -1;
+                        beg[2 * r + h] = sr >= 0 ? a.s.ptr[sr] : 0;
+                        cnt[2 * r + h] = sr >= 0 ? a.s.ptr[sr + 1] - beg[2 * r + h] : 0;
+                        most = max(most, cnt[2 * r + h]);
+                    }
+                }
+                float acc[2 * RR];
+#pragma unroll
+                for (int i = 0; i < 2 * RR; ++i) acc[i] = 0.f;
+                for (int q = 0; q < most; ++q) {
+#pragma unroll
+                    for (int i = 0; i < 2 * RR; ++i)
+                        if (q < cnt[i]) acc[i] += a.s.val[beg[i] + q] * a.x[a.s.col[beg[i] + q]];
+                }
+#pragma unroll
+                for (int r = 0; r < RR; ++r) {
+                    out[r].x += acc[2 * r];
+                    out[r].y += acc[2 * r + 1];
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < RR; ++r) {
                 const int row = jw + r;
                 if (c0 < a.n0 && row < a.n1) {  // n0 is even: c0 + 1 < n0 too
-                    const long long n = pb + (long long)row * a.n0 + c0;
-                    if (sp != 0) {
-                        const long long mb = (long long)(sp - 1) * s2 + (long long)row * a.n0 + c0;
-#pragma unroll
-                        for (int h = 0; h < 2; ++h) {
-                            const int sr = a.s.map[mb + h];
-                            if (sr >= 0) {
-                                float acc = 0.f;
-                                for (int q = a.s.ptr[sr]; q < a.s.ptr[sr + 1]; ++q)
-                                    acc += a.s.val[q] * a.x[a.s.col[q]];
-                                if (h == 0)
-                                    out.x += acc;
-                                else
-                                    out.y += acc;
-                            }
-                        }
-                    }
-                    dot = fma2(xrLo[r], out, dot);
-                    *reinterpret_cast<float2*>(a.y + n) = out;
+                    dot = fma2(xrLo[r], out[r], dot);
+                    *reinterpret_cast<float2*>(a.y + pb + (long long)row * a.n0 + c0) = out[r];
                 }
             }
         }
