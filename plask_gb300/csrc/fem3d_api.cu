@@ -1330,27 +1330,49 @@ struct plgpu_fem3d {
     }
 
     // The CG of fem3d_cg_fused.cu runs where the TMA operator does
-    bool fused_ready() const { return !planar && tma != nullptr && tma_fresh && !dyn_active; }
-    TmaCg fused_args() {
-        return TmaCg{N, x32.as<float>(), r32v.as<float>(), p32.as<float>(), q32.as<float>(), minv32.as<float>(),
-                     cgpart.as<double>(), tmacg_blocks(cfg), tma_operator_blocks(tma)};
+    // the TMA-staged operator is set up for the current coefficients
+    bool tma_ready() const { return !planar && tma != nullptr && tma_fresh && !dyn_active; }
+    // the inner FP32 solve runs the fused iteration (operator, update, direction): on the
+    // TMA-staged operator where it is set up, else on the register-march operator
+    bool fused_ready() const {
+        static const bool off = std::getenv("PLGPU_NO_FUSED") != nullptr;
+        return !planar && !dyn_active && (tma_ready() || !off);
     }
-    // x32 = the FP32 Jacobi-PCG solution of A x = r32v to inner_rtol: the TMA operator with
-    // the surface rows, then the update and direction kernels
+    TmaCg fused_args() {
+        if (!cgpart.p) cgpart.alloc(sizeof(double) * 3 * kMaxPartialBlocks);
+        const int opb = tma_ready() ? tma_operator_blocks(tma)
+                                    : op_blocks(cfg, n[0], n[1], n[2], false) + surface_cg_blocks(s32.nrows);
+        return TmaCg{N, x32.as<float>(), r32v.as<float>(), p32.as<float>(), q32.as<float>(), minv32.as<float>(),
+                     cgpart.as<double>(), tmacg_blocks(cfg, N), opb};
+    }
+    // x32 = the FP32 Jacobi-PCG solution of A x = r32v to inner_rtol: the operator with the
+    // surface rows (in the TMA kernel, or k_surface_cg before the register-march kernel, its
+    // partials after the operator's), then the update and direction kernels
     void fused_cg(int& status, int& iters, int cap) {
         SolveCtl* ctl = d_ctl.as<SolveCtl>();
         const TmaCg f = fused_args();
+        const bool staged = tma_ready();
+        const int mblocks = staged ? 0 : op_blocks(cfg, n[0], n[1], n[2], false);
         launch_tmacg_start(cfg, f, ctl, inner_rtol, -1, cap, cap);
         auto enqueue = [&](int len) {  // len is even: every chunk starts at parity 0
             for (int it = 0; it < len; ++it) {
                 const int q = it & 1;
-                launch_operator_tma(cfg, tma, q32.as<float>(), tmacg_op_partials(f), tmacg_op_run(ctl, q), ctl,
-                                    tsurf);
+                const int* run = tmacg_op_run(ctl, q);
+                if (staged) {
+                    launch_operator_tma(cfg, tma, q32.as<float>(), tmacg_op_partials(f), run, ctl, tsurf);
+                } else {
+                    const int ss = launch_surface_cg_run(cfg, s32, p32.as<float>(), q32.as<float>(),
+                                                         tmacg_op_partials(f), mblocks, run);
+                    launch_operator(cfg, g32, zf32.as<float>(), zr32.as<float>(), p32.as<float>(), q32.as<float>(),
+                                    k32.as<float>(), aniso ? kz32.as<float>() : nullptr, aniso,
+                                    dmask.as<uint32_t>(), (const float*)nullptr, tmacg_op_partials(f), MODE_CG, ctl,
+                                    ss > 0 ? smask.as<uint32_t>() : nullptr, ss, nullptr, nullptr, run);
+                }
                 launch_tmacg_update(cfg, f, ctl, q);
                 launch_tmacg_direction(cfg, f, ctl, q);
             }
         };
-        run_chunks(3, chunk, 256, enqueue, status, iters, cap);
+        run_chunks(staged ? 3 : 4, chunk, 256, enqueue, status, iters, cap);
     }
 
     // r64 = b - A T (Dirichlet columns eliminated)
@@ -2033,7 +2055,7 @@ struct plgpu_fem3d {
                 launch_operator(cfg, g64, zf64.as<double>(), zr64.as<double>(), p64.as<double>(), q64.as<double>(),
                                 k64.as<double>(), aniso ? kz64.as<double>() : nullptr, aniso, dmask.as<uint32_t>(),
                                 nullptr, partials.as<double>(), MODE_CG, ctl);
-            else if (fused_ready())  // the kernel the FP32 CG solve runs, without surface rows
+            else if (tma_ready())  // the kernel the FP32 CG solve runs, without surface rows
                 launch_operator_tma(cfg, tma, q32.as<float>(), partials.as<double>(), &ctl->status, ctl,
                                     TmaSurface{});
             else
@@ -2073,7 +2095,7 @@ struct plgpu_fem3d {
         launch_from_mesh_order_f64(cfg, n[0], n[1], n[2], n[0], n[1], n[2], ns[0], ns[1], ns[2], tmp.as<double>(),
                                    p64.as<double>(), 0.0);
         launch_norm2(cfg, N, p64.as<double>(), p32.as<float>(), partials.as<double>(), d_ctl.as<SolveCtl>(), 4);
-        const bool fused = fused_ready();
+        const bool fused = tma_ready();
         if (fused) {
             launch_operator_tma(cfg, tma, q32.as<float>(), partials.as<double>(), &ctl->status, ctl, tsurf);
             launch_partials_to_ctl(cfg, partials.as<double>(), tma_operator_blocks(tma), ctl);

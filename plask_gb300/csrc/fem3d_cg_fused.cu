@@ -309,7 +309,13 @@ void launch_tmacg_direction(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, i
     launch_kernel_pdl(k_tmacg_direction, dim3(f.upd_blocks), dim3(kCgThreads), 0, c.stream, f, ctl, q);
 }
 
-int tmacg_blocks(const LaunchCfg& c) { return std::max(1, c.sm_count * (1024 / kCgThreads)); }
+// one wave of resident blocks, fewer for small meshes (down to one block per SM: a thread
+// takes at least kUnroll float4 groups, and every block reduces the others' partials)
+int tmacg_blocks(const LaunchCfg& c, long long N) {
+    const long long wave = std::max(1, c.sm_count * (1024 / kCgThreads));
+    const long long need = ((N >> 2) + (long long)kCgThreads * kUnroll - 1) / ((long long)kCgThreads * kUnroll);
+    return (int)std::min(wave, std::max<long long>(std::max(1, c.sm_count), need));
+}
 
 void launch_partials_to_ctl(const LaunchCfg& c, const double* partials, int nslots, SolveCtl* ctl) {
     launch_kernel(k_partials_to_ctl, dim3(1), dim3(256), c.stream, partials, nslots, ctl);

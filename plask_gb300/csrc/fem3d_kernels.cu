@@ -78,8 +78,8 @@ __device__ __forceinline__ R surface_row(const SurfaceT<R>& s, const R* __restri
 template <typename R>
 __global__ void __launch_bounds__(256) k_surface_cg(const SurfaceT<R> s, const R* __restrict__ x, R* __restrict__ y,
                                                     double* __restrict__ partials, int slot0,
-                                                    const SolveCtl* __restrict__ ctl) {
-    if (ctl->status != SOLVE_RUNNING) return;
+                                                    const int* __restrict__ run) {
+    if (*run != SOLVE_RUNNING) return;
     double dot = 0.0;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < s.nrows; r += gridDim.x * blockDim.x) {
         const int n = s.row[r];
@@ -764,18 +764,22 @@ static void launch_surface_any(const LaunchCfg& c, const SurfaceT<R>& s, const R
 int surface_cg_blocks(int nrows) { return nrows > 0 ? grid_for(nrows, 256, 256) : 0; }
 template <typename R>
 static int surface_cg_any(const LaunchCfg& c, const SurfaceT<R>& s, const R* x, R* y, double* partials, int slot0,
-                          const SolveCtl* ctl) {
+                          const int* run) {
     const int blocks = surface_cg_blocks(s.nrows);
-    if (blocks > 0) launch(k_surface_cg<R>, blocks, 256, c.stream, s, x, y, partials, slot0, ctl);
+    if (blocks > 0) launch(k_surface_cg<R>, blocks, 256, c.stream, s, x, y, partials, slot0, run);
     return blocks;
 }
 int launch_surface_cg(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, double* partials,
                       int slot0, const SolveCtl* ctl) {
-    return surface_cg_any<float>(c, s, x, y, partials, slot0, ctl);
+    return surface_cg_any<float>(c, s, x, y, partials, slot0, &ctl->status);
+}
+int launch_surface_cg_run(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, double* partials,
+                          int slot0, const int* run) {
+    return surface_cg_any<float>(c, s, x, y, partials, slot0, run);
 }
 int launch_surface_cg(const LaunchCfg& c, const SurfaceT<double>& s, const double* x, double* y, double* partials,
                       int slot0, const SolveCtl* ctl) {
-    return surface_cg_any<double>(c, s, x, y, partials, slot0, ctl);
+    return surface_cg_any<double>(c, s, x, y, partials, slot0, &ctl->status);
 }
 void launch_surface(const LaunchCfg& c, const SurfaceT<double>& s, const double* x, double* y, int mode) {
     launch_surface_any<double>(c, s, x, y, mode);

@@ -137,11 +137,13 @@ int choose_op_rows(int n1);
 // MODE_CG: y = A x, where nodes flagged in smask add the S x that k_surface (launched
 // just before, launch_surface_cg) left in y; the last block sums the operator's partials
 // and the sslots surface partials after them into (x, A x) and sets alpha = rz / (x, A x)
-// (or the breakdown / non-finite status).
+// (or the breakdown / non-finite status).  With run (FP32, the fused CG iteration of
+// fem3d_cg_fused.cu): the launch runs while *run == SOLVE_RUNNING and leaves only its block
+// partials (op_blocks of them, slot = block index) for the update kernel.
 void launch_operator(const LaunchCfg& c, const GridT<float>& g, const float* zf, const float* zr, const float* x,
                      float* y, const float* kxy, const float* kz, bool aniso, const uint32_t* dmask, const float* rhs,
                      double* partials, int mode, SolveCtl* ctl, const uint32_t* smask = nullptr, int sslots = 0,
-                     const float* dshift = nullptr, const float* cmass = nullptr);
+                     const float* dshift = nullptr, const float* cmass = nullptr, const int* run = nullptr);
 void launch_operator(const LaunchCfg& c, const GridT<double>& g, const double* zf, const double* zr, const double* x,
                      double* y, const double* kxy, const double* kz, bool aniso, const uint32_t* dmask,
                      const double* rhs, double* partials, int mode, SolveCtl* ctl, const uint32_t* smask = nullptr,
@@ -194,7 +196,7 @@ void launch_tmacg_start(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, doubl
 double* tmacg_op_partials(const TmaCg& f);
 const int* tmacg_op_run(SolveCtl* ctl, int q);
 // grid of the start, update and direction kernels (TmaCg::upd_blocks)
-int tmacg_blocks(const LaunchCfg& c);
+int tmacg_blocks(const LaunchCfg& c, long long N);
 void launch_tmacg_update(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, int q);
 void launch_tmacg_direction(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, int q);
 // ctl->pq = the sum of nslots block partials (fixed order)
@@ -207,6 +209,9 @@ int launch_surface_cg(const LaunchCfg& c, const SurfaceT<float>& s, const float*
                       int slot0, const SolveCtl* ctl);
 int launch_surface_cg(const LaunchCfg& c, const SurfaceT<double>& s, const double* x, double* y, double* partials,
                       int slot0, const SolveCtl* ctl);
+// the same, running while *run == SOLVE_RUNNING (the fused CG iteration)
+int launch_surface_cg_run(const LaunchCfg& c, const SurfaceT<float>& s, const float* x, float* y, double* partials,
+                          int slot0, const int* run);
 int surface_cg_blocks(int nrows);
 
 // convective face terms in MODE_MULT (y += S x) or MODE_RESID (y -= S x)

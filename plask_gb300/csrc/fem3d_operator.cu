@@ -57,6 +57,10 @@ struct OpArgs {
     // capacity c, adding c (M (x) M (x) M), M = [[2,1],[1,2]] / 3, to the element matrix,
     // or nullptr
     const R* cmass;
+    // MODE_CG inside the fused CG iteration (fem3d_cg_fused.cu): the launch runs only while
+    // *run == SOLVE_RUNNING and leaves its block partials for the update kernel (no last-block
+    // reduction); nullptr: the status word of ctl and the last block sets alpha
+    const int* run;
 };
 
 // Weights of the consistent capacity in the butterfly basis: per axis M = (1/2) e e^T +
@@ -91,7 +95,9 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 template <typename R, int RR, bool ANISO, int MODE, bool SHIFT = false, bool MASS = false,
           int MINB = (sizeof(R) == 4 ? 4 : 2), int UNR = 1>
 __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
-    if (MODE == MODE_CG && a.ctl != nullptr && a.ctl->status != SOLVE_RUNNING) return;
+    if (MODE == MODE_CG &&
+        (a.run != nullptr ? *a.run != SOLVE_RUNNING : (a.ctl != nullptr && a.ctl->status != SOLVE_RUNNING)))
+        return;
     const int n0 = a.g.n0, n1 = a.g.n1, n2 = a.g.n2;
     const int s2 = n0 * n1;  // N < 2^31 (checked on the host)
     const int lane = threadIdx.x & 31;
@@ -294,7 +300,7 @@ __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
         double v[1] = {(double)dot};
         write_partial<1, OpSum>(v, a.partials, bid);
         const int nblocks = gridDim.x * gridDim.y * gridDim.z;
-        if (arrive_last(&a.ctl->arrive[0], nblocks)) {
+        if (a.run == nullptr && arrive_last(&a.ctl->arrive[0], nblocks)) {
             reduce_partials<1, OpSum>(v, a.partials, nblocks + a.sslots);
             if (threadIdx.x == 0) {
                 const double pq = v[0];
@@ -321,7 +327,9 @@ __global__ void __launch_bounds__(128, MINB) k_apply_haar(const OpArgs<R> a) {
 template <typename R, int RR, bool ANISO, int MODE, bool SHIFT = false, bool MASS = false,
           int MINB = (sizeof(R) == 4 ? 4 : 2)>
 __global__ void __launch_bounds__(128, MINB) k_apply_shared(const OpArgs<R> a) {
-    if (MODE == MODE_CG && a.ctl != nullptr && a.ctl->status != SOLVE_RUNNING) return;
+    if (MODE == MODE_CG &&
+        (a.run != nullptr ? *a.run != SOLVE_RUNNING : (a.ctl != nullptr && a.ctl->status != SOLVE_RUNNING)))
+        return;
     const int n0 = a.g.n0, n1 = a.g.n1, n2 = a.g.n2;
     const int s2 = n0 * n1;  // N < 2^31 (checked on the host)
     const int lane = threadIdx.x & 31;
@@ -520,7 +528,7 @@ __global__ void __launch_bounds__(128, MINB) k_apply_shared(const OpArgs<R> a) {
         double v[1] = {(double)dot};
         write_partial<1, OpSum>(v, a.partials, bid);
         const int nblocks = gridDim.x * gridDim.y * gridDim.z;
-        if (arrive_last(&a.ctl->arrive[0], nblocks)) {
+        if (a.run == nullptr && arrive_last(&a.ctl->arrive[0], nblocks)) {
             reduce_partials<1, OpSum>(v, a.partials, nblocks + a.sslots);
             if (threadIdx.x == 0) {
                 const double pq = v[0];
@@ -649,12 +657,13 @@ static void op_launch_rows(const LaunchCfg& c, dim3 grid, const OpArgs<R>& a, bo
 template <typename R>
 static void op_launch(const LaunchCfg& c, const GridT<R>& g, const R* zf, const R* zr, const R* x, R* y, const R* kxy,
                       const R* kz, bool aniso, const uint32_t* dmask, const R* rhs, double* partials, int mode,
-                      SolveCtl* ctl, const uint32_t* smask, int sslots, const R* dshift, const R* cmass) {
+                      SolveCtl* ctl, const uint32_t* smask, int sslots, const R* dshift, const R* cmass,
+                      const int* run = nullptr) {
     constexpr bool fp64 = sizeof(R) == 8;
     dim3 grid;
     int zchunk;
     op_grid(c, g.n0, g.n1, g.n2, fp64, grid, zchunk);
-    OpArgs<R> a{g, x, y, kxy, kz, dmask, rhs, partials, ctl, zf, zr, zchunk, smask, sslots, dshift, cmass};
+    OpArgs<R> a{g, x, y, kxy, kz, dmask, rhs, partials, ctl, zf, zr, zchunk, smask, sslots, dshift, cmass, run};
     if constexpr (fp64) {
         op_launch_rows<R, 4>(c, grid, a, aniso, mode);
     } else {
@@ -669,9 +678,9 @@ static void op_launch(const LaunchCfg& c, const GridT<R>& g, const R* zf, const 
 void launch_operator(const LaunchCfg& c, const GridT<float>& g, const float* zf, const float* zr, const float* x,
                      float* y, const float* kxy, const float* kz, bool aniso, const uint32_t* dmask, const float* rhs,
                      double* partials, int mode, SolveCtl* ctl, const uint32_t* smask, int sslots,
-                     const float* dshift, const float* cmass) {
+                     const float* dshift, const float* cmass, const int* run) {
     op_launch<float>(c, g, zf, zr, x, y, kxy, kz, aniso, dmask, rhs, partials, mode, ctl, smask, sslots, dshift,
-                     cmass);
+                     cmass, run);
 }
 void launch_operator(const LaunchCfg& c, const GridT<double>& g, const double* zf, const double* zr, const double* x,
                      double* y, const double* kxy, const double* kz, bool aniso, const uint32_t* dmask,
