@@ -112,6 +112,7 @@ __device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
+
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
 }
@@ -280,7 +281,8 @@ __global__ void __launch_bounds__(32 * WX * tma_wy(WX), PLGPU_TMA_MINB)
         // plane u + 1 landed?
         bool ok = true;
         if (u + 1 >= waited) {
-            ok = mbar_wait(bar_of(u + 1), (uint32_t)(((u + 1) / NS) & 1));
+            // warp-uniform: a warp takes one path through the stage
+            ok = __all_sync(0xffffffffu, mbar_wait(bar_of(u + 1), (uint32_t)(((u + 1) / NS) & 1)));
             if (ok) waited = u + 2;
         }
         if (ok) {
@@ -402,7 +404,7 @@ __global__ void __launch_bounds__(32 * WX * tma_wy(WX), PLGPU_TMA_MINB)
 
     // prologue: plane 0 of the chunk
     {
-        const bool ok = mbar_wait(bar_of(0), 0u);
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(bar_of(0), 0u));
         if (ok) {
             waited = 1;
             plane_stage(0, ya, xra);
