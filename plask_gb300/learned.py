@@ -13,6 +13,7 @@ The weights it produced are shipped as ``data/unet_c2.bin`` (the weights file
 format of ``plgpu_unet_save``: header, FP32 weights, checksum).
 
     python -m plask_gb300.learned [--out PATH] [--steps 2000] [--pairs jacobi]
+    python -m plask_gb300.learned --time SEED   # device time of the shipped network on learned_c2(SEED)
 """
 from __future__ import annotations
 
@@ -63,13 +64,29 @@ def load_c2(path=WEIGHTS_C2):
     return net
 
 
+def time_c2(seed, reps=3):
+    """(forward ms, preconditioner application ms) of the shipped network on learned_c2(seed)."""
+    from . import structures as S
+    from . import thermal as TH
+
+    sv = TH.solver_for_structure(S.learned_c2(seed=seed), algorithm="gpu-learned")
+    sv.initialize()
+    return load_c2().time_apply(sv._fem, reps=reps)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--time", type=int, default=None, metavar="SEED",
+                    help="time the shipped network on learned_c2(SEED) instead of training")
     ap.add_argument("--out", default=str(WEIGHTS_C2))
     ap.add_argument("--steps", type=int, default=STEPS_PER_STRUCTURE, help="pairs per training structure")
     ap.add_argument("--pairs", default="jacobi", choices=["jacobi", "cg"])
     ap.add_argument("--lr", type=float, default=1e-3)
     args = ap.parse_args(argv)
+    if args.time is not None:
+        fwd, app = time_c2(args.time)
+        print(f"forward {1e3 * fwd:.1f} us, preconditioner application {1e3 * app:.1f} us")
+        return 0
     smooth = (5, 60) if args.pairs == "jacobi" else (20, 300)
     net, _ = train_c2(steps=args.steps, lr=args.lr, smooth=smooth, pairs=args.pairs)
     out = pathlib.Path(args.out)
