@@ -494,7 +494,7 @@ class Shockley3D:
         sym = tuple(getattr(self._geometry, "symmetric", ())) if self._geometry is not None else ()
         if not any(sym):
             return pts, {}
-        return wrap_symmetric(pts, sym, [float(a[0]) for a in self._mesh.axes])
+        return wrap_symmetric(pts, sym, [float(a[0]) for a in self._mesh.axes], [float(a[-1]) for a in self._mesh.axes])
 
     def _get_voltage(self, dst_mesh, interpolation="linear"):
         """Potential on a destination mesh (electr3d.cpp:507-515): trilinear or the nearest

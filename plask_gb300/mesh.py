@@ -336,17 +336,23 @@ class RectangularMesh2D:
                 "bottom": RectangularMesh2D.Bottom, "top": RectangularMesh2D.Top}[name]()
 
 
-def wrap_symmetric(pts, sym, lows):
+def wrap_symmetric(pts, sym, lows, highs=None):
     """Points as a provider reads them along axes where the geometry mirrors at 0
     (InterpolationFlags::wrap, plask/mesh/interpolation.hpp:232-250, non-periodic branch):
     a coordinate 0 becomes 1e-12, then, when the geometry lies on the positive side of the
     axis (its lower bound ``lows[d]`` >= 0), every coordinate reads at its absolute value,
     otherwise at minus it.  Returns the wrapped points and, per mirrored axis, the mask of
     points on the other side, whose vector components along that axis change sign
-    (InterpolationFlags::postprocess, interpolation.hpp:272-287)."""
+    (InterpolationFlags::postprocess, interpolation.hpp:272-287).  A mirrored axis whose
+    geometry spans both sides of 0 (``lows[d]`` < 0 < ``highs[d]``) raises ValueError, as
+    the reference's InterpolationFlags constructor does (interpolation.hpp:185-203)."""
     flips = {}
     if not any(sym):
         return pts, flips
+    names = ("longitudinal", "transverse", "vertical") if len(sym) == 3 else ("horizontal", "vertical")
+    for d, on in enumerate(sym):
+        if on and highs is not None and lows[d] < 0.0 < highs[d]:
+            raise ValueError(f"interpolation: Symmetric geometry spans at both sides of {names[d]} axis")
     w = np.array(pts, dtype=np.float64, copy=True)
     for d, on in enumerate(sym):
         if not on:

@@ -853,7 +853,7 @@ class Static3D:
         sym = tuple(getattr(self._geometry, "symmetric", ())) if self._geometry is not None else ()
         if not any(sym):
             return pts, {}
-        return wrap_symmetric(pts, sym, [float(a[0]) for a in self._mesh.axes])
+        return wrap_symmetric(pts, sym, [float(a[0]) for a in self._mesh.axes], [float(a[-1]) for a in self._mesh.axes])
 
     def _get_temperatures(self, dst_mesh, interpolation="linear"):
         """Temperatures on a destination mesh (therm3d.cpp:387-395): trilinear or the nearest

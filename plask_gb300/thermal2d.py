@@ -340,7 +340,7 @@ class Static2D:
             sym[0] = True
         if not any(sym):
             return pts, {}
-        return wrap_symmetric(pts, sym, [float(a[0]) for a in self._mesh.axes])
+        return wrap_symmetric(pts, sym, [float(a[0]) for a in self._mesh.axes], [float(a[-1]) for a in self._mesh.axes])
 
     def _get_temperatures(self, dst_mesh, interpolation="linear"):
         """Temperatures on a destination mesh or points (therm2d.cpp:544-553): bilinear or the

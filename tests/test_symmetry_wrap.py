@@ -24,3 +24,13 @@ def test_no_symmetric_axis_leaves_points_alone():
     pts = np.array([[-1.0, 2.0, 3.0]])
     w, flips = wrap_symmetric(pts, (False, False, False), (0.0, 0.0, 0.0))
     assert w is pts and flips == {}
+
+
+def test_symmetric_axis_spanning_both_sides_is_rejected():
+    import pytest
+
+    pts = np.array([[1.0, 2.0, 3.0]])
+    with pytest.raises(ValueError, match="both sides of transverse axis"):
+        wrap_symmetric(pts, (False, True, False), (0.0, -2.0, 0.0), (5.0, 2.0, 9.0))
+    w, _ = wrap_symmetric(pts, (False, True, False), (0.0, 0.0, 0.0), (5.0, 2.0, 9.0))
+    assert w[0, 1] == 2.0
