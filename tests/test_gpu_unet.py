@@ -155,3 +155,9 @@ def test_shipped_network_gain_on_config2():
     assert learned.stats["loops"] == base.stats["loops"]
     assert np.nanmax(np.abs(T1 - T0)) <= 1e-6
     assert learned.stats["inner_iterations"] <= 1.15 * base.stats["inner_iterations"]
+    # the split of the iterations and the network's own device time are reported
+    assert 0 < learned.stats["learned_iterations"] <= learned.stats["inner_iterations"]
+    assert base.stats["learned_iterations"] == 0
+    fwd, app = net.time_apply(learned._fem, reps=2)
+    print("network forward ms", fwd, "preconditioner application ms", app)
+    assert 0.0 < fwd < app
