@@ -32,8 +32,11 @@ namespace plgpu {
 constexpr int kCgThreads = PLGPU_CG_THREADS;
 
 namespace {
-// float4 groups in flight per thread
-constexpr int kUnroll = 2;
+// float4 groups in flight per thread (overridable at compile time for tuning sweeps)
+#ifndef PLGPU_CG_UNROLL
+#define PLGPU_CG_UNROLL 2
+#endif
+constexpr int kUnroll = PLGPU_CG_UNROLL;
 constexpr size_t kPQ = 0;                          // (p, A p): one value per operator block
 constexpr size_t kRZ = (size_t)kMaxPartialBlocks;  // (r, M^-1 r) and (r, r) per update block
 }  // namespace
