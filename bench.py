@@ -19,6 +19,12 @@ parity   max |dT| of the final field against the reference's own NSPCG solution
          (zeta 1e-12, tests/golden/static3d_layered_c1_128x128x200_nspcg.npz) at
          16384 seeded nodes, the plane and the vertical line through the hottest
          node, and the FP64 relative residuals of both;
+learned  the learned preconditioner on a structure of its own configuration
+         (structures.learned_c2, seed 2001, 124x108x128): learned flexible CG + mixed
+         precision, Jacobi-PCG mixed precision and plain FP64, with iterations, the
+         network's device time and max |dT| between them;
+coupled  the thermo-electric loop at 200x200x120 (structures.shockley_c4), per round;
+sweep    64 structures of the uneven-size sweep, batched and one at a time;
 cpu_baseline  the reference's default iterative algorithm (IC + CG) restated
          on the host (oracle), timed on a bounded sample of the 128x128x200 case
          and extrapolated with the reference NSPCG's own iteration counts; beside
