@@ -106,13 +106,13 @@ def _mesa_with_faces(seed, n):
 @pytest.mark.parametrize("algorithm,always", [("gpu-mixed", False), ("gpu-pcg", False), ("gpu-mixed", True)])
 @pytest.mark.parametrize("order", ["201", "012"])
 def test_masked_mesh_with_face_conditions_matches_oracle(order, algorithm, always, monkeypatch):
-    # always: the TMA operator and its CG on this 12-column mesh too (surface rows on the
-    # top, right and front faces, masked-out nodes)
-    if always:
-        monkeypatch.setenv("PLGPU_TMA_ALWAYS", "1")
     """Full compute() with a masked mesh and heat-flux, convective and radiative faces in
     the reference's placement (face terms on element corners 0-3, radiation reading the
-    temperatures of global nodes 0-7), against the oracle."""
+    temperatures of global nodes 0-7), against the oracle.  always: the TMA operator and
+    its CG on this 12-column mesh too (surface rows on the top, right and front faces,
+    masked-out nodes)."""
+    if always:
+        monkeypatch.setenv("PLGPU_TMA_ALWAYS", "1")
     s = _mesa_with_faces(seed=12, n=(12, 11, 16))
     p = O.from_structure(s, order=order)
     To, tot_o, rec = O.compute(p)
@@ -122,5 +122,24 @@ def test_masked_mesh_with_face_conditions_matches_oracle(order, algorithm, alway
     assert n_act < act.size  # the etched corner drops nodes
     assert sv.stats["loops"] == len(rec)
     assert np.all(np.isnan(T[~act]))
+    assert np.max(np.abs(T[act] - To[act])) <= TOL_T
+    assert abs(tot - tot_o) <= TOL_T
+
+
+@pytest.mark.parametrize("algorithm", ["gpu-mixed", "gpu-pcg"])
+@pytest.mark.parametrize("seed", [2005, 2006])
+def test_config2_structure_matches_oracle(seed, algorithm):
+    """Structures of the learned preconditioner's configuration (random layers, a mesa etched
+    through the upper ones: a masked mesh, an oxide aperture at 1e-2 of its host layer's
+    conductivity, Gaussian heat blobs) at 24x24x32 nodes against the oracle's band
+    Cholesky: the register-march operator's fused iteration (24 columns)."""
+    s = S.learned_c2(seed=seed, n=(24, 24, 32))
+    order = "201"
+    p = O.from_structure(s, order=order)
+    To, tot_o, rec = O.compute(p)
+    sv, T, tot = _gpu(s, order, algorithm)
+    act = O.masked_numbering(p)[0] >= 0
+    assert not act.all()  # the etched region drops nodes
+    assert sv.stats["loops"] == len(rec)
     assert np.max(np.abs(T[act] - To[act])) <= TOL_T
     assert abs(tot - tot_o) <= TOL_T
