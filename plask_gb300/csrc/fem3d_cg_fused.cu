@@ -312,12 +312,14 @@ void launch_tmacg_direction(const LaunchCfg& c, const TmaCg& f, SolveCtl* ctl, i
     launch_kernel_pdl(k_tmacg_direction, dim3(f.upd_blocks), dim3(kCgThreads), 0, c.stream, f, ctl, q);
 }
 
-// one wave of resident blocks, fewer for small meshes (down to one block per SM: a thread
-// takes at least kUnroll float4 groups, and every block reduces the others' partials)
+// one wave of resident blocks (of the share of the GPU the handle's grid policy aims at),
+// fewer for small meshes (down to one block per SM of that share: a thread takes at least
+// kUnroll float4 groups, and every block reduces the others' partials)
 int tmacg_blocks(const LaunchCfg& c, long long N) {
-    const long long wave = std::max(1, c.sm_count * (1024 / kCgThreads));
+    const long long sms = std::max(1, c.sm_count / std::max(1, c.op_share));
+    const long long wave = sms * (1024 / kCgThreads);
     const long long need = ((N >> 2) + (long long)kCgThreads * kUnroll - 1) / ((long long)kCgThreads * kUnroll);
-    return (int)std::min(wave, std::max<long long>(std::max(1, c.sm_count), need));
+    return (int)std::min(wave, std::max(sms, need));
 }
 
 void launch_partials_to_ctl(const LaunchCfg& c, const double* partials, int nslots, SolveCtl* ctl) {
