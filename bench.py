@@ -433,15 +433,18 @@ def sweep_record(count, sequential, algorithm="gpu-mixed", loops=30):
         f.invalidate()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    _native.batch_compute(fems, loops=loops, threads=threads)
+    _, bstats, _ = _native.batch_compute(fems, loops=loops, threads=threads)
     torch.cuda.synchronize()
     t_bat = time.perf_counter() - t0
+    node_iters = float(sum(int(np.prod(st.shape)) * b["inner_iterations"] for st, b in zip(structs, bstats)))
     dT = max(float(np.max(np.abs(fems[k].temperature() - T_seq[k]))) for k in range(len(seq)))
     return {"workload": f"{count} structures of the uneven-size sweep (seed 3000: 32..96 nodes per axis, "
                         f"{nodes} nodes in total, 1e15..1e16 W/m^3, at most {loops} outer loops)",
             "batched_solves_per_s": count / t_bat, "batched_seconds": t_bat, "threads": threads, "grid_share": share,
             "one_at_a_time_solves_per_s": sequential / t_seq, "one_at_a_time_sample": sequential,
             "speedup": (count / t_bat) / (sequential / t_seq),
+            "cg_iterations": int(sum(b["inner_iterations"] for b in bstats)),
+            "batched_node_iterations_per_us": node_iters / (t_bat * 1e6),
             "max_dT_batched_vs_one_at_a_time_K": dT}
 
 
