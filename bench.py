@@ -527,9 +527,14 @@ def run_sweep(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     iters = 0
-    unconverged = []
+    unconverged, failed = [], []
     for k, f in enumerate(fems):
-        _, st = f.compute(args.sweep_loops)
+        try:
+            _, st = f.compute(args.sweep_loops)
+        except _native.ComputationError:  # a runaway structure whose solve breaks down
+            failed.append(k)
+            unconverged.append(k)
+            continue
         iters += st["inner_iterations"]
         if st["err"] > 0.05 or not st["converged"]:
             unconverged.append(k)
@@ -537,14 +542,17 @@ def run_sweep(args):
     t_seq = time.perf_counter() - t0
     T_seq = [f.temperature() for f in fems]
     # autotune on a sample, then the whole sweep batched
-    sample = fems[: min(32, len(fems))]
+    sample = [f for k, f in enumerate(fems) if k not in failed][: min(32, len(fems))]
     threads, share, trials = _native.batch_tune(sample, loops=args.sweep_loops, max_threads=32)
     for f in fems:
         f.set_grid_share(share)
         f.invalidate()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    _native.batch_compute(fems, loops=args.sweep_loops, threads=threads)
+    try:
+        _native.batch_compute(fems, loops=args.sweep_loops, threads=threads)
+    except _native.ComputationError:  # every solve has run; the runaway ones are counted above
+        pass
     torch.cuda.synchronize()
     t_bat = time.perf_counter() - t0
     # solves that did not settle within the loop cap (thermal runaway) follow different
@@ -559,7 +567,8 @@ def run_sweep(args):
                                f"source power 1e15..1e16 W/m^3, at most {args.sweep_loops} outer loops per solve",
                    "algorithm": args.algorithm},
         "one_at_a_time": {"solves_per_s": len(fems) / t_seq, "seconds": t_seq, "cg_iterations": iters,
-                          "solves_not_within_maxerr": len(unconverged)},
+                          "solves_not_within_maxerr": len(unconverged),
+                          "solves_broken_down": len(failed)},
         "batched": {"seconds": t_bat, "threads": threads, "grid_share": share,
                     "speedup_vs_one_at_a_time": t_seq / t_bat},
         "tuner_trials_solves_per_s": [float(v) for v in trials],
